@@ -1,0 +1,160 @@
+/*
+ * sevc.h — C ABI of the GB300 vertex-model grain-growth engine.
+ *
+ * The reference (tclaudioe/SE-grain-growth-GPU) has no library API: its
+ * drop-in contract is the executable `SEVC -c file.ini`, its .ini keys,
+ * its four input files and its `DATA/%06d.txt` snapshots.  Inside that
+ * executable the hot path is the body of the main loop (src/main.cu:120-394)
+ * operating on device arrays.  Each entry point below replaces one piece
+ * of that program; the citation on each says which.  The `sevc` CLI in
+ * se-grain-growth-gpu_gb300/cli is the drop-in executable built on them.
+ *
+ * Conventions: plain C types only; every call returns an sevc_status;
+ * host buffers are owned by the caller; device memory is owned by the
+ * handle; one handle = one CUDA stream on the current device; a handle is
+ * not thread-safe.  There is no CPU fallback: without a CUDA device every
+ * compute call returns SEVC_ERR_CUDA.
+ */
+#ifndef SEVC_H
+#define SEVC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEVC_MAX_VRT_PER_GRN 100 /* src/geometry.h:9 */
+
+typedef enum sevc_status {
+    SEVC_OK = 0,
+    SEVC_ERR_IO = 1,           /* a file could not be opened/written        */
+    SEVC_ERR_PARSE = 2,        /* malformed input file or option            */
+    SEVC_ERR_CAPACITY = 3,     /* a grain list would exceed 100 vertices    */
+    SEVC_ERR_NONCONVERGED = 4, /* polling loop hit its iteration cap        */
+    SEVC_ERR_TOPOLOGY = 5,     /* inconsistent mesh met by an event kernel  */
+    SEVC_ERR_CUDA = 6,         /* CUDA runtime error / no device            */
+    SEVC_ERR_ARG = 7           /* invalid argument                           */
+} sevc_status;
+
+/* struct options, src/options.h:15-46, plus the stop threshold that the
+ * reference hard-codes at src/main.cu:49. */
+typedef struct sevc_options {
+    double dt, dtau;
+    int nucleation_gap;
+    double tmax;
+    int nmax, snap_gap;
+    double leave_percent;
+    int n_grains;
+    char vertex_fname[256], boundary_fname[256], orientation_fname[256], SE_fname[256];
+    double GB_eps, GB_scaling, SE_eps, SE_min, SE_max, nucleation_scaling, domain_bound;
+    int do_nucleation;
+    double MC_k;
+    int n_blocks, n_threads, debug_lvl;
+    char output_folder[256];
+    int min_grains; /* stop when fewer grains remain; <=0 disables.  The
+                       reference always uses 5000 (src/main.cu:49). */
+} sevc_options;
+
+/* Host mirror of the mesh, structure-of-arrays, entity = index, -1 = NULL.
+ * Field meanings follow src/geometry.h:39-86. */
+typedef struct sevc_mesh_host {
+    int nv, nb, ng;
+    double *px, *py, *vx, *vy, *venergy;
+    double *vel_bnd_x, *vel_grn_x, *vel_bnd_y, *vel_grn_y;
+    uint8_t *ven;
+    int32_t *vb;    /* 3 per vertex */
+    int32_t *vg;    /* 3 per vertex */
+    int32_t *bini, *bend;
+    double *benergy, *blen, *btext;
+    uint8_t *ben, *bcand;
+    int32_t *glist; /* 100 per grain */
+    int32_t *gvlen;
+    double *garea, *gdadt, *gori, *gse;
+    uint8_t *gen, *gtype;
+} sevc_mesh_host;
+
+/* What one loop iteration did (src/main.cu:121-325). */
+typedef struct sevc_step_info {
+    int n;                     /* iteration index of the step just run       */
+    double t;                  /* its time n*dt                              */
+    int curr_n_grains;         /* src/main.cu:317                            */
+    double nucleated_area;     /* src/main.cu:321 (percent of domain)        */
+    int export_due;            /* src/main.cu:328 condition                  */
+    int keep_going;            /* src/main.cu:120 and :391 after n++         */
+    int polling_iters;         /* iterations of src/topological.h:555        */
+    int n_two_three_iters;     /* passes of src/main.cu:227-250              */
+    int two_three_counts[20];  /* the count printed by each pass             */
+    int n_flips, n_removals, n_two_three, n_nucleations;
+    int nucleation_attempted;  /* src/main.cu:141 condition was true         */
+    int nucleation_candidate;  /* vertex id kept by the Metropolis test, -1  */
+    double gpu_ms;             /* device time of the step (CUDA events)      */
+} sevc_step_info;
+
+typedef struct sevc_handle sevc_handle;
+
+/* Defaults of src/options.h:71-85 (min_grains = 5000 as src/main.cu:49). */
+sevc_status sevc_default_options(sevc_options *opt);
+/* load_config_file, src/options.h:69-206 (same keys and parsing quirks). */
+sevc_status sevc_load_ini(const char *path, sevc_options *opt);
+
+/* load_from_files + host_to_device, src/io.h:66-264 and
+ * src/translation.h:140-155: read the four input files named in `opt`,
+ * build grains by face traversal, and upload the mesh. */
+sevc_status sevc_create(const sevc_options *opt, sevc_handle **out);
+/* Same from in-memory arrays: nv positions in [0,1) (xy interleaved),
+ * nb ridges (pairs), ng orientations in [0,1) and stored energies. */
+sevc_status sevc_create_from_arrays(const sevc_options *opt, int nv, const double *xy, int nb,
+                                    const int32_t *ridges, int ng, const double *oris,
+                                    const double *se, sevc_handle **out);
+void sevc_destroy(sevc_handle *h);
+/* load_from_files alone (src/io.h:66-264), on the host, no GPU needed:
+ * call once with out == NULL to get the sizes, then with caller arrays. */
+sevc_status sevc_load_mesh_host(const sevc_options *opt, sevc_mesh_host *out, int *nv, int *nb, int *ng);
+
+/* One iteration of the loop body src/main.cu:121-389: geometry refresh,
+ * optional nucleation, finite-difference velocities, extinction times,
+ * polling, conflicts, 2x3 and 3-sided removal, T1 flips, grain-list
+ * fix-ups, position update, grain count and nucleated area; then n++ and
+ * t = n*dt.  `info` (may be NULL) describes the step that ran. */
+sevc_status sevc_step(sevc_handle *h, sevc_step_info *info);
+/* Run `nsteps` iterations back to back without per-step host reads of the
+ * step counters (stops early on the stop criterion).  `done` = steps run. */
+sevc_status sevc_run_steps(sevc_handle *h, int nsteps, int *done, sevc_step_info *last);
+/* Loop condition of src/main.cu:120 for the current state. */
+int sevc_should_continue(const sevc_handle *h);
+
+/* export_data, src/io.h:280-377: write one snapshot with the reference's
+ * exact text format; `time` is printed as TIME. */
+sevc_status sevc_export_text(sevc_handle *h, const char *path, double time);
+/* device_to_host, src/translation.h:184-199 (without freeing anything):
+ * copy the mesh into caller-owned arrays sized like sevc_mesh_sizes. */
+sevc_status sevc_get_state(sevc_handle *h, sevc_mesh_host *out);
+sevc_status sevc_mesh_sizes(const sevc_handle *h, int *nv, int *nb, int *ng);
+/* check_data, src/utils.h:85-336: number of violated invariants (>= 0). */
+sevc_status sevc_check_data(sevc_handle *h, int *n_bad);
+
+/* The whole program of src/main.cu:21-424 after option loading: create
+ * DATA folder, load, loop with snapshots and the reference's log lines.
+ * `log` (may be NULL) receives stdout-style lines. */
+sevc_status sevc_run_program(const sevc_options *opt, int verbose);
+
+/* The reference seeds 8192 cuRAND XORWOW states with curand_init(32, tid,
+ * 0) (src/nucleation2.cu:12-16) and draws curand_uniform_double.  This
+ * records the first `ndraws` draws of streams 0..nstreams-1 into `out`
+ * (stream-major), for replay by an independent checker. */
+sevc_status sevc_rng_record(int nstreams, int ndraws, double *out);
+
+/* Per-kernel device time accumulated while profiling is on (CUDA events
+ * around each launch on the handle's stream). */
+sevc_status sevc_set_profiling(sevc_handle *h, int on);
+sevc_status sevc_get_profile(sevc_handle *h, int max_entries, char (*names)[48], double *ms,
+                             int64_t *launches, int *n_entries);
+
+/* Text of the last error on this thread. */
+const char *sevc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -11,6 +11,7 @@
  *   SEVC_REF_RNG_NDRAWS   draws per stream in that file
  *   SEVC_REF_QUIET        silence printf
  */
+#include <setjmp.h>
 #include <ucontext.h>
 #include <cstdarg>
 #include <cstdint>
@@ -29,8 +30,12 @@ int sevc_ref_main(int argc, char const *argv[]);
 
 /* ---------------- kernel launch emulation ---------------- */
 namespace {
-struct Fiber { ucontext_t ctx; std::vector<char> stack; bool done; };
-ucontext_t g_sched;
+/* Fibers start once through makecontext/swapcontext; afterwards every
+ * switch uses _setjmp/_longjmp, which do not touch the signal mask (no
+ * system call per barrier). */
+struct Fiber { ucontext_t ctx; jmp_buf jb; std::vector<char> stack; bool done, started; };
+jmp_buf g_sched_jb;
+ucontext_t g_boot;
 Fiber *g_cur = nullptr;
 bool g_fiber_mode = false;
 const std::function<void()> *g_body = nullptr;
@@ -40,7 +45,7 @@ void fiber_entry()
 {
     (*g_body)();
     g_cur->done = true;
-    swapcontext(&g_cur->ctx, &g_sched);
+    _longjmp(g_sched_jb, 1);
 }
 
 /* kernels of the reference that synchronise their block
@@ -57,7 +62,7 @@ bool uses_barrier(const char *name)
 void sevc_syncthreads()
 {
     if (!g_fiber_mode) { fprintf(stderr, "sevc_ref: __syncthreads outside a barrier kernel\n"); abort(); }
-    swapcontext(&g_cur->ctx, &g_sched);
+    if (!_setjmp(g_cur->jb)) _longjmp(g_sched_jb, 1);
 }
 
 void sevc_launch(const char *name, unsigned int grid, unsigned int block, const std::function<void()> &body)
@@ -85,6 +90,7 @@ void sevc_launch(const char *name, unsigned int grid, unsigned int block, const 
         for (unsigned t = 0; t < block; t++) {
             Fiber &f = g_pool[t];
             f.done = false;
+            f.started = false;
             getcontext(&f.ctx);
             f.ctx.uc_stack.ss_sp = f.stack.data();
             f.ctx.uc_stack.ss_size = f.stack.size();
@@ -99,7 +105,10 @@ void sevc_launch(const char *name, unsigned int grid, unsigned int block, const 
                 if (f.done) continue;
                 threadIdx = { t, 0, 0 };
                 g_cur = &f;
-                swapcontext(&g_sched, &f.ctx);
+                if (!_setjmp(g_sched_jb)) {
+                    if (!f.started) { f.started = true; swapcontext(&g_boot, &f.ctx); }
+                    else _longjmp(f.jb, 1);
+                }
                 if (!f.done) alive = true;
             }
         }

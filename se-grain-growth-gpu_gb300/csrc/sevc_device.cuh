@@ -1,0 +1,171 @@
+/*
+ * Device-side mesh layout and exact periodic geometry.
+ *
+ * Layout (structure of arrays, entity = int32 index, -1 = NULL):
+ *   vertex   pos/vel double2, terms double4 (finite-difference energy
+ *            terms, kept raw), energy double, enabled u8, boundaries int4
+ *            (x,y,z used), grains int4, mods int4[4] (grn, vrt, prev, fix)
+ *   boundary ends int2 (ini, end), energy/arclength/t_ext double,
+ *            enabled/candidate/candidate-buffer u8, votes/conflict int
+ *   grain    list int32[100] row-major, vlen int32, area/dAdt/orientation/
+ *            stored-energy double, enabled/candidate/fix/type u8
+ * Field meanings follow src/geometry.h:39-86 of the reference.
+ *
+ * Arithmetic: every helper restates the reference's expression tree
+ * operation by operation.  The library is compiled with -fmad=false, so no
+ * multiply-add is fused and results equal the reference semantics computed
+ * in IEEE binary64 without contraction.
+ */
+#ifndef SEVC_DEVICE_CUH
+#define SEVC_DEVICE_CUH
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define SEVC_MAXV 100
+#define SEVC_GRAD_EPS_D 1e-8          /* src/calculus.h:7 */
+#define SEVC_MAX_T_EXT_D 100000.0     /* src/geometry.h:11 */
+
+enum { FIX_ADD = 0, FIX_REMOVE = 1, FIX_REPLACE = 2, FIX_NONE = 3 }; /* src/geometry.h:17 */
+enum { GT_COMMON = 0, GT_NUCLEATED = 1 };                            /* src/geometry.h:19 */
+
+/* error bits raised by kernels (read back once per step) */
+enum {
+    ERRB_CAPACITY = 1,
+    ERRB_TOPOLOGY = 2,
+    ERRB_RNG = 4,
+    ERRB_WORKLIST = 8,
+    ERRB_NONCONVERGED = 16
+};
+
+struct DevMesh {
+    int nv, nb, ng;
+    double D;            /* domain bound */
+    /* vertices */
+    double2 *pos, *vel;
+    struct alignas(16) FdTerms { double bx, gx, by, gy; } *terms; /* energy terms of src/calculus.h:59-69 */
+    double2 *contrib;    /* 3 per vertex: stored-energy FD term per grain slot */
+    double *venergy;
+    uint8_t *ven;
+    int4 *vb, *vg;
+    int4 *vmod;          /* 4 per vertex */
+    int *voted;
+    uint8_t *vmodmark;
+    /* boundaries */
+    int2 *bv;
+    double *benergy, *blen, *btext;
+    uint8_t *ben, *bcand, *bcandbuf;
+    int *bvotes, *bconf;
+    /* grains */
+    int *glist, *gvlen;
+    double *garea, *gdadt, *gori, *gse, *gq;
+    uint8_t *gen, *gcand, *gfix, *gtype;
+    /* worklists of the grain-list fix-up (src/topological.h:1209) */
+    int *fixlist, *nfix;
+    int *modlist, *nmod;
+    int *err;            /* ERRB_* bits */
+    int *evt;            /* event counters, EVT_* */
+};
+
+enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
+
+/* ---- periodic geometry, src/geometry.h:133-331 ---- */
+__device__ __forceinline__ double dmod(double a, double D)        /* dom_mod :133 */
+{
+    if (a < 0) return a + D;
+    else if (a >= D) return a - D;
+    return a;
+}
+__device__ __forceinline__ double wrapd(double dest, double orig, double D) /* wrap_dist :147 */
+{
+    double d = dest - orig;
+    if (d > +(D / 2.0)) return (d - D);
+    if (d < -(D / 2.0)) return (D + d);
+    return d;
+}
+__device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :217 */
+{
+    double ax = fabs(x), ay = fabs(y);
+    double p = fmax(ax, ay);
+    if (p == 0) return 0;
+    double q = fmin(ax, ay);
+    double r = q / p;
+    return p * sqrt(1.0 + r * r);
+}
+/* compute_arclength(a, b) = |delta_to(a, b)|, :328 */
+__device__ __forceinline__ double arclen(double2 a, double2 b, double D)
+{
+    return vmag(wrapd(a.x, b.x, D), wrapd(a.y, b.y, D));
+}
+/* boundary_energy_func, :548 */
+__device__ __forceinline__ double gb_energy(double d_alpha, double eps)
+{
+    return (1 + 0.5 * eps * (1 - pow(cos(4 * d_alpha), 3)));
+}
+
+/* compute_area (src/geometry.h:757-765, with adjust_origin_for_points
+ * :908-931) streamed over a grain list: point 0 becomes the origin,
+ * later points accumulate wrapped deltas, shoelace terms add in list
+ * order.  Slot `ps` (if >= 0) is replaced by position `pp`. */
+__device__ __forceinline__ double area_stream(const int *__restrict__ L, int n, const double2 *__restrict__ pos,
+                                              int ps, double2 pp, double D)
+{
+    double area = 0;
+    if (n > 0) {
+        double2 r0 = (ps == 0) ? pp : pos[L[0]];
+        double ax = 0, ay = 0, rx = r0.x, ry = r0.y;
+        for (int k = 1; k < n; k++) {
+            double2 r = (k == ps) ? pp : pos[L[k]];
+            double nx = ax + wrapd(r.x, rx, D);
+            double ny = ay + wrapd(r.y, ry, D);
+            area += ax * ny - ay * nx;
+            ax = nx; ay = ny; rx = r.x; ry = r.y;
+        }
+        area += ax * 0.0 - ay * 0.0; /* closing term with point 0 = (0, 0) */
+    }
+    area *= 0.5;
+    return area;
+}
+
+/* grains_intersect, src/geometry.h:837-848; returns count found */
+__device__ __forceinline__ int gintersect(int4 a, int4 b, int *out)
+{
+    int k = 0;
+    out[0] = -1; out[1] = -1;
+    int A[3] = { a.x, a.y, a.z }, B[3] = { b.x, b.y, b.z };
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            if (A[i] == B[j]) {
+                out[k++] = A[i];
+                if (k == 2) return k;
+            }
+    return k;
+}
+/* grains_union + grains_symdiff, src/geometry.h:863-898 */
+__device__ __forceinline__ void gsymdiff(int4 a, int4 b, int *out)
+{
+    int gic[2], gun[4];
+    gintersect(a, b, gic);
+    gun[0] = a.x; gun[1] = a.y; gun[2] = a.z; gun[3] = -1;
+    int B[3] = { b.x, b.y, b.z };
+    for (int i = 0; i < 3; i++)
+        if (B[i] != gun[0] && B[i] != gun[1] && B[i] != gun[2]) { gun[3] = B[i]; break; }
+    int k = 0;
+    out[0] = -1; out[1] = -1;
+    for (int i = 0; i < 4; i++)
+        if (gun[i] != gic[0] && gun[i] != gic[1]) {
+            out[k++] = gun[i];
+            if (k == 2) return;
+        }
+}
+
+__device__ __forceinline__ int slot3(int4 s, int i) { return i == 0 ? s.x : (i == 1 ? s.y : s.z); }
+__device__ __forceinline__ void set_slot3(int4 &s, int i, int v)
+{
+    if (i == 0) s.x = v; else if (i == 1) s.y = v; else s.z = v;
+}
+__device__ __forceinline__ int other_end(int2 e, int v) { return e.x == v ? e.y : e.x; }
+
+__device__ __forceinline__ void raise_err(const DevMesh &m, int bits) { atomicOr(m.err, bits); }
+
+#endif

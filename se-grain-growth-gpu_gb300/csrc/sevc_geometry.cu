@@ -1,0 +1,252 @@
+/*
+ * Geometry and kinetics kernels of one time step (src/calculus.h and
+ * src/topological.h:303-353 of the reference), one thread per entity.
+ *
+ * The finite-difference velocity (src/calculus.h:19-73,143-154) is split
+ * in two passes so that no thread re-reads another grain's polygon:
+ *   grain pass   for every grain: its area, and for every list slot p the
+ *                areas with that vertex moved by +eps in x and in y; the
+ *                stored-energy terms SE*(|A'|-|A|) are scattered to the
+ *                vertex's grain slot;
+ *   vertex pass  for every vertex: the three perturbed arclengths, the
+ *                boundary terms, the velocity, and the vertex energy.
+ * Both passes repeat the reference's arithmetic in the same order, so the
+ * results are the ones energy_diff computes.
+ */
+#include "sevc_internal.h"
+
+namespace {
+
+constexpr int TPB = 256;
+inline int nblk(int n) { return (n + TPB - 1) / TPB; }
+
+/* src/calculus.h:83-114 */
+__global__ void k_boundary_geometry(DevMesh m, double eps, double scaling)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.nb || !m.ben[b]) return;
+    int2 e = m.bv[b];
+    double2 a = m.pos[e.x], c = m.pos[e.y];
+    m.blen[b] = arclen(a, c, m.D);
+    double gamma;
+    if (eps == 0.0) {
+        /* 1 + 0.5*0*(1 - cos^3) is exactly 1 for every finite cosine */
+        gamma = 1.0 * scaling;
+    } else {
+        int gic[2];
+        if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) { raise_err(m, ERRB_TOPOLOGY); return; }
+        double d_alpha = m.gori[gic[0]] - m.gori[gic[1]];
+        gamma = gb_energy(d_alpha, eps) * scaling;
+    }
+    m.benergy[b] = gamma;
+}
+
+/* grain pass of the finite-difference velocity, see file comment;
+ * also compute_grain_areas (src/calculus.h:224) and the per-grain part of
+ * vertex_compute_energy (src/geometry.h:476). */
+__global__ void k_grain_fd(DevMesh m)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= m.ng || !m.gen[g]) return;
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    double2 none = make_double2(0, 0);
+    double A = area_stream(L, n, m.pos, -1, none, m.D);
+    m.garea[g] = A;
+    double se = m.gse[g];
+    m.gq[g] = se * A / n;
+    double absA = fabs(A);
+    for (int p = 0; p < n; p++) {
+        int v = L[p];
+        double2 q = m.pos[v];
+        double2 px = make_double2(dmod(q.x + SEVC_GRAD_EPS_D, m.D), dmod(q.y, m.D));
+        double2 py = make_double2(dmod(q.x, m.D), dmod(q.y + SEVC_GRAD_EPS_D, m.D));
+        double Ax = area_stream(L, n, m.pos, p, px, m.D);
+        double Ay = area_stream(L, n, m.pos, p, py, m.D);
+        int4 sg = m.vg[v];
+        int j = sg.x == g ? 0 : (sg.y == g ? 1 : (sg.z == g ? 2 : -1));
+        if (j >= 0) m.contrib[3 * v + j] = make_double2(se * (fabs(Ax) - absA), se * (fabs(Ay) - absA));
+    }
+}
+
+/* vertex pass: src/calculus.h:19-73 (boundary part) and :143-154;
+ * vertex_compute_energy src/geometry.h:472-479 */
+__global__ void k_vertex_fd(DevMesh m)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m.nv || !m.ven[v]) return;
+    double2 p = m.pos[v];
+    int4 sb = m.vb[v], sg = m.vg[v];
+    double2 q[3];
+    double gam[3], len[3];
+    for (int j = 0; j < 3; j++) {
+        int b = slot3(sb, j);
+        q[j] = m.pos[other_end(m.bv[b], v)];
+        gam[j] = m.benergy[b];
+        len[j] = m.blen[b];
+    }
+    double2 cg[3];
+    for (int j = 0; j < 3; j++) cg[j] = m.contrib[3 * v + j];
+    DevMesh::FdTerms t;
+    double vel[2];
+    for (int c = 0; c < 2; c++) {
+        double2 np = p;
+        if (c == 0) np.x += SEVC_GRAD_EPS_D; else np.y += SEVC_GRAD_EPS_D;
+        np.x = dmod(np.x, m.D);
+        np.y = dmod(np.y, m.D);
+        double bt = 0.0, gt = 0.0;
+        for (int j = 0; j < 3; j++) {
+            double Lj = arclen(np, q[j], m.D);
+            bt += (gam[j] * (Lj - len[j]));
+            gt += (c == 0 ? cg[j].x : cg[j].y);
+        }
+        if (c == 0) { t.bx = bt; t.gx = gt; } else { t.by = bt; t.gy = gt; }
+        vel[c] = -(bt + gt) / SEVC_GRAD_EPS_D;
+    }
+    m.terms[v] = t;
+    m.vel[v] = make_double2(vel[0], vel[1]);
+    double e = 0.0;
+    for (int j = 0; j < 3; j++) {
+        int g = slot3(sg, j);
+        e += (len[j] * gam[j] * 0.5);
+        e += g >= 0 ? m.gq[g] : 0.0;
+    }
+    m.venergy[v] = e;
+}
+
+/* compute_grain_dAdts, src/calculus.h:243 with compute_dAdt
+ * src/geometry.h:779-787 streamed over the list */
+__global__ void k_grain_dadt(DevMesh m)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= m.ng || !m.gen[g]) return;
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    double d = 0;
+    if (n > 0) {
+        double2 r0 = m.pos[L[0]], v0 = m.vel[L[0]];
+        double ax = 0, ay = 0, rx = r0.x, ry = r0.y, vxk = v0.x, vyk = v0.y;
+        for (int k = 1; k < n; k++) {
+            double2 r = m.pos[L[k]], w = m.vel[L[k]];
+            double nx = ax + wrapd(r.x, rx, m.D);
+            double ny = ay + wrapd(r.y, ry, m.D);
+            d += (vxk * ny + ax * w.y);
+            d -= (vyk * nx + ay * w.x);
+            ax = nx; ay = ny; rx = r.x; ry = r.y; vxk = w.x; vyk = w.y;
+        }
+        d += (vxk * 0.0 + ax * v0.y);
+        d -= (vyk * 0.0 + ay * v0.x);
+    }
+    m.gdadt[g] = d;
+}
+
+/* compute_t_ext (src/topological.h:303-334) then label_boundaries
+ * (:343-353), which runs on every slot including disabled ones */
+__global__ void k_text_label(DevMesh m, double dt)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.nb) return;
+    double text = m.btext[b];
+    if (m.ben[b]) {
+        int2 e = m.bv[b];
+        double2 pi = m.pos[e.x], pe = m.pos[e.y];
+        double dx = 0.0 + wrapd(pe.x, pi.x, m.D);  /* adjust_origin_for_points on 2 points */
+        double dy = 0.0 + wrapd(pe.y, pi.y, m.D);
+        dx = dx - 0.0;
+        dy = dy - 0.0;
+        double norm = vmag(dx, dy);
+        double tx = 0, ty = 0;
+        if (norm != 0) {                            /* vector2_unitary, src/geometry.h:274 */
+            double ang = atan2(dy, dx);
+            tx = cos(ang);
+            ty = sin(ang);
+        }
+        double2 vi = m.vel[e.x], ve = m.vel[e.y];
+        double aux = tx * (ve.x - vi.x) + ty * (ve.y - vi.y);
+        text = (aux == 0) ? 100 : -norm / aux;
+        m.btext[b] = text;
+    }
+    m.bcand[b] = (text >= 0 && text <= dt) ? 1 : 0;
+    m.bconf[b] = -1;
+}
+
+/* compute_grain_areas, src/calculus.h:224 */
+__global__ void k_grain_area(DevMesh m)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= m.ng || !m.gen[g]) return;
+    double2 none = make_double2(0, 0);
+    m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
+}
+
+/* update_vertices_positions, src/calculus.h:391-404 */
+__global__ void k_update(DevMesh m, double dt)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m.nv || !m.ven[v]) return;
+    double2 p = m.pos[v], w = m.vel[v];
+    p.x += w.x * dt;
+    p.y += w.y * dt;
+    p.x = dmod(p.x, m.D);
+    p.y = dmod(p.y, m.D);
+    m.pos[v] = p;
+}
+
+/* current_n_grains (src/calculus.h:264-313): an integer count */
+__global__ void k_count_grains(DevMesh m, int *out)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = (g < m.ng && m.gen[g]) ? 1 : 0;
+    c = __syncthreads_count(c);
+    if (threadIdx.x == 0 && c) atomicAdd(out, c);
+}
+
+/* nucl_area_per_block (src/calculus.h:322-348): launched on the
+ * reference's grid so that the floating-point sum order is the same:
+ * per-thread strided partial sums, then the shared-memory tree. */
+__global__ void k_nucl_area_blocks(DevMesh m, double *block_out)
+{
+    __shared__ double t[256];
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    int stride = gridDim.x * blockDim.x;
+    double a = 0.0;
+    for (int g = tid; g < m.ng; g += stride)
+        if (m.gen[g] && m.gtype[g] == GT_NUCLEATED) a += m.garea[g];
+    t[threadIdx.x] = a;
+    __syncthreads();
+    for (int i = blockDim.x / 2; i != 0; i /= 2) {
+        if ((int)threadIdx.x < i) t[threadIdx.x] += t[threadIdx.x + i];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) block_out[blockIdx.x] = t[0];
+}
+
+/* host loop of nucleated_fraction_area, src/calculus.h:373-377 */
+__global__ void k_nucl_area_final(const double *block_out, int nblocks, double D, double *out)
+{
+    double s = 0.0;
+    for (int i = 0; i < nblocks; i++) s += block_out[i];
+    *out = 100 * s / (D * D);
+}
+
+} // namespace
+
+void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s)
+{
+    k_boundary_geometry<<<nblk(m.nb), TPB, 0, s>>>(m, eps, scaling);
+}
+void launch_grain_fd(const DevMesh &m, cudaStream_t s) { k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
+void launch_vertex_fd(const DevMesh &m, cudaStream_t s) { k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m); }
+void launch_grain_dadt(const DevMesh &m, cudaStream_t s) { k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m); }
+void launch_text_label(const DevMesh &m, double dt, cudaStream_t s) { k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt); }
+void launch_grain_area(const DevMesh &m, cudaStream_t s) { k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
+void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { k_update<<<nblk(m.nv), TPB, 0, s>>>(m, dt); }
+
+void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
+{
+    cudaMemsetAsync(x.counters + CTR_NGRAINS, 0, sizeof(int), s);
+    k_count_grains<<<nblk(m.ng), TPB, 0, s>>>(m, x.counters + CTR_NGRAINS);
+    k_nucl_area_blocks<<<p.n_blocks, p.n_threads, 0, s>>>(m, x.block_area);
+    k_nucl_area_final<<<1, 1, 0, s>>>(x.block_area, p.n_blocks, m.D,
+                                      reinterpret_cast<double *>(x.counters + CTR_NUCL_AREA_SLOT));
+}

@@ -1,0 +1,490 @@
+/*
+ * Host side of the engine, in C: .ini options (src/options.h:69-206),
+ * initial mesh construction (src/io.h:66-264), snapshot text
+ * (src/io.h:280-377) and the invariant checker (src/utils.h:85-336).
+ *
+ * These run on the CPU in the reference too; they are restated here so the
+ * engine accepts the same files and writes byte-identical snapshots.
+ * Compiled without FMA contraction so the boundary ordering angles
+ * (atan2 of wrapped deltas) match the reference's host build.
+ */
+#include "sevc_host.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+static __thread char g_err[512];
+
+void sevc_set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+const char *sevc_last_error(void) { return g_err; }
+
+/* ---------------------------------------------------------------- */
+/* options                                                           */
+/* ---------------------------------------------------------------- */
+sevc_status sevc_default_options(sevc_options *o)
+{
+    if (!o) return SEVC_ERR_ARG;
+    memset(o, 0, sizeof(*o));
+    o->tmax = -1;                 /* src/options.h:71-85 */
+    o->nmax = -1;
+    o->GB_eps = 0.02;
+    o->GB_scaling = 1.0;
+    o->SE_eps = 1.0;
+    o->SE_min = 999;
+    o->SE_max = 999;
+    o->MC_k = 1.0;
+    o->nucleation_scaling = 0.9;
+    o->domain_bound = 1.0;
+    o->do_nucleation = 1;
+    o->nucleation_gap = 1;
+    o->debug_lvl = 0;
+    o->leave_percent = -1;
+    o->n_blocks = 32;
+    o->n_threads = 256;
+    o->min_grains = 5000;         /* src/main.cu:49 */
+    return SEVC_OK;
+}
+
+static void chop_last(char *s)    /* fix_string, src/options.h:55 */
+{
+    size_t n = strlen(s);
+    if (n) s[n - 1] = '\0';
+}
+
+static void copy_name(char *dst, const char *val)
+{
+    snprintf(dst, 256, "%s", val);
+    chop_last(dst);
+}
+
+sevc_status sevc_load_ini(const char *path, sevc_options *o)
+{
+    sevc_default_options(o);
+    FILE *f = fopen(path, "r");
+    if (!f) { sevc_set_error("cannot open %s", path); return SEVC_ERR_IO; }
+    char line[1000], key[1000];
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '#' || line[0] == '[') continue;
+        char *eq = strchr(line, '=');
+        if (!eq) continue;
+        size_t k = (size_t)(eq - line);
+        memcpy(key, line, k);
+        key[k] = '\0';
+        const char *v = eq + 1;
+        /* keys compare without trimming, like src/options.h:103-106 */
+        if (!strcmp(key, "dt")) o->dt = atof(v);
+        else if (!strcmp(key, "dtau")) o->dtau = atof(v);
+        else if (!strcmp(key, "tmax")) o->tmax = atof(v);
+        else if (!strcmp(key, "nmax")) o->nmax = atoi(v);
+        else if (!strcmp(key, "snap_gap")) o->snap_gap = atoi(v);
+        else if (!strcmp(key, "leave_percent")) o->leave_percent = atof(v);
+        else if (!strcmp(key, "n_grains")) o->n_grains = atoi(v);
+        else if (!strcmp(key, "vertex_fname")) copy_name(o->vertex_fname, v);
+        else if (!strcmp(key, "boundary_fname")) copy_name(o->boundary_fname, v);
+        else if (!strcmp(key, "orientation_fname")) copy_name(o->orientation_fname, v);
+        else if (!strcmp(key, "SE_fname")) copy_name(o->SE_fname, v);
+        else if (!strcmp(key, "n_blocks")) o->n_blocks = atoi(v);
+        else if (!strcmp(key, "n_threads")) o->n_threads = atoi(v);
+        else if (!strcmp(key, "debug_lvl")) o->debug_lvl = atoi(v);
+        else if (!strcmp(key, "folder")) copy_name(o->output_folder, v);
+        else if (!strcmp(key, "GB_eps")) o->GB_eps = atof(v);
+        else if (!strcmp(key, "GB_scaling")) o->GB_scaling = atof(v);
+        else if (!strcmp(key, "SE_eps")) o->SE_eps = atof(v);
+        else if (!strcmp(key, "SE_min")) o->SE_min = atof(v);
+        else if (!strcmp(key, "SE_max")) o->SE_max = atof(v);
+        else if (!strcmp(key, "MC_k")) o->MC_k = atof(v);
+        else if (!strcmp(key, "nucleation_scaling")) o->nucleation_scaling = atof(v);
+        else if (!strcmp(key, "domain_bound")) o->domain_bound = atof(v);
+        else if (!strcmp(key, "do_nucleation")) o->do_nucleation = strcmp(v, "true\n") == 0;
+    }
+    fclose(f);
+    o->nucleation_gap = (int)(o->dtau / o->dt);  /* src/options.h:172 */
+    if (o->tmax > 0 && o->nmax == -1) {
+    } else if (o->tmax == -1 && o->nmax > 0) {
+    } else {
+        o->tmax = 1.0;
+        o->nmax = -1;
+    }
+    return SEVC_OK;
+}
+
+/* ---------------------------------------------------------------- */
+/* host mesh storage                                                 */
+/* ---------------------------------------------------------------- */
+int sevc_hmesh_alloc(sevc_hmesh *hm, int nv, int nb, int ng)
+{
+    memset(hm, 0, sizeof(*hm));
+    size_t V = (size_t)nv, B = (size_t)nb, G = (size_t)ng;
+    size_t bytes = 9 * V * 8 + V + 6 * V * 4 + 2 * B * 4 + 3 * B * 8 + 2 * B +
+                   (SEVC_MAX_VRT_PER_GRN + 1) * G * 4 + 4 * G * 8 + 2 * G + 64 * 8;
+    char *p = (char *)calloc(1, bytes);
+    if (!p) return SEVC_ERR_CAPACITY;
+    hm->block = p;
+    sevc_mesh_host *m = &hm->m;
+    m->nv = nv; m->nb = nb; m->ng = ng;
+#define TAKE(f, n, t) do { m->f = (t *)p; p += (n) * sizeof(t); } while (0)
+    TAKE(px, V, double); TAKE(py, V, double); TAKE(vx, V, double); TAKE(vy, V, double);
+    TAKE(venergy, V, double); TAKE(vel_bnd_x, V, double); TAKE(vel_grn_x, V, double);
+    TAKE(vel_bnd_y, V, double); TAKE(vel_grn_y, V, double);
+    TAKE(benergy, B, double); TAKE(blen, B, double); TAKE(btext, B, double);
+    TAKE(garea, G, double); TAKE(gdadt, G, double); TAKE(gori, G, double); TAKE(gse, G, double);
+    TAKE(vb, 3 * V, int32_t); TAKE(vg, 3 * V, int32_t);
+    TAKE(bini, B, int32_t); TAKE(bend, B, int32_t);
+    TAKE(glist, SEVC_MAX_VRT_PER_GRN * G, int32_t); TAKE(gvlen, G, int32_t);
+    TAKE(ven, V, uint8_t); TAKE(ben, B, uint8_t); TAKE(bcand, B, uint8_t);
+    TAKE(gen, G, uint8_t); TAKE(gtype, G, uint8_t);
+#undef TAKE
+    return SEVC_OK;
+}
+
+void sevc_hmesh_free(sevc_hmesh *hm)
+{
+    free(hm->block);
+    memset(hm, 0, sizeof(*hm));
+}
+
+/* ---------------------------------------------------------------- */
+/* mesh construction, src/io.h:66-264                                */
+/* ---------------------------------------------------------------- */
+static double wrapd(double dest, double orig, double D) /* src/geometry.h:147 */
+{
+    double d = dest - orig;
+    if (d > +(D / 2.0)) return (d - D);
+    if (d < -(D / 2.0)) return (D + d);
+    return d;
+}
+
+/* vertex_set_boundaries_clockwise, src/geometry.h:437-460: order the three
+ * boundaries by decreasing atan2 angle of the edge vector (three
+ * compare-swaps, stable on ties). */
+static void order_boundaries(sevc_mesh_host *m, int v, double D)
+{
+    int *s = &m->vb[3 * v];
+    double a[3];
+    for (int i = 0; i < 3; i++) {
+        int b = s[i];
+        int o = (m->bini[b] == v) ? m->bend[b] : m->bini[b];
+        a[i] = atan2(wrapd(m->py[o], m->py[v], D), wrapd(m->px[o], m->px[v], D));
+    }
+    static const int pairs[3][2] = { { 0, 1 }, { 1, 2 }, { 0, 1 } };
+    for (int k = 0; k < 3; k++) {
+        int i = pairs[k][0], j = pairs[k][1];
+        if (a[i] < a[j]) {
+            double t = a[i]; a[i] = a[j]; a[j] = t;
+            int tb = s[i]; s[i] = s[j]; s[j] = tb;
+        }
+    }
+}
+
+int sevc_host_build(const sevc_options *opt, int nv, const double *xy, int nb, const int *ridges,
+                    int n_ori, const double *oris, int n_se, const double *se, sevc_hmesh *out)
+{
+    int ng = opt->n_grains;
+    if (nv <= 0 || nb <= 0 || ng <= 0) { sevc_set_error("empty mesh"); return SEVC_ERR_PARSE; }
+    if (n_ori > ng || n_se > ng) { sevc_set_error("more orientations/SE values than grains"); return SEVC_ERR_PARSE; }
+    if (sevc_hmesh_alloc(out, nv, nb, ng)) { sevc_set_error("out of host memory"); return SEVC_ERR_CAPACITY; }
+    sevc_mesh_host *m = &out->m;
+    double D = opt->domain_bound;
+    for (int i = 0; i < nv; i++) {              /* init_vertex, src/geometry.h:346 */
+        m->px[i] = xy[2 * i] * D;
+        m->py[i] = xy[2 * i + 1] * D;
+        m->ven[i] = 1;
+        m->vb[3 * i] = m->vb[3 * i + 1] = m->vb[3 * i + 2] = -1;
+        m->vg[3 * i] = m->vg[3 * i + 1] = m->vg[3 * i + 2] = -1;
+    }
+    for (int b = 0; b < nb; b++) {              /* init_boundary, src/geometry.h:491 */
+        int a = ridges[2 * b], c = ridges[2 * b + 1];
+        if (a < 0 || a >= nv || c < 0 || c >= nv) { sevc_set_error("ridge %d out of range", b); goto bad; }
+        m->bini[b] = a;
+        m->bend[b] = c;
+        int ends[2] = { a, c };
+        for (int e = 0; e < 2; e++) {
+            int *s = &m->vb[3 * ends[e]];
+            if (s[0] < 0) s[0] = b; else if (s[1] < 0) s[1] = b; else if (s[2] < 0) s[2] = b;
+        }
+        m->btext[b] = SEVC_MAX_T_EXT;
+        m->ben[b] = 1;
+    }
+    for (int v = 0; v < nv; v++)
+        if (m->vb[3 * v] < 0 || m->vb[3 * v + 1] < 0 || m->vb[3 * v + 2] < 0) {
+            sevc_set_error("vertex %d has fewer than three boundaries", v);
+            goto bad;
+        }
+    for (int v = 0; v < nv; v++) order_boundaries(m, v, D);
+
+    {   /* face traversal, src/io.h:137-186 */
+        unsigned char *seen = (unsigned char *)calloc(3 * (size_t)nv, 1);
+        int ngr = 0;
+        for (int j = 0; j < nv && ngr >= 0; j++)
+            for (int side0 = 0; side0 < 3; side0++) {
+                if (seen[3 * j + side0]) continue;
+                if (ngr >= ng) { ngr = -1; break; }
+                int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * ngr];
+                int n = 0, cur = j, side = side0;
+                do {
+                    if (seen[3 * cur + side] || n >= SEVC_MAX_VRT_PER_GRN) { ngr = -2; break; }
+                    seen[3 * cur + side] = 1;
+                    L[n++] = cur;
+                    int b = m->vb[3 * cur + side];
+                    cur = (m->bini[b] == cur) ? m->bend[b] : m->bini[b];
+                    int i = 0;
+                    while (i < 3 && m->vb[3 * cur + i] != b) i++;
+                    if (i == 3) { ngr = -2; break; }
+                    side = (i + 1) % 3;
+                } while (cur != j);
+                if (ngr < 0) break;
+                for (int k = n; k < SEVC_MAX_VRT_PER_GRN; k++) L[k] = -1;
+                m->gvlen[ngr] = n;
+                m->gen[ngr] = 1;
+                ngr++;
+            }
+        free(seen);
+        if (ngr != ng) {
+            sevc_set_error("face traversal found %d grains, expected %d", ngr, ng);
+            goto bad;
+        }
+    }
+    for (int v = 0; v < nv; v++) {               /* src/io.h:189-192 */
+        order_boundaries(m, v, D);
+        int t = m->vb[3 * v + 1]; m->vb[3 * v + 1] = m->vb[3 * v]; m->vb[3 * v] = t;
+    }
+    for (int g = 0; g < ng; g++)                  /* src/io.h:196-200 */
+        for (int k = 0; k < m->gvlen[g]; k++) {
+            int *s = &m->vg[3 * m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * g + k]];
+            if (s[0] < 0) s[0] = g; else if (s[1] < 0) s[1] = g; else if (s[2] < 0) s[2] = g;
+        }
+    for (int g = 0; g < ng; g++) m->gori[g] = (g < n_ori ? oris[g] : 0.0) * 2 * M_PI; /* :214-218 */
+    for (int g = 0; g < ng; g++) m->gse[g] = g < n_se ? se[g] : 0.0;                   /* :223 */
+    if (opt->SE_min == 999 && opt->SE_max == 999) {                                    /* :228-248 */
+        for (int g = 0; g < ng; g++) m->gse[g] *= opt->SE_eps;
+    } else if (opt->SE_min == opt->SE_max) {
+        for (int g = 0; g < ng; g++) m->gse[g] = opt->SE_max * opt->SE_eps;
+    } else {
+        double slope = (opt->SE_max - opt->SE_min), shift = opt->SE_min;
+        for (int g = 0; g < ng; g++) m->gse[g] = slope * m->gse[g] + shift;
+    }
+    return SEVC_OK;
+bad:
+    sevc_hmesh_free(out);
+    return SEVC_ERR_PARSE;
+}
+
+static int slurp_numbers(const char *path, int per_line, int as_int, void **out, int *count)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) { sevc_set_error("cannot open %s", path); return SEVC_ERR_IO; }
+    size_t cap = 4096, n = 0, w = as_int ? sizeof(int) : sizeof(double);
+    char *buf = (char *)malloc(cap * w);
+    for (;;) {
+        int r;
+        if (as_int) {
+            int a, b;
+            r = fscanf(f, "%d %d\n", &a, &b);
+            if (r == EOF) break;
+            if (r != 2) goto parse_err;
+            if (n + 2 > cap) { cap *= 2; buf = (char *)realloc(buf, cap * w); }
+            ((int *)buf)[n++] = a;
+            ((int *)buf)[n++] = b;
+        } else if (per_line == 2) {
+            double a, b;
+            r = fscanf(f, "%lf %lf\n", &a, &b);
+            if (r == EOF) break;
+            if (r != 2) goto parse_err;
+            if (n + 2 > cap) { cap *= 2; buf = (char *)realloc(buf, cap * w); }
+            ((double *)buf)[n++] = a;
+            ((double *)buf)[n++] = b;
+        } else {
+            double a;
+            r = fscanf(f, "%lf\n", &a);
+            if (r == EOF) break;
+            if (r != 1) goto parse_err;
+            if (n + 1 > cap) { cap *= 2; buf = (char *)realloc(buf, cap * w); }
+            ((double *)buf)[n++] = a;
+        }
+    }
+    fclose(f);
+    *out = buf;
+    *count = (int)(n / (size_t)per_line);
+    return SEVC_OK;
+parse_err:
+    fclose(f);
+    free(buf);
+    sevc_set_error("malformed line in %s", path);
+    return SEVC_ERR_PARSE;
+}
+
+int sevc_host_load_files(const sevc_options *opt, sevc_hmesh *out)
+{
+    void *xy = NULL, *rd = NULL, *ori = NULL, *se = NULL;
+    int nv, nb, no, ns, rc;
+    if ((rc = slurp_numbers(opt->vertex_fname, 2, 0, &xy, &nv))) goto done;
+    if ((rc = slurp_numbers(opt->boundary_fname, 2, 1, &rd, &nb))) goto done;
+    if ((rc = slurp_numbers(opt->orientation_fname, 1, 0, &ori, &no))) goto done;
+    if ((rc = slurp_numbers(opt->SE_fname, 1, 0, &se, &ns))) goto done;
+    rc = sevc_host_build(opt, nv, (double *)xy, nb, (int *)rd, no, (double *)ori, ns, (double *)se, out);
+done:
+    free(xy); free(rd); free(ori); free(se);
+    return rc;
+}
+
+sevc_status sevc_load_mesh_host(const sevc_options *opt, sevc_mesh_host *out, int *nv, int *nb, int *ng)
+{
+    if (!opt) return SEVC_ERR_ARG;
+    sevc_hmesh hm;
+    int rc = sevc_host_load_files(opt, &hm);
+    if (rc) return (sevc_status)rc;
+    if (nv) *nv = hm.m.nv;
+    if (nb) *nb = hm.m.nb;
+    if (ng) *ng = hm.m.ng;
+    if (out) {
+        if (out->nv != hm.m.nv || out->nb != hm.m.nb || out->ng != hm.m.ng) {
+            sevc_hmesh_free(&hm);
+            sevc_set_error("output sizes do not match the mesh");
+            return SEVC_ERR_ARG;
+        }
+        size_t V = (size_t)hm.m.nv, B = (size_t)hm.m.nb, G = (size_t)hm.m.ng;
+#define CP(f, n) memcpy(out->f, hm.m.f, (n) * sizeof(*hm.m.f))
+        CP(px, V); CP(py, V); CP(vx, V); CP(vy, V); CP(venergy, V); CP(vel_bnd_x, V); CP(vel_grn_x, V);
+        CP(vel_bnd_y, V); CP(vel_grn_y, V); CP(ven, V); CP(vb, 3 * V); CP(vg, 3 * V); CP(bini, B); CP(bend, B);
+        CP(benergy, B); CP(blen, B); CP(btext, B); CP(ben, B); CP(bcand, B); CP(glist, SEVC_MAX_VRT_PER_GRN * G);
+        CP(gvlen, G); CP(garea, G); CP(gdadt, G); CP(gori, G); CP(gse, G); CP(gen, G); CP(gtype, G);
+#undef CP
+    }
+    sevc_hmesh_free(&hm);
+    return SEVC_OK;
+}
+
+/* ---------------------------------------------------------------- */
+/* snapshot text, src/io.h:280-377                                   */
+/* ---------------------------------------------------------------- */
+int sevc_host_export(const sevc_mesh_host *m, const sevc_options *o, const char *path, double time)
+{
+    FILE *f = fopen(path, "w");
+    if (!f) { sevc_set_error("cannot write %s", path); return SEVC_ERR_IO; }
+    setvbuf(f, NULL, _IOFBF, 1 << 22);
+    int cv = 0, cb = 0, cg = 0;
+    for (int i = 0; i < m->nv; i++) cv += m->ven[i] != 0;
+    for (int i = 0; i < m->nb; i++) cb += m->ben[i] != 0;
+    for (int i = 0; i < m->ng; i++) cg += m->gen[i] != 0;
+    fprintf(f, "TIME %.16f\nDELTA T %.16f\nDELTA TAU %.16f\nMAX TIME %.16f\nNUCLEATION %d\n", time, o->dt, o->dtau,
+            o->tmax, o->do_nucleation ? 1 : 0);
+    fprintf(f, "DOMAIN BOUND %.16f\nGB EPSILON %.16f\nGB SCALING %.16f\nSE EPSILON %.16f\nSE MIN %.16f\n",
+            o->domain_bound, o->GB_eps, o->GB_scaling, o->SE_eps, o->SE_min);
+    fprintf(f, "SE MAX %.16f\nNUCLEATION SCALING %.16f\nMAX VERTICES PER GRN %d\n", o->SE_max,
+            o->nucleation_scaling, SEVC_MAX_VRT_PER_GRN);
+    fprintf(f, "VERTICES %d\nBOUNDARIES %d\nGRAINS %d\nCURR VERTICES %d\nCURR BOUNDARIES %d\nCURR GRAINS %d\n",
+            m->nv, m->nb, m->ng, cv, cb, cg);
+    fputs("#VERTEX ENABLED ENERGY X Y VX VY VXbnd VXgrn VYbnd VYgrn VG1 G2 G3 N1 N2 N3\n", f);
+    for (int i = 0; i < m->nv; i++) {
+        const int *s = &m->vb[3 * i];
+        int nbr[3];
+        for (int j = 0; j < 3; j++)
+            nbr[j] = s[j] < 0 ? -1 : (m->bini[s[j]] == i ? m->bend[s[j]] : m->bini[s[j]]);
+        fprintf(f, "%d %d %.16f %.16f %.16f %.16f %.16f %.16f %.16f %.16f %.16f %d %d %d %d %d %d\n", i,
+                m->ven[i] ? 1 : 0, m->venergy[i], m->px[i], m->py[i], m->vx[i], m->vy[i], m->vel_bnd_x[i],
+                m->vel_grn_x[i], m->vel_bnd_y[i], m->vel_grn_y[i], m->vg[3 * i], m->vg[3 * i + 1],
+                m->vg[3 * i + 2], nbr[0], nbr[1], nbr[2]);
+    }
+    fputs("#BOUNDARY ENABLED INI END ENERGY ARCLEN EXTTIME CANDIDATE\n", f);
+    for (int i = 0; i < m->nb; i++)
+        fprintf(f, "%d %d %d %d %.16f %.16f %.16f %d\n", i, m->ben[i] ? 1 : 0, m->bini[i], m->bend[i],
+                m->benergy[i], m->blen[i], m->btext[i], m->bcand[i] ? 1 : 0);
+    fputs("#GRAIN ID ENABLED NUCLEATED ORIENT SE AREA dAdt VLEN VERTICES\n", f);
+    for (int i = 0; i < m->ng; i++) {
+        int n = m->gvlen[i];
+        fprintf(f, "%d %d %d %.16f %.16f %.16f %.16f %d ", i, m->gen[i] ? 1 : 0, (int)m->gtype[i], m->gori[i],
+                m->gse[i], m->garea[i], m->gdadt[i], n);
+        const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * i];
+        for (int j = 0; j < SEVC_MAX_VRT_PER_GRN; j++) {
+            if (j < n) fprintf(f, "%d ", L[j]);
+            else if (j == SEVC_MAX_VRT_PER_GRN - 1) fputs("-1", f);
+            else fputs("-1 ", f);
+        }
+        fputc('\n', f);
+    }
+    if (fclose(f)) { sevc_set_error("write error on %s", path); return SEVC_ERR_IO; }
+    return SEVC_OK;
+}
+
+/* ---------------------------------------------------------------- */
+/* invariants, src/utils.h:85-336 (the is_valid = false checks)      */
+/* ---------------------------------------------------------------- */
+static int two_common(const sevc_mesh_host *m, int a, int b, int *g0, int *g1)
+{
+    int k = 0, out[2] = { -1, -1 };
+    for (int i = 0; i < 3 && k < 2; i++)
+        for (int j = 0; j < 3 && k < 2; j++)
+            if (m->vg[3 * a + i] == m->vg[3 * b + j]) out[k++] = m->vg[3 * a + i];
+    *g0 = out[0];
+    *g1 = out[1];
+    return k;
+}
+
+static int in_list(const sevc_mesh_host *m, int g, int v)
+{
+    const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * g];
+    for (int i = 0; i < m->gvlen[g]; i++)
+        if (L[i] == v) return 1;
+    return 0;
+}
+
+int sevc_host_check(const sevc_mesh_host *m)
+{
+    int bad = 0;
+    for (int b = 0; b < m->nb; b++) {
+        if (!m->ben[b]) continue;
+        int a = m->bini[b], c = m->bend[b];
+        const int *sa = &m->vb[3 * a], *sc = &m->vb[3 * c];
+        bad += a == c;
+        bad += !m->ven[a] || !m->ven[c];
+        bad += sa[0] != b && sa[1] != b && sa[2] != b;
+        bad += sc[0] != b && sc[1] != b && sc[2] != b;
+        bad += !m->ben[sc[0]] || !m->ben[sc[1]] || !m->ben[sc[2]];
+        bad += !m->ben[sa[0]] || !m->ben[sa[1]] || !m->ben[sa[2]];
+        int g0, g1;
+        bad += two_common(m, a, c, &g0, &g1) < 2 || g0 == g1;
+    }
+    for (int v = 0; v < m->nv; v++) {
+        if (!m->ven[v]) continue;
+        const int *s = &m->vb[3 * v], *g = &m->vg[3 * v];
+        bad += s[0] == s[1] || s[1] == s[2] || s[2] == s[0];
+        bad += g[0] == g[1] || g[1] == g[2] || g[2] == g[0];
+        int nb[3];
+        for (int j = 0; j < 3; j++) {
+            bad += !m->ben[s[j]];
+            bad += g[j] < 0 || !m->gen[g[j]];
+            bad += m->bini[s[j]] == m->bend[s[j]];
+            nb[j] = m->bini[s[j]] == v ? m->bend[s[j]] : m->bini[s[j]];
+            bad += m->bini[s[j]] != v && m->bend[s[j]] != v;
+            bad += g[j] < 0 || !in_list(m, g[j], v);
+        }
+        bad += nb[0] == nb[1] || nb[1] == nb[2] || nb[2] == nb[0];
+    }
+    for (int gi = 0; gi < m->ng; gi++) {
+        if (!m->gen[gi]) continue;
+        const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * gi];
+        for (int j = 0; j < m->gvlen[gi]; j++) bad += !m->ven[L[j]];
+        for (int j = 0; j < m->gvlen[gi]; j++) {
+            const int *g = &m->vg[3 * L[j]];
+            if (g[0] != gi && g[1] != gi && g[2] != gi) { bad++; break; }
+        }
+        int cnt = 0;
+        for (int j = 0; j < SEVC_MAX_VRT_PER_GRN; j++) cnt += L[j] != -1;
+        bad += cnt != m->gvlen[gi];
+    }
+    return bad;
+}

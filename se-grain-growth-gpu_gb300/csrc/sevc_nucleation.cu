@@ -1,0 +1,368 @@
+/*
+ * Monte-Carlo nucleation (src/nucleation2.cu of the reference) with an
+ * exact replay of its random stream.
+ *
+ * The reference keeps 8192 cuRAND XORWOW states seeded with
+ * curand_init(32, tid, 0) (:12-16) and lets thread tid of its 32x256 grid
+ * consume, per attempt: 2 uniforms for every enabled vertex of its stride
+ * set (compute_nucleation_factor :262-263), 1 uniform if that set has an
+ * enabled vertex and, for thread 0 of each block, 1 more
+ * (get_vertex_id_per_block :315, :342), then state 0 draws 1 or 2 in
+ * get_vertex_id2 (:392, :421).
+ *
+ * Here the same states are kept and advanced by the same calls, but the
+ * triangle construction (two per vertex in the reference) is done only for
+ * the one vertex the selection picks: the vertex choice depends only on
+ * the enabled flags and the draws, never on the per-vertex energies.  The
+ * chosen vertex's two uniforms are regenerated from a copy of its stream
+ * taken before the attempt.
+ */
+#include "sevc_internal.h"
+
+#include <cmath>
+#include <vector>
+
+namespace {
+
+constexpr int NBLK = 32, NTHR = 256, GRID = NBLK * NTHR;
+
+__global__ void k_rng_init(curandState *st, int n)
+{
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < n) curand_init(32, tid, 0, &st[tid]);
+}
+
+__global__ void k_rng_draw(curandState *st, int n, int ndraws, double *out)
+{
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= n) return;
+    curandState s = st[tid];
+    for (int k = 0; k < ndraws; k++) out[(size_t)tid * ndraws + k] = curand_uniform_double(&s);
+    st[tid] = s;
+}
+
+/* compute_nucleation_factor's draws + get_vertex_id_per_block
+ * (src/nucleation2.cu:239-363), on the reference's 32x256 grid */
+__global__ void __launch_bounds__(NTHR) k_nucl_blocks(DevMesh m, curandState *rng, curandState *saved, int *buf)
+{
+    __shared__ int alive[NTHR], pick[NTHR];
+    int tid = blockIdx.x * NTHR + threadIdx.x;
+    curandState s = rng[tid];
+    saved[tid] = s;
+    int n_alive = 0;
+    for (int v = tid; v < m.nv; v += GRID) n_alive += m.ven[v] ? 1 : 0;
+    for (int k = 0; k < 2 * n_alive; k++) (void)curand_uniform_double(&s);
+    alive[threadIdx.x] = n_alive;
+    int rid = -1;
+    if (n_alive > 0) {
+        int n_steps = (int)(curand_uniform_double(&s) * (n_alive - 1));
+        int k = 0;
+        for (int v = tid; v < m.nv; v += GRID)
+            if (m.ven[v]) {
+                if (k == n_steps) { rid = v; break; }
+                k++;
+            }
+    }
+    pick[threadIdx.x] = rid;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int i = 0; i < NTHR; i++) tot += alive[i];
+        if (tot > 0) {
+            double p = curand_uniform_double(&s);
+            double pc = 0.0;
+            for (int i = 0; i < NTHR; i++) {
+                if (pick[i] != -1 && pc <= p && p < (pc + (alive[i] / (double)tot))) {
+                    pick[0] = pick[i];
+                    break;
+                }
+                pc += alive[i] / (double)tot;
+            }
+            buf[blockIdx.x] = pick[0];
+            buf[NBLK + blockIdx.x] = tot;
+        } else {
+            buf[blockIdx.x] = -1;
+            buf[NBLK + blockIdx.x] = 0;
+        }
+    }
+    rng[tid] = s;
+}
+
+struct NuclGeo {
+    double2 Apos, Bpos, Cpos;
+    int D, E, F, AD, AE, AF, g1, g2, g3;
+    double DeltaE;
+};
+
+/* 3-point compute_area (src/geometry.h:757) */
+__device__ double area3(double2 a, double2 b, double2 c, double D)
+{
+    double x1 = 0 + wrapd(b.x, a.x, D), y1 = 0 + wrapd(b.y, a.y, D);
+    double x2 = x1 + wrapd(c.x, b.x, D), y2 = y1 + wrapd(c.y, b.y, D);
+    double x0 = 0, y0 = 0;
+    double area = 0;
+    area += x0 * y1 - y0 * x1;
+    area += x1 * y2 - y1 * x2;
+    area += x2 * y0 - y2 * x0;
+    area *= 0.5;
+    return area;
+}
+
+/* generate_grain_for_nucleation, src/nucleation2.cu:116-212 */
+__device__ int gen_triangle(const DevMesh &m, int A, double nucl_r, double nucl_ori, double eps, double scaling,
+                            bool do_scale, NuclGeo &o)
+{
+    double D = m.D;
+    int4 sa = m.vb[A];
+    o.AD = sa.x; o.AE = sa.y; o.AF = sa.z;
+    o.D = other_end(m.bv[o.AD], A);
+    o.E = other_end(m.bv[o.AE], A);
+    o.F = other_end(m.bv[o.AF], A);
+    int gAD[2], gAE[2], gAF[2];
+    int4 ga = m.vg[A];
+    gintersect(ga, m.vg[o.D], gAD);
+    gintersect(ga, m.vg[o.E], gAE);
+    gintersect(ga, m.vg[o.F], gAF);
+    if (gAD[0] == gAE[0] || gAD[0] == gAE[1]) { o.g2 = gAD[0]; o.g1 = gAD[1]; }
+    else if (gAD[1] == gAE[0] || gAD[1] == gAE[1]) { o.g2 = gAD[1]; o.g1 = gAD[0]; }
+    else return -1;
+    if (gAE[0] == o.g2) o.g3 = gAE[1];
+    else if (gAE[1] == o.g2) o.g3 = gAE[0];
+    else return -1;
+    if (o.g1 < 0 || o.g2 < 0 || o.g3 < 0) return -1;
+    double2 pa = m.pos[A];
+    int far[3] = { o.D, o.E, o.F };
+    double2 out[3];
+    for (int k = 0; k < 3; k++) {
+        double2 q = m.pos[far[k]];
+        double tx = wrapd(q.x, pa.x, D), ty = wrapd(q.y, pa.y, D);
+        double w = nucl_r / vmag(tx, ty);
+        if (do_scale) w *= 0.99;
+        double2 r = make_double2(w * tx + pa.x, w * ty + pa.y);
+        r.x = dmod(r.x, D);
+        r.y = dmod(r.y, D);
+        out[k] = r;
+    }
+    o.Apos = out[0]; o.Bpos = out[1]; o.Cpos = out[2];
+    double LAB = arclen(o.Apos, o.Bpos, D), LBC = arclen(o.Bpos, o.Cpos, D), LCA = arclen(o.Cpos, o.Apos, D);
+    double A1 = area3(pa, o.Cpos, o.Apos, D);
+    double A2 = area3(pa, o.Apos, o.Bpos, D);
+    double A3 = area3(pa, o.Bpos, o.Cpos, D);
+    double E0 = 0.0, E1 = 0.0;
+    for (int i = 0; i < 3; i++) {
+        double gam = m.benergy[slot3(sa, i)];
+        if (do_scale) E0 += 0.99 * nucl_r * gam;
+        else E0 += nucl_r * gam;
+    }
+    E0 += A1 * m.gse[o.g1] + A2 * m.gse[o.g2] + A3 * m.gse[o.g3];
+    E1 = gb_energy(nucl_ori - m.gori[o.g1], eps) * scaling * LCA;
+    E1 += gb_energy(nucl_ori - m.gori[o.g2], eps) * scaling * LAB;
+    E1 += gb_energy(nucl_ori - m.gori[o.g3], eps) * scaling * LBC;
+    o.DeltaE = E1 - E0;
+    return 0;
+}
+
+__device__ void add_bnd_slot(const DevMesh &m, int v, int b)   /* vertex_add_boundary :385 */
+{
+    int4 s = m.vb[v];
+    if (s.x < 0) s.x = b; else if (s.y < 0) s.y = b; else if (s.z < 0) s.z = b;
+    m.vb[v] = s;
+}
+__device__ void add_grn_slot(const DevMesh &m, int v, int g)   /* vertex_add_grain :406 */
+{
+    int4 s = m.vg[v];
+    if (s.x < 0) s.x = g; else if (s.y < 0) s.y = g; else if (s.z < 0) s.z = g;
+    m.vg[v] = s;
+}
+__device__ bool list_add_after(const DevMesh &m, int g, int v, int prev) /* grain_add_vertex :629 */
+{
+    int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g], pos = -1;
+    for (int i = 0; i < n; i++)
+        if (L[i] == prev) { pos = i + 1; break; }
+    if (pos < 0 || n >= SEVC_MAXV) return false;
+    for (int i = n; i > pos; i--) L[i] = L[i - 1];
+    L[pos] = v;
+    m.gvlen[g] = n + 1;
+    return true;
+}
+__device__ void list_remove(const DevMesh &m, int g, int v)   /* grain_remove_vertex :653 */
+{
+    int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    for (int i = 0; i < n; i++)
+        if (L[i] == v) {
+            for (int j = i; j < n - 1; j++) L[j] = L[j + 1];
+            m.gvlen[g] = n - 1;
+            L[n - 1] = -1;
+            return;
+        }
+}
+__device__ void init_vertex_dev(const DevMesh &m, int v, double2 p) /* init_vertex :346 */
+{
+    m.pos[v] = p;
+    m.vel[v] = make_double2(0.0, 0.0);
+    m.venergy[v] = 0.0;
+    m.ven[v] = 1;
+    m.vg[v] = make_int4(-1, -1, -1, -1);
+    m.vb[v] = make_int4(-1, -1, -1, -1);
+    m.voted[v] = -1;
+    for (int j = 0; j < 4; j++) m.vmod[4 * (size_t)v + j] = make_int4(-1, -1, -1, FIX_NONE);
+}
+__device__ void init_boundary_dev(const DevMesh &m, int b, int ini, int end) /* init_boundary :491 */
+{
+    m.bv[b] = make_int2(ini, end);
+    add_bnd_slot(m, ini, b);
+    add_bnd_slot(m, end, b);
+    m.blen[b] = 0;
+    m.btext[b] = SEVC_MAX_T_EXT_D;
+    m.ben[b] = 1;
+    m.bcand[b] = 0;
+    m.bvotes[b] = 0;
+    m.bconf[b] = -1;
+}
+
+/* get_vertex_id2 (:375-443), the chosen vertex's factor
+ * (compute_nucleation_factor for that vertex), get_nucleation_ids (:33-72)
+ * and nucleate (:474-676) */
+__global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *saved, const int *buf, int *ctr,
+                              double eps, double scaling, double MC_k)
+{
+    int tot = 0;
+    for (int i = 0; i < NBLK; i++) tot += buf[NBLK + i];
+    curandState s0 = rng[0];
+    double p = curand_uniform_double(&s0);
+    double pc = 0.0, pn = 0.0;
+    int cand = ctr[CTR_CANDIDATE];
+    for (int i = 0; i < NBLK; i++) {
+        pn = ((double)buf[NBLK + i]) / tot;
+        if (buf[i] != -1 && pc < p && p <= (pc + pn)) { cand = buf[i]; break; }
+        pc += pn;
+    }
+    int v = cand;
+    if (v < 0 || v >= m.nv || !m.ven[v]) {
+        /* the reference would read a stale or out-of-range vertex here */
+        raise_err(m, ERRB_RNG);
+        ctr[CTR_CANDIDATE] = -1;
+        rng[0] = s0;
+        return;
+    }
+    /* the two draws compute_nucleation_factor made for v: v is the k-th
+     * enabled vertex of stream (v mod 8192) */
+    int t = v % GRID, k = 0;
+    for (int u = t; u < v; u += GRID) k += m.ven[u] ? 1 : 0;
+    curandState s = saved[t];
+    for (int j = 0; j < 2 * k; j++) (void)curand_uniform_double(&s);
+    double u1 = curand_uniform_double(&s);
+    double u2 = curand_uniform_double(&s);
+    int4 sb = m.vb[v];
+    double AL[3] = { m.blen[sb.x], m.blen[sb.y], m.blen[sb.z] };
+    double mn = AL[0];
+    for (int i = 0; i < 3; i++) if (mn > AL[i]) mn = AL[i];   /* min(), src/geometry.h:116 */
+    double nucl_r = 0.8 * mn * u1 + 0.1;
+    double nucl_ori = 2 * M_PI * u2;
+    NuclGeo o0, o1;
+    if (gen_triangle(m, v, nucl_r, nucl_ori, eps, scaling, false, o0) ||
+        gen_triangle(m, v, nucl_r, nucl_ori, eps, scaling, true, o1)) {
+        raise_err(m, ERRB_TOPOLOGY);
+        ctr[CTR_CANDIDATE] = -1;
+        rng[0] = s0;
+        return;
+    }
+    double DeltaE = o0.DeltaE, factor = o0.DeltaE - o1.DeltaE;
+    bool nucl = false;
+    if (DeltaE < 0) nucl = true;
+    else if (factor < 0) {
+        double q = curand_uniform_double(&s0);
+        double thr = exp(-MC_k * DeltaE);
+        if (q < thr) nucl = true; else cand = -1;
+    } else cand = -1;
+    ctr[CTR_CANDIDATE] = cand;
+    rng[0] = s0;
+    if (cand < 0 || !nucl) return;
+
+    /* get_nucleation_ids: lowest free slots */
+    int gfree = -1, bfree[3] = { -1, -1, -1 }, vfree[2] = { -1, -1 };
+    for (int i = 0; i < m.ng; i++) if (!m.gen[i]) { gfree = i; break; }
+    for (int i = 0, f = 0; i < m.nb && f < 3; i++) if (!m.ben[i]) bfree[f++] = i;
+    for (int i = 0, f = 0; i < m.nv && f < 2; i++) if (!m.ven[i]) vfree[f++] = i;
+    bool diff_vrt = vfree[0] != vfree[1];
+    bool diff_bnd = bfree[0] != bfree[1] && bfree[1] != bfree[2] && bfree[2] != bfree[0];
+    if (!diff_bnd || !diff_vrt || gfree == -1) return;      /* :496-499 */
+    if (vfree[1] < 0 || bfree[2] < 0) { raise_err(m, ERRB_CAPACITY); return; }
+
+    int A = v, B = vfree[0], C = vfree[1];
+    int AB = bfree[0], BC = bfree[1], CA = bfree[2], g = gfree;
+    /* the reference passes (scaling, eps) swapped here; only the unused
+     * energy changes */
+    NuclGeo o;
+    if (gen_triangle(m, A, nucl_r, nucl_ori, scaling, eps, true, o)) { raise_err(m, ERRB_TOPOLOGY); return; }
+    init_vertex_dev(m, B, o.Bpos);
+    init_vertex_dev(m, C, o.Cpos);
+    m.pos[A] = o.Apos;
+    m.vb[A] = make_int4(-1, -1, -1, -1);
+    init_boundary_dev(m, AB, A, B);
+    init_boundary_dev(m, BC, B, C);
+    init_boundary_dev(m, CA, C, A);
+    add_bnd_slot(m, A, o.AD);
+    int *L = m.glist + (size_t)SEVC_MAXV * g;              /* nucleate_grain :596 */
+    for (int i = 0; i < SEVC_MAXV; i++) L[i] = -1;
+    m.gvlen[g] = 0; m.garea[g] = 0; m.gse[g] = 0; m.gori[g] = 0;
+    m.gen[g] = 1; m.gcand[g] = 0; m.gfix[g] = 0; m.gtype[g] = GT_NUCLEATED;
+    m.gori[g] = nucl_ori;
+    L[0] = A; L[1] = B; L[2] = C;
+    m.gvlen[g] = 3;
+    int4 ga = m.vg[A];
+    if (ga.x == o.g3) ga.x = g; else if (ga.y == o.g3) ga.y = g; else if (ga.z == o.g3) ga.z = g;
+    m.vg[A] = ga;
+    add_grn_slot(m, B, g); add_grn_slot(m, B, o.g2); add_grn_slot(m, B, o.g3);
+    add_grn_slot(m, C, g); add_grn_slot(m, C, o.g3); add_grn_slot(m, C, o.g1);
+    bool ok = list_add_after(m, o.g1, C, A);
+    int2 ae = m.bv[o.AE];
+    if (ae.x == A) ok &= list_add_after(m, o.g2, B, ae.y);
+    else if (ae.y == A) ok &= list_add_after(m, o.g2, B, ae.x);
+    ok &= list_add_after(m, o.g3, C, A);
+    ok &= list_add_after(m, o.g3, B, C);
+    list_remove(m, o.g3, A);
+    if (!ok) raise_err(m, ERRB_TOPOLOGY);
+    int4 t4;
+    t4 = m.vb[B]; { int x = t4.y; t4.y = t4.x; t4.x = x; } m.vb[B] = t4;  /* vertex_invert_boundary_order */
+    t4 = m.vb[C]; { int x = t4.y; t4.y = t4.x; t4.x = x; } m.vb[C] = t4;
+    ae = m.bv[o.AE];
+    if (ae.x == A) ae.x = B; else if (ae.y == A) ae.y = B;
+    m.bv[o.AE] = ae;
+    t4 = m.vb[B]; t4.z = o.AE; m.vb[B] = t4;
+    int2 af = m.bv[o.AF];
+    if (af.x == A) af.x = C; else af.y = C;
+    m.bv[o.AF] = af;
+    t4 = m.vb[C]; t4.z = o.AF; m.vb[C] = t4;
+    m.evt[EVT_NUCLEATIONS]++;
+}
+
+} // namespace
+
+void launch_rng_init(curandState *st, int n, cudaStream_t s)
+{
+    k_rng_init<<<(n + 255) / 256, 256, 0, s>>>(st, n);
+}
+
+void launch_nucleation(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
+{
+    k_nucl_blocks<<<NBLK, NTHR, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf);
+    k_nucl_finish<<<1, 1, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf, x.counters, p.eps, p.scaling, p.MC_k);
+}
+
+int rng_record(int nstreams, int ndraws, double *host_out)
+{
+    curandState *st = nullptr;
+    double *d = nullptr;
+    size_t bytes = (size_t)nstreams * ndraws * sizeof(double);
+    if (cudaMalloc(&st, sizeof(curandState) * nstreams) != cudaSuccess) return 1;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) { cudaFree(st); return 1; }
+    k_rng_init<<<(nstreams + 255) / 256, 256>>>(st, nstreams);
+    k_rng_draw<<<(nstreams + 255) / 256, 256>>>(st, nstreams, ndraws, d);
+    cudaError_t e = cudaMemcpy(host_out, d, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(st);
+    cudaFree(d);
+    return e == cudaSuccess ? 0 : 1;
+}

@@ -1,0 +1,780 @@
+/*
+ * Topological transitions of one time step (src/topological.h of the
+ * reference): candidate compaction, the polling system, conflict
+ * resolution, removal of adjacent 3-sided pairs, 3-sided grain removal,
+ * T1 flips and the deferred grain-list edits.
+ *
+ * Candidates are gathered by an order-preserving warp-ballot compaction,
+ * so every later pass touches only the few boundaries and grains that can
+ * change.  Edits whose order is observable run in ascending index order,
+ * like the reference's single-thread kernels; the list edits
+ * (ADD -> REMOVE -> REPLACE) touch only the grain being edited and run one
+ * thread per grain, which gives the reference's serial result.
+ */
+#include "sevc_internal.h"
+
+namespace {
+
+constexpr int TPB = 256;
+constexpr int CT_ITEMS = 16;
+constexpr int CT_TILE = TPB * CT_ITEMS;
+constexpr int WL_BLOCKS = 152;
+
+/* ------------------------------------------------------------------ */
+/* grain-list primitives, src/geometry.h:614-734                       */
+/* ------------------------------------------------------------------ */
+__device__ int glist_find(const DevMesh &m, int g, int v)          /* grain_contains_vertex :703 */
+{
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    for (int i = 0; i < n; i++)
+        if (L[i] == v) return i;
+    return -1;
+}
+__device__ int glist_consecutive(const DevMesh &m, int g, int A, int B) /* :724 */
+{
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    for (int i = 0; i < n; i++) {
+        if (L[i] == A && L[(i + 1) % n] == B) return 1;
+        if (L[i] == B && L[(i + 1) % n] == A) return 2;
+    }
+    return -1;
+}
+__device__ void glist_add_after(const DevMesh &m, int g, int v, int prev) /* :629 */
+{
+    int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g], pos = -1;
+    for (int i = 0; i < n; i++)
+        if (L[i] == prev) { pos = i + 1; break; }
+    if (pos < 0) { raise_err(m, ERRB_TOPOLOGY); return; }
+    if (n >= SEVC_MAXV) { raise_err(m, ERRB_CAPACITY); return; }
+    for (int i = n; i > pos; i--) L[i] = L[i - 1];
+    L[pos] = v;
+    m.gvlen[g] = n + 1;
+}
+__device__ void glist_remove(const DevMesh &m, int g, int v)      /* :653 */
+{
+    int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    for (int i = 0; i < n; i++)
+        if (L[i] == v) {
+            for (int j = i; j < n - 1; j++) L[j] = L[j + 1];
+            m.gvlen[g] = n - 1;
+            L[n - 1] = -1;
+            return;
+        }
+}
+__device__ void glist_replace(const DevMesh &m, int g, int oldv, int newv) /* :686 */
+{
+    int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    for (int i = 0; i < n; i++)
+        if (L[i] == oldv) { L[i] = newv; return; }
+}
+
+/* queue a grain for the fix-up pass (grain.fix = true) */
+__device__ void mark_fix(const DevMesh &m, int g)
+{
+    if (m.gfix[g]) return;
+    m.gfix[g] = 1;
+    int i = atomicAdd(m.nfix, 1);
+    if (i < m.ng) m.fixlist[i] = g; else raise_err(m, ERRB_WORKLIST);
+}
+/* write a deferred edit into vertex v's mod slot (mod_t, src/geometry.h:26);
+ * prev < -1 keeps the slot's previous vrt_prev_id, as the reference does
+ * when it only assigns fix/vrt/grn */
+__device__ void set_mod(const DevMesh &m, int v, int slot, int fix, int grn, int vrt, int prev)
+{
+    int4 *md = m.vmod + 4 * (size_t)v + slot;
+    int4 x = *md;
+    x.x = grn; x.y = vrt; if (prev >= -1) x.z = prev; x.w = fix;
+    *md = x;
+    if (!m.vmodmark[v]) {
+        m.vmodmark[v] = 1;
+        int i = atomicAdd(m.nmod, 1);
+        if (i < m.nv) m.modlist[i] = v; else raise_err(m, ERRB_WORKLIST);
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* order-preserving compaction                                         */
+/* ------------------------------------------------------------------ */
+template <int KIND>
+__device__ __forceinline__ bool pred(const DevMesh &m, int i)
+{
+    if (KIND == CK_CAND) return m.ben[i] && m.bcand[i];
+    if (KIND == CK_GRAIN_CAND) return m.gen[i] && m.gcand[i];
+    if (KIND == CK_GVLEN3) return m.gvlen[i] == 3;
+    /* CK_TWO_THREE: enabled boundary whose two common grains both have
+     * three vertices (src/topological.h:31-35, :970-974) */
+    if (!m.ben[i]) return false;
+    int2 e = m.bv[i];
+    int gic[2];
+    if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) return false;
+    return m.gvlen[gic[0]] == 3 && m.gvlen[gic[1]] == 3;
+}
+
+template <int KIND>
+__global__ void k_compact_count(DevMesh m, int n, int *blockcnt)
+{
+    int base = blockIdx.x * CT_TILE, c = 0;
+    for (int k = 0; k < CT_ITEMS; k++) {
+        int i = base + k * TPB + threadIdx.x;
+        if (i < n && pred<KIND>(m, i)) c++;
+    }
+    __shared__ int s[TPB / 32];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < TPB / 32; w++) t += s[w];
+        blockcnt[blockIdx.x] = t;
+    }
+}
+
+template <int KIND>
+__global__ void k_compact_scatter(DevMesh m, int n, const int *blockcnt, int *out, int *n_out)
+{
+    __shared__ int s[TPB / 32 + 1];
+    __shared__ int base_off;
+    int part = 0;
+    for (int j = threadIdx.x; j < (int)blockIdx.x; j += TPB) part += blockcnt[j];
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < TPB / 32; w++) t += s[w];
+        base_off = t;
+    }
+    __syncthreads();
+    int off = base_off;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < CT_ITEMS; k++) {
+        int i = blockIdx.x * CT_TILE + k * TPB + threadIdx.x;
+        bool f = i < n && pred<KIND>(m, i);
+        unsigned bal = __ballot_sync(0xffffffffu, f);
+        __syncthreads();
+        if (lane == 0) s[warp] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int w = 0; w < TPB / 32; w++) { int t = s[w]; s[w] = acc; acc += t; }
+            s[TPB / 32] = acc;
+        }
+        __syncthreads();
+        if (f) out[off + s[warp] + __popc(bal & ((1u << lane) - 1))] = i;
+        off += s[TPB / 32];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *n_out = off;
+}
+
+/* ------------------------------------------------------------------ */
+/* polling system, src/topological.h:362-578                           */
+/* ------------------------------------------------------------------ */
+/* vertices_vote (:362) for the endpoints of listed boundaries */
+__global__ void k_poll_vote(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+    int2 e = m.bv[list[i]];
+    for (int k = 0; k < 2; k++) {
+        int v = k == 0 ? e.x : e.y;
+        if (!m.ven[v]) continue;
+        int4 sb = m.vb[v];
+        double mt = 99999999;
+        int am = 0;
+        for (int j = 0; j < 3; j++) {
+            int b = slot3(sb, j);
+            if (m.btext[b] <= mt && m.bcand[b]) { mt = m.btext[b]; am = j; }
+        }
+        m.voted[v] = slot3(sb, am);
+    }
+    }
+}
+/* count_boundaries_votes (:406) */
+__global__ void k_poll_count(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int b = list[i];
+        if (!(m.ben[b] && m.bcand[b])) continue;
+        int2 e = m.bv[b];
+        m.bvotes[b] = (m.voted[e.x] == b) + (m.voted[e.y] == b);
+    }
+}
+/* unlabel (:441).  A two-vote candidate is never adjacent to another
+ * two-vote candidate (their shared vertex votes once), so the parallel
+ * writes cannot change any thread's decision. */
+__global__ void k_poll_unlabel(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int b = list[i];
+        if (!(m.ben[b] && m.bcand[b] && m.bvotes[b] == 2)) continue;
+        int2 e = m.bv[b];
+        int4 si = m.vb[e.x], se = m.vb[e.y];
+        for (int j = 0; j < 3; j++) {
+            int x = slot3(si, j), y = slot3(se, j);
+            if (x != b) m.bcand[x] = 0;
+            if (y != b) m.bcand[y] = 0;
+        }
+    }
+}
+/* flips_per_block (:486-511) part one: a mismatch of boundary b marks
+ * grid thread (b mod grid) as failed; then write_candidate_results
+ * (:466-477) for the same element. */
+__global__ void k_poll_compare_write(DevMesh m, int *threadfail, int grid)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.nb) return;
+    uint8_t en = m.ben[b], c = m.bcand[b];
+    if (en && c != m.bcandbuf[b]) threadfail[b % grid] = 1;
+    m.bcandbuf[b] = en ? c : 0;
+}
+/* part two, on the reference's grid: per thread AND over its stride set
+ * (already folded into threadfail), per block the shared-memory tree
+ * whose bool += acts as OR, then AND over blocks (compare_candidates
+ * :526-537). */
+__global__ void k_poll_final(int *threadfail, int *converged)
+{
+    __shared__ int t[256];
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    t[threadIdx.x] = threadfail[tid] ? 0 : 1;
+    threadfail[tid] = 0;
+    __syncthreads();
+    for (int i = blockDim.x / 2; i != 0; i /= 2) {
+        if ((int)threadIdx.x < i) t[threadIdx.x] = (t[threadIdx.x] || t[threadIdx.x + i]) ? 1 : 0;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && !t[0]) atomicAnd(converged, 0);
+}
+
+/* ------------------------------------------------------------------ */
+/* conflicts, src/topological.h:83-155                                 */
+/* ------------------------------------------------------------------ */
+__device__ void conflict_check_one(const DevMesh &m, int b)
+{
+    if (!(m.ben[b] && !m.bcand[b])) return;
+    int2 e = m.bv[b];
+    int4 si = m.vb[e.x], se = m.vb[e.y];
+    int bi = -1, be = -1;
+    for (int j = 0; j < 3; j++) {
+        int x = slot3(si, j);
+        if (x != b && m.bcand[x]) { bi = x; break; }
+    }
+    for (int j = 0; j < 3; j++) {
+        int x = slot3(se, j);
+        if (x != b && m.bcand[x]) { be = x; break; }
+    }
+    if (bi >= 0 && be >= 0) {
+        double ti = m.btext[bi], te = m.btext[be];
+        int w;
+        if (ti == te) w = bi < be ? bi : be;
+        else w = ti < te ? bi : be;
+        m.bconf[b] = w;
+    }
+}
+/* check_conflictive_boundaries for every non-candidate boundary adjacent
+ * to a candidate (the only ones it can mark) */
+__global__ void k_conflict_check(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int c = list[i];
+        if (!(m.ben[c] && m.bcand[c])) continue;
+        int2 e = m.bv[c];
+        for (int k = 0; k < 2; k++) {
+            int4 s = m.vb[k == 0 ? e.x : e.y];
+            for (int j = 0; j < 3; j++) {
+                int b = slot3(s, j);
+                if (b != c) conflict_check_one(m, b);
+            }
+        }
+    }
+}
+__global__ void k_conflict_unlabel(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int b = list[i];
+        if (!(m.ben[b] && m.bcand[b])) continue;
+        int2 e = m.bv[b];
+        int4 si = m.vb[e.x], se = m.vb[e.y];
+        bool drop = false;
+        for (int j = 0; j < 3; j++) {
+            int x = slot3(si, j);
+            if (b != x && m.bconf[x] != -1) { if (m.bconf[x] != b) { drop = true; break; } }
+        }
+        for (int j = 0; j < 3; j++) {
+            int x = slot3(se, j);
+            if (b != x && m.bconf[x] != -1) { if (m.bconf[x] != b) { drop = true; break; } }
+        }
+        if (drop) m.bcand[b] = 0;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* removal of two adjacent 3-sided grains, src/topological.h:840-985   */
+/* ------------------------------------------------------------------ */
+/* remove_two_grains (:840-955); returns the rewired boundary CE or -1 */
+__device__ int remove_two_grains_dev(const DevMesh &m, int bnd, const int *gnic)
+{
+    int2 eb = m.bv[bnd];
+    int A = eb.x, B = eb.y;
+    int4 sa = m.vb[A], sbv = m.vb[B];
+    int AC = -1, BD = -1;
+    for (int i = 0; i < 3; i++) if (slot3(sa, i) == bnd) { AC = slot3(sa, (i + 1) % 3); break; }
+    for (int j = 0; j < 3; j++) if (slot3(sbv, j) == bnd) { BD = slot3(sbv, (j + 1) % 3); break; }
+    if (AC < 0 || BD < 0) { raise_err(m, ERRB_TOPOLOGY); return -1; }
+    int C = other_end(m.bv[AC], A);
+    int D = other_end(m.bv[BD], B);
+    int4 sc = m.vb[C], sd = m.vb[D];
+    int CE = -1, DF = -1;
+    for (int k = 0; k < 3; k++) if (slot3(sc, k) == AC) { CE = slot3(sc, (k + 2) % 3); break; }
+    for (int l = 0; l < 3; l++) if (slot3(sd, l) == BD) { DF = slot3(sd, (l + 2) % 3); break; }
+    if (CE < 0 || DF < 0) { raise_err(m, ERRB_TOPOLOGY); return -1; }
+    int F = other_end(m.bv[DF], D);
+    int2 ce = m.bv[CE];
+    if (ce.x == C) ce.x = F; else ce.y = F;
+    m.bv[CE] = ce;
+    int4 sf = m.vb[F];
+    for (int p = 0; p < 3; p++) if (slot3(sf, p) == DF) { set_slot3(sf, p, CE); break; }
+    m.vb[F] = sf;
+    if (gnic[0] < 0 || gnic[1] < 0) { raise_err(m, ERRB_TOPOLOGY); return -1; }
+    int G3, G4;
+    if (glist_find(m, gnic[0], A) >= 0) { G3 = gnic[0]; G4 = gnic[1]; } else { G3 = gnic[1]; G4 = gnic[0]; }
+    set_mod(m, A, 0, FIX_REMOVE, G3, A, -2); mark_fix(m, G3);
+    set_mod(m, A, 1, FIX_REMOVE, G3, C, -2);
+    set_mod(m, A, 2, FIX_REMOVE, G3, D, -2);
+    set_mod(m, B, 0, FIX_REMOVE, G4, B, -2); mark_fix(m, G4);
+    set_mod(m, B, 1, FIX_REMOVE, G4, C, -2);
+    set_mod(m, B, 2, FIX_REMOVE, G4, D, -2);
+    sa = m.vb[A]; sbv = m.vb[B];
+    for (int i = 0; i < 3; i++) { m.ben[slot3(sa, i)] = 0; m.ben[slot3(sbv, i)] = 0; }
+    m.ben[DF] = 0;
+    m.ben[bnd] = 0;
+    m.ven[A] = 0; m.ven[D] = 0; m.ven[C] = 0; m.ven[B] = 0;
+    return CE;
+}
+
+__device__ bool two_three_qualifies(const DevMesh &m, int b, int *gic)
+{
+    if (!m.ben[b]) return false;
+    int2 e = m.bv[b];
+    if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) return false;
+    return m.gvlen[gic[0]] == 3 && m.gvlen[gic[1]] == 3;
+}
+
+__device__ bool sorted_contains(const int *a, int lo, int hi, int x)
+{
+    int end = hi;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    return lo < end && a[lo] == x;
+}
+
+/* remove_two_grains_configurations (:965-985) is one thread scanning every
+ * boundary in index order.  Only listed boundaries (those qualifying at the
+ * count) and boundaries re-wired during the scan (CE) can qualify, so the
+ * scan visits exactly those, in index order, re-testing each on visit. */
+constexpr int EXTRA_CAP = 1024;
+__global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int *extra)
+{
+    int N = *n, i = 0, ne = 0;
+    while (i < N || ne > 0) {
+        int b;
+        if (ne > 0 && (i >= N || extra[0] < list[i])) {
+            b = extra[0];
+            for (int k = 1; k < ne; k++) extra[k - 1] = extra[k];
+            ne--;
+        } else {
+            b = list[i++];
+        }
+        int gic[2];
+        if (!two_three_qualifies(m, b, gic)) continue;
+        int2 e = m.bv[b];
+        int gnic[2];
+        gsymdiff(m.vg[e.x], m.vg[e.y], gnic);
+        int CE = remove_two_grains_dev(m, b, gnic);
+        m.gen[gic[0]] = 0;
+        m.gen[gic[1]] = 0;
+        m.evt[EVT_TWO_THREE]++;
+        if (CE > b && !sorted_contains(list, i, N, CE)) {
+            int g2[2];
+            if (two_three_qualifies(m, CE, g2)) {
+                bool dup = false;
+                for (int k = 0; k < ne; k++) dup |= extra[k] == CE;
+                if (!dup) {
+                    if (ne >= EXTRA_CAP) { raise_err(m, ERRB_WORKLIST); continue; }
+                    int k = ne++;
+                    while (k > 0 && extra[k - 1] > CE) { extra[k] = extra[k - 1]; k--; }
+                    extra[k] = CE;
+                }
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* 3-sided grain removal, src/topological.h:614-822, :994-1004         */
+/* ------------------------------------------------------------------ */
+/* clear_grains_state + label_3sided_grains for enabled grains */
+__global__ void k_label_3sided(DevMesh m, double dt)
+{
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= m.ng || !m.gen[g]) return;
+    uint8_t cand = 0;
+    if (m.gvlen[g] == 3) {
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        int l0 = L[0], l1 = L[1], l2 = L[2];
+        int ans = 0;
+        for (int i = 0; i < 3; i++) {
+            int4 s = m.vb[L[i]];
+            for (int k = 0; k < 3; k++) {
+                int b = slot3(s, k);
+                int2 e = m.bv[b];
+                bool ii = e.x == l0 || e.x == l1 || e.x == l2;
+                bool ee = e.y == l0 || e.y == l1 || e.y == l2;
+                if (ii && ee && m.bcand[b] && m.ben[b]) { cand = 1; break; }
+                double t = m.btext[b];
+                if (ii && ee && (t >= 0 && t <= dt) && m.ben[b]) ans++;
+            }
+        }
+        ans /= 2;
+        if (ans == 3) cand = 1;
+    }
+    m.gcand[g] = cand;
+}
+
+/* remove_grain (:687-822) */
+__device__ void remove_grain_dev(const DevMesh &m, int grn)
+{
+    const int *L = m.glist + (size_t)SEVC_MAXV * grn;
+    int A = L[0], B = L[1], C = L[2];
+    double D = m.D;
+    double2 pa = m.pos[A], pb = m.pos[B], pc = m.pos[C];
+    double nAB = arclen(pa, pb, D), nBC = arclen(pb, pc, D), nCA = arclen(pc, pa, D);
+    double denom = nAB + nBC + nCA;
+    double x0 = 0, y0 = 0;                                      /* adjust_origin_for_points, 3 points */
+    double x1 = x0 + wrapd(pb.x, pa.x, D), y1 = y0 + wrapd(pb.y, pa.y, D);
+    double x2 = x1 + wrapd(pc.x, pb.x, D), y2 = y1 + wrapd(pc.y, pb.y, D);
+    pa.x += (nBC * x0 + nCA * x1 + nAB * x2) / denom;
+    pa.y += (nBC * y0 + nCA * y1 + nAB * y2) / denom;
+    pa.x = dmod(pa.x, D);
+    pa.y = dmod(pa.y, D);
+    m.pos[A] = pa;
+    int gbc[2], gab[2], gac[2];
+    gintersect(m.vg[B], m.vg[C], gbc);
+    int G3 = gbc[0] == grn ? gbc[1] : gbc[0];
+    gintersect(m.vg[A], m.vg[B], gab);
+    int G2 = gab[0] == grn ? gab[1] : gab[0];
+    gintersect(m.vg[A], m.vg[C], gac);
+    int G1 = gac[0] == grn ? gac[1] : gac[0];
+    if (G1 < 0 || G2 < 0 || G3 < 0) { raise_err(m, ERRB_TOPOLOGY); return; }
+    m.vel[A] = make_double2(0.0, 0.0);
+    int4 sc = m.vb[C], sb = m.vb[B];
+    for (int i = 0; i < 3; i++) {
+        int x = slot3(sc, i);
+        int2 e = m.bv[x];
+        if ((e.x == B && e.y == C) || (e.y == B && e.x == C)) { m.ben[x] = 0; break; }
+    }
+    int BE = -1, CF = -1;
+    for (int i = 0; i < 3; i++) {
+        int x = slot3(sb, i);
+        int2 e = m.bv[x];
+        if (!(e.x == A || e.y == A) && !(e.x == C || e.y == C)) { BE = x; break; }
+    }
+    for (int i = 0; i < 3; i++) {
+        int x = slot3(sc, i);
+        int2 e = m.bv[x];
+        if (!(e.x == A || e.y == A) && !(e.x == B || e.y == B)) { CF = x; break; }
+    }
+    if (BE < 0 || CF < 0) { raise_err(m, ERRB_TOPOLOGY); return; }
+    int2 e;
+    e = m.bv[BE]; if (e.x == B) e.x = A; else e.y = A; m.bv[BE] = e;
+    e = m.bv[CF]; if (e.x == C) e.x = A; else e.y = A; m.bv[CF] = e;
+    int4 sa = m.vb[A];
+    for (int i = 0; i < 3; i++) {
+        int x = slot3(sa, i);
+        int2 f = m.bv[x];
+        if (f.x == B || f.y == B) { m.ben[x] = 0; set_slot3(sa, i, BE); break; }
+    }
+    for (int i = 0; i < 3; i++) {
+        int x = slot3(sa, i);
+        int2 f = m.bv[x];
+        if (f.x == C || f.y == C) { m.ben[x] = 0; set_slot3(sa, i, CF); break; }
+    }
+    m.vb[A] = sa;
+    m.ven[B] = 0;
+    m.ven[C] = 0;
+    m.gen[grn] = 0;
+    set_mod(m, B, 0, FIX_REMOVE, G2, B, -2); mark_fix(m, G2);
+    set_mod(m, C, 0, FIX_REMOVE, G1, C, -2); mark_fix(m, G1);
+    set_mod(m, B, 1, FIX_REMOVE, G3, B, -2); mark_fix(m, G3);
+    set_mod(m, C, 1, FIX_REPLACE, G3, A, C);
+    int4 ga = m.vg[A];
+    for (int i = 0; i < 3; i++) if (slot3(ga, i) == grn) set_slot3(ga, i, G3);
+    m.vg[A] = ga;
+}
+
+/* remove_grains (:994), launched <<<1,1>>> by the reference: grains in
+ * ascending index order */
+__global__ void k_remove_grains(DevMesh m, const int *list, const int *n)
+{
+    int N = *n;
+    for (int i = 0; i < N; i++) {
+        int g = list[i];
+        if (m.gen[g] && m.gcand[g]) {
+            remove_grain_dev(m, g);
+            m.evt[EVT_REMOVALS]++;
+        }
+    }
+}
+
+/* unlabel_boundaries_st2 (:588-606) */
+__global__ void k_unlabel_st2(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int b = list[i];
+        if (!(m.ben[b] && m.bcand[b])) continue;
+        int2 e = m.bv[b];
+        int gic[2];
+        if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) { raise_err(m, ERRB_TOPOLOGY); continue; }
+        if (m.gvlen[gic[0]] == 3 || m.gvlen[gic[1]] == 3) m.bcand[b] = 0;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* T1 flip, src/topological.h:174-291                                  */
+/* ------------------------------------------------------------------ */
+__device__ void flip_dev(const DevMesh &m, int bnd, double eps)
+{
+    int2 eb = m.bv[bnd];
+    int A = eb.x, B = eb.y;
+    int gic[2], gnic[2];
+    if (gintersect(m.vg[A], m.vg[B], gic) < 2) { raise_err(m, ERRB_TOPOLOGY); return; }
+    gsymdiff(m.vg[A], m.vg[B], gnic);
+    int4 sa = m.vb[A], sb = m.vb[B];
+    int i = -1, j = -1, AC = -1, BE = -1;
+    for (int k = 0; k < 3; k++) if (slot3(sa, k) == bnd) { i = (k + 1) % 3; AC = slot3(sa, i); break; }
+    for (int k = 0; k < 3; k++) if (slot3(sb, k) == bnd) { j = (k + 1) % 3; BE = slot3(sb, j); break; }
+    if (AC < 0 || BE < 0 || gnic[0] < 0 || gnic[1] < 0) { raise_err(m, ERRB_TOPOLOGY); return; }
+    set_slot3(sa, i, BE);
+    set_slot3(sb, j, AC);
+    m.vb[A] = sa;
+    m.vb[B] = sb;
+    int2 e = m.bv[AC]; if (e.x == A) e.x = B; else e.y = B; m.bv[AC] = e;
+    e = m.bv[BE]; if (e.x == B) e.x = A; else e.y = A; m.bv[BE] = e;
+    int g1, g2, g3, g4;
+    for (g2 = 0; g2 < 2; g2++)
+        if (glist_consecutive(m, gic[g2], A, B) == 1) { set_mod(m, A, 0, FIX_REMOVE, gic[g2], A, -2); mark_fix(m, gic[g2]); break; }
+    for (g4 = 0; g4 < 2; g4++)
+        if (glist_consecutive(m, gic[g4], B, A) == 1) { set_mod(m, B, 0, FIX_REMOVE, gic[g4], B, -2); mark_fix(m, gic[g4]); break; }
+    for (g3 = 0; g3 < 2; g3++)
+        if (glist_find(m, gnic[g3], A) >= 0) { set_mod(m, A, 1, FIX_ADD, gnic[g3], B, A); mark_fix(m, gnic[g3]); break; }
+    for (g1 = 0; g1 < 2; g1++)
+        if (glist_find(m, gnic[g1], B) >= 0) { set_mod(m, B, 1, FIX_ADD, gnic[g1], A, B); mark_fix(m, gnic[g1]); break; }
+    if (g1 == 2 || g2 == 2 || g3 == 2 || g4 == 2) { raise_err(m, ERRB_TOPOLOGY); return; }
+    int4 ga = m.vg[A], gb = m.vg[B];
+    for (int k = 0; k < 3; k++) {
+        if (slot3(ga, k) == gic[g2]) set_slot3(ga, k, gnic[g1]);
+        if (slot3(gb, k) == gic[g4]) set_slot3(gb, k, gnic[g3]);
+    }
+    m.vg[A] = ga;
+    m.vg[B] = gb;
+    double2 pa = m.pos[A], pb = m.pos[B];                 /* vector2_mean, src/geometry.h:311 */
+    double2 c = pa;
+    c.x += wrapd(pb.x, pa.x, m.D) / 2;
+    c.y += wrapd(pb.y, pa.y, m.D) / 2;
+    c.x = dmod(c.x, m.D);
+    c.y = dmod(c.y, m.D);
+    m.pos[A] = c;
+    m.pos[B] = c;
+    sa = m.vb[A]; { int t = sa.y; sa.y = sa.x; sa.x = t; } m.vb[A] = sa; /* vertex_invert_boundary_order */
+    sb = m.vb[B]; { int t = sb.y; sb.y = sb.x; sb.x = t; } m.vb[B] = sb;
+    /* boundary_compute_energy (no GB scaling here, as in the reference) */
+    if (eps == 0.0) {
+        m.benergy[bnd] = 1.0;
+    } else {
+        int g2c[2];
+        if (gintersect(m.vg[A], m.vg[B], g2c) < 2) { raise_err(m, ERRB_TOPOLOGY); return; }
+        m.benergy[bnd] = gb_energy(m.gori[g2c[0]] - m.gori[g2c[1]], eps);
+    }
+    m.vel[A] = make_double2(0, 0);
+    m.vel[B] = make_double2(0, 0);
+}
+
+/* apply_flippings (:1016-1026); flips that share no vertex commute, the
+ * rest are applied in ascending boundary order */
+__global__ void k_flips(DevMesh m, double eps, const int *list, const int *n)
+{
+    int N = *n;
+    for (int i = 0; i < N; i++) {
+        int b = list[i];
+        if (m.ben[b] && m.bcand[b]) {
+            flip_dev(m, b, eps);
+            m.evt[EVT_FLIPS]++;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* fix_grain_lists, src/topological.h:1035-1227                        */
+/* ------------------------------------------------------------------ */
+__global__ void k_fix_add(DevMesh m)
+{
+    int nf = *m.nfix;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
+        int g = m.fixlist[w];
+        if (!(m.gen[g] && m.gfix[g])) continue;
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        for (int i = 0; i < m.gvlen[g]; i++) {
+            int v = L[i];
+            for (int j = 0; j < 4; j++) {
+                int4 md = m.vmod[4 * (size_t)v + j];
+                if (md.w == FIX_ADD && md.x == g) glist_add_after(m, g, md.y, md.z);
+            }
+        }
+    }
+}
+__global__ void k_fix_remove(DevMesh m)
+{
+    int nf = *m.nfix;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
+        int g = m.fixlist[w];
+        if (!(m.gen[g] && m.gfix[g])) continue;
+        int snap[SEVC_MAXV];   /* the list as it was when the mod buffer was filled (:1088-1097) */
+        int n0 = m.gvlen[g];
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        for (int i = 0; i < n0; i++) snap[i] = L[i];
+        for (int i = 0; i < n0; i++)
+            for (int j = 0; j < 4; j++) {
+                int4 md = m.vmod[4 * (size_t)snap[i] + j];
+                if (md.w == FIX_REMOVE && md.x == g) glist_remove(m, g, md.y);
+            }
+    }
+}
+__global__ void k_fix_replace(DevMesh m)
+{
+    int nf = *m.nfix;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
+        int g = m.fixlist[w];
+        if (!(m.gen[g] && m.gfix[g])) continue;
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        for (int i = 0; i < m.gvlen[g]; i++) {
+            int v = L[i];
+            for (int j = 0; j < 4; j++) {
+                int4 md = m.vmod[4 * (size_t)v + j];
+                if (md.w == FIX_REPLACE && md.x == g) glist_replace(m, g, md.z, md.y);
+            }
+        }
+    }
+}
+/* clear_grains_fix_state (:1150-1163): fix = false for enabled grains and
+ * reset the mods of every vertex listed by an enabled grain.  Only queued
+ * grains can have fix set and only marked vertices can hold mods. */
+__global__ void k_fix_clear(DevMesh m)
+{
+    int nf = *m.nfix, nm = *m.nmod;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
+        int g = m.fixlist[w];
+        if (m.gen[g]) m.gfix[g] = 0;
+    }
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nm; w += gridDim.x * blockDim.x) {
+        int v = m.modlist[w];
+        m.vmodmark[v] = 0;
+        int4 sg = m.vg[v];
+        bool listed = false;
+        for (int j = 0; j < 3 && !listed; j++) {
+            int g = slot3(sg, j);
+            if (g >= 0 && m.gen[g] && glist_find(m, g, v) >= 0) listed = true;
+        }
+        if (listed)
+            for (int j = 0; j < 4; j++) m.vmod[4 * (size_t)v + j] = make_int4(-1, -1, -1, FIX_NONE);
+    }
+}
+__global__ void k_fix_reset(DevMesh m)
+{
+    *m.nfix = 0;
+    *m.nmod = 0;
+}
+
+template <int KIND>
+void compact_impl(const DevMesh &m, const DevScratch &x, int n, int *out, int *n_out, cudaStream_t s)
+{
+    int tiles = (n + CT_TILE - 1) / CT_TILE;
+    if (tiles == 0) { cudaMemsetAsync(n_out, 0, sizeof(int), s); return; }
+    k_compact_count<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt);
+    k_compact_scatter<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt, out, n_out);
+}
+
+inline int listgrid(int cap) { int g = (cap + TPB - 1) / TPB; return g < 4 * WL_BLOCKS ? g : 4 * WL_BLOCKS; }
+
+} // namespace
+
+void launch_compact(const DevMesh &m, const DevScratch &x, CompactKind kind, int *out, int *n_out, cudaStream_t s)
+{
+    switch (kind) {
+    case CK_CAND: compact_impl<CK_CAND>(m, x, m.nb, out, n_out, s); break;
+    case CK_TWO_THREE: compact_impl<CK_TWO_THREE>(m, x, m.nb, out, n_out, s); break;
+    case CK_GRAIN_CAND: compact_impl<CK_GRAIN_CAND>(m, x, m.ng, out, n_out, s); break;
+    case CK_GVLEN3: compact_impl<CK_GVLEN3>(m, x, m.ng, out, n_out, s); break;
+    }
+}
+
+void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *cand, const int *ncand,
+                           const StepParams &p, cudaStream_t s)
+{
+    int g = listgrid(m.nb);
+    k_poll_vote<<<g, TPB, 0, s>>>(m, cand, ncand);
+    k_poll_count<<<g, TPB, 0, s>>>(m, cand, ncand);
+    k_poll_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
+    int grid = p.n_blocks * p.n_threads;
+    int one = 1;
+    cudaMemcpyAsync(x.counters + CTR_CONVERGED, &one, sizeof(int), cudaMemcpyHostToDevice, s);
+    k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+    k_poll_final<<<p.n_blocks, p.n_threads, 0, s>>>(x.threadfail, x.counters + CTR_CONVERGED);
+}
+
+void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
+{
+    int g = listgrid(m.nb);
+    k_conflict_check<<<g, TPB, 0, s>>>(m, cand, ncand);
+    k_conflict_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
+}
+
+void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s)
+{
+    k_remove_two_three<<<1, 1, 0, s>>>(m, list, n, x.extra);
+}
+
+void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s)
+{
+    k_label_3sided<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, dt);
+}
+
+void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
+{
+    k_remove_grains<<<1, 1, 0, s>>>(m, list, n);
+}
+
+void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
+{
+    k_unlabel_st2<<<listgrid(m.nb), TPB, 0, s>>>(m, cand, ncand);
+}
+
+void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
+                  cudaStream_t s)
+{
+    (void)x;
+    k_flips<<<1, 1, 0, s>>>(m, eps, cand, ncand);
+}
+
+void launch_fix_lists(const DevMesh &m, cudaStream_t s)
+{
+    k_fix_add<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    k_fix_remove<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    k_fix_replace<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    k_fix_reset<<<1, 1, 0, s>>>(m);
+}

@@ -1,0 +1,228 @@
+"""Python binding of the engine's C ABI (include/sevc.h), over ctypes.
+
+This is a thin host-side mirror for tests, benchmarks and scripting: every
+call goes through libsevc.so, built in-tree by build.py.  There is no CPU
+fallback; importing works without a GPU, but every compute call raises
+SevcError when no CUDA device is present.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libsevc.so")
+MAXV = 100
+
+STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "CAPACITY", 4: "NONCONVERGED", 5: "TOPOLOGY", 6: "CUDA", 7: "ARG"}
+
+# every symbol include/sevc.h declares
+EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_from_arrays", "sevc_destroy", "sevc_load_mesh_host",
+           "sevc_step", "sevc_run_steps", "sevc_should_continue", "sevc_export_text", "sevc_get_state",
+           "sevc_mesh_sizes", "sevc_check_data", "sevc_run_program", "sevc_rng_record", "sevc_set_profiling",
+           "sevc_get_profile", "sevc_last_error"]
+
+
+class SevcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("sevc error %d (%s): %s" % (code, STATUS.get(code, "?"), msg))
+        self.code = code
+
+
+class Options(C.Structure):
+    """sevc_options (src/options.h:15-46 + min_grains)."""
+    _fields_ = [
+        ("dt", C.c_double), ("dtau", C.c_double), ("nucleation_gap", C.c_int), ("tmax", C.c_double),
+        ("nmax", C.c_int), ("snap_gap", C.c_int), ("leave_percent", C.c_double), ("n_grains", C.c_int),
+        ("vertex_fname", C.c_char * 256), ("boundary_fname", C.c_char * 256),
+        ("orientation_fname", C.c_char * 256), ("SE_fname", C.c_char * 256),
+        ("GB_eps", C.c_double), ("GB_scaling", C.c_double), ("SE_eps", C.c_double), ("SE_min", C.c_double),
+        ("SE_max", C.c_double), ("nucleation_scaling", C.c_double), ("domain_bound", C.c_double),
+        ("do_nucleation", C.c_int), ("MC_k", C.c_double), ("n_blocks", C.c_int), ("n_threads", C.c_int),
+        ("debug_lvl", C.c_int), ("output_folder", C.c_char * 256), ("min_grains", C.c_int),
+    ]
+
+
+_MESH_FIELDS = [
+    ("px", "v", np.float64), ("py", "v", np.float64), ("vx", "v", np.float64), ("vy", "v", np.float64),
+    ("venergy", "v", np.float64), ("vel_bnd_x", "v", np.float64), ("vel_grn_x", "v", np.float64),
+    ("vel_bnd_y", "v", np.float64), ("vel_grn_y", "v", np.float64), ("ven", "v", np.uint8),
+    ("vb", "v3", np.int32), ("vg", "v3", np.int32), ("bini", "b", np.int32), ("bend", "b", np.int32),
+    ("benergy", "b", np.float64), ("blen", "b", np.float64), ("btext", "b", np.float64), ("ben", "b", np.uint8),
+    ("bcand", "b", np.uint8), ("glist", "g100", np.int32), ("gvlen", "g", np.int32), ("garea", "g", np.float64),
+    ("gdadt", "g", np.float64), ("gori", "g", np.float64), ("gse", "g", np.float64), ("gen", "g", np.uint8),
+    ("gtype", "g", np.uint8),
+]
+
+
+class MeshHost(C.Structure):
+    _fields_ = [("nv", C.c_int), ("nb", C.c_int), ("ng", C.c_int)] + [(f, C.c_void_p) for f, _, _ in _MESH_FIELDS]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("t", C.c_double), ("curr_n_grains", C.c_int), ("nucleated_area", C.c_double),
+        ("export_due", C.c_int), ("keep_going", C.c_int), ("polling_iters", C.c_int),
+        ("n_two_three_iters", C.c_int), ("two_three_counts", C.c_int * 20), ("n_flips", C.c_int),
+        ("n_removals", C.c_int), ("n_two_three", C.c_int), ("n_nucleations", C.c_int),
+        ("nucleation_attempted", C.c_int), ("nucleation_candidate", C.c_int), ("gpu_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["two_three_counts"] = list(self.two_three_counts)[: self.n_two_three_iters]
+        return d
+
+
+_lib = None
+
+
+def lib():
+    """Load the in-tree libsevc.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libsevc.so is not built: run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        L.sevc_default_options.argtypes = [C.POINTER(Options)]
+        L.sevc_load_ini.argtypes = [C.c_char_p, C.POINTER(Options)]
+        L.sevc_create.argtypes = [C.POINTER(Options), C.POINTER(H)]
+        L.sevc_create_from_arrays.argtypes = [C.POINTER(Options), C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                              C.c_void_p, C.c_void_p, C.POINTER(H)]
+        L.sevc_destroy.argtypes = [H]
+        L.sevc_destroy.restype = None
+        L.sevc_step.argtypes = [H, C.POINTER(StepInfo)]
+        L.sevc_run_steps.argtypes = [H, C.c_int, C.POINTER(C.c_int), C.POINTER(StepInfo)]
+        L.sevc_should_continue.argtypes = [H]
+        L.sevc_export_text.argtypes = [H, C.c_char_p, C.c_double]
+        L.sevc_get_state.argtypes = [H, C.POINTER(MeshHost)]
+        L.sevc_mesh_sizes.argtypes = [H, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.sevc_check_data.argtypes = [H, C.POINTER(C.c_int)]
+        L.sevc_run_program.argtypes = [C.POINTER(Options), C.c_int]
+        L.sevc_rng_record.argtypes = [C.c_int, C.c_int, C.c_void_p]
+        L.sevc_set_profiling.argtypes = [H, C.c_int]
+        L.sevc_get_profile.argtypes = [H, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
+        L.sevc_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc:
+        raise SevcError(rc, lib().sevc_last_error().decode(errors="replace"))
+
+
+def default_options(**kw):
+    o = Options()
+    _check(lib().sevc_default_options(C.byref(o)))
+    for k, v in kw.items():
+        setattr(o, k, v.encode() if isinstance(v, str) else v)
+    return o
+
+
+def load_ini(path):
+    o = Options()
+    _check(lib().sevc_load_ini(path.encode(), C.byref(o)))
+    return o
+
+
+def load_mesh_host(opt):
+    """Host-only loader (src/io.h:66-264): the mesh as numpy arrays."""
+    L = lib()
+    L.sevc_load_mesh_host.argtypes = [C.POINTER(Options), C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]
+    nv, nb, ng = C.c_int(), C.c_int(), C.c_int()
+    _check(L.sevc_load_mesh_host(C.byref(opt), None, C.byref(nv), C.byref(nb), C.byref(ng)))
+    sizes = {"v": nv.value, "v3": 3 * nv.value, "b": nb.value, "g": ng.value, "g100": MAXV * ng.value}
+    arrs = {f: np.empty(sizes[k], dt) for f, k, dt in _MESH_FIELDS}
+    mh = MeshHost(nv.value, nb.value, ng.value, *[arrs[f].ctypes.data for f, _, _ in _MESH_FIELDS])
+    _check(L.sevc_load_mesh_host(C.byref(opt), C.byref(mh), None, None, None))
+    return arrs
+
+
+def rng_record(nstreams, ndraws):
+    """First `ndraws` cuRAND draws of streams curand_init(32, tid, 0)."""
+    out = np.empty((nstreams, ndraws), np.float64)
+    _check(lib().sevc_rng_record(nstreams, ndraws, out.ctypes.data))
+    return out
+
+
+class Engine:
+    """One simulation on the GPU (an sevc_handle)."""
+
+    def __init__(self, handle, opt):
+        self._h = handle
+        self.opt = opt
+        nv, nb, ng = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().sevc_mesh_sizes(self._h, C.byref(nv), C.byref(nb), C.byref(ng)))
+        self.nv, self.nb, self.ng = nv.value, nb.value, ng.value
+
+    @classmethod
+    def from_files(cls, opt):
+        h = C.c_void_p()
+        _check(lib().sevc_create(C.byref(opt), C.byref(h)))
+        return cls(h, opt)
+
+    @classmethod
+    def from_arrays(cls, opt, xy, ridges, oris, se):
+        xy = np.ascontiguousarray(xy, np.float64)
+        ridges = np.ascontiguousarray(ridges, np.int32)
+        oris = np.ascontiguousarray(oris, np.float64)
+        se = np.ascontiguousarray(se, np.float64)
+        h = C.c_void_p()
+        _check(lib().sevc_create_from_arrays(C.byref(opt), len(xy), xy.ctypes.data, len(ridges), ridges.ctypes.data,
+                                             len(oris), oris.ctypes.data, se.ctypes.data, C.byref(h)))
+        return cls(h, opt)
+
+    def close(self):
+        if self._h:
+            lib().sevc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self):
+        info = StepInfo()
+        _check(lib().sevc_step(self._h, C.byref(info)))
+        return info
+
+    def run_steps(self, n):
+        info, done = StepInfo(), C.c_int()
+        _check(lib().sevc_run_steps(self._h, n, C.byref(done), C.byref(info)))
+        return done.value, info
+
+    def should_continue(self):
+        return bool(lib().sevc_should_continue(self._h))
+
+    def export(self, path, time):
+        _check(lib().sevc_export_text(self._h, path.encode(), time))
+
+    def check_data(self):
+        n = C.c_int()
+        _check(lib().sevc_check_data(self._h, C.byref(n)))
+        return n.value
+
+    def get_state(self):
+        """Full mesh as numpy arrays (keys as in sevc_mesh_host)."""
+        sizes = {"v": self.nv, "v3": 3 * self.nv, "b": self.nb, "g": self.ng, "g100": MAXV * self.ng}
+        arrs = {f: np.empty(sizes[k], dt) for f, k, dt in _MESH_FIELDS}
+        mh = MeshHost(self.nv, self.nb, self.ng, *[arrs[f].ctypes.data for f, _, _ in _MESH_FIELDS])
+        _check(lib().sevc_get_state(self._h, C.byref(mh)))
+        return arrs
+
+    def set_profiling(self, on):
+        _check(lib().sevc_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self):
+        cap = 64
+        names = (C.c_char * 48 * cap)()
+        ms = np.zeros(cap)
+        launches = np.zeros(cap, np.int64)
+        n = C.c_int()
+        _check(lib().sevc_get_profile(self._h, cap, names, ms.ctypes.data, launches.ctypes.data, C.byref(n)))
+        return {names[i].value.decode(): (float(ms[i]), int(launches[i])) for i in range(min(n.value, cap))}

@@ -1,0 +1,179 @@
+"""GPU engine (through the C ABI) against the oracle and the reference.
+
+Parity bar:
+  * integer state (enabled flags, connectivity, candidate flags, grain lists,
+    types) and every event count: bit-exact after every step;
+  * positions, velocities, energies, areas, dA/dt, arclengths: bit-exact
+    whenever no transcendental function feeds them (isotropic boundaries,
+    GB_eps = 0); with anisotropic boundaries the boundary energy carries
+    libm's last-bit differences, so these fields must agree to
+    REL_TOL = 1e-12 relative per step (both sides restart every step from
+    the GPU's floating-point state);
+  * extinction times come from atan2/cos/sin (CUDA vs glibc): REL_TOL.
+Nucleation draws: the oracle replays the exact cuRAND XORWOW draws that
+the GPU consumes, recorded through sevc_rng_record.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import configs
+import snapshot
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-12
+GOLDEN = json.load(open(os.path.join(configs.HERE, "golden.json")))
+
+INT_FIELDS = ["ven", "vb", "vg", "bini", "bend", "ben", "bcand", "glist", "gvlen", "gen", "gtype"]
+FLOAT_FIELDS = ["px", "py", "vx", "vy", "venergy", "vel_bnd_x", "vel_grn_x", "vel_bnd_y", "vel_grn_y", "blen",
+                "benergy", "garea", "gdadt", "gori", "gse"]
+RESYNC = ["px", "py", "vx", "vy", "venergy", "vel_bnd_x", "vel_grn_x", "vel_bnd_y", "vel_grn_y", "blen", "benergy",
+          "btext", "garea", "gdadt", "gori"]
+
+
+def close(a, b, rel):
+    d = np.abs(a - b)
+    scale = np.maximum(np.abs(a), np.abs(b))
+    return np.all((d <= rel * scale) | (a == b))
+
+
+def compare(st, orc, exact_float, where):
+    for f in INT_FIELDS:
+        a, b = st[f], orc.field(f)
+        if not np.array_equal(a, b):
+            i = int(np.nonzero(a != b)[0][0])
+            raise AssertionError("%s: %s differs at %d: gpu %s oracle %s" % (where, f, i, a[i], b[i]))
+    for f in FLOAT_FIELDS:
+        a, b = st[f], orc.field(f)
+        ok = np.array_equal(a, b) if exact_float else close(a, b, REL_TOL)
+        if not ok:
+            i = int(np.argmax(np.abs(a - b)))
+            raise AssertionError("%s: %s differs at %d: gpu %r oracle %r" % (where, f, i, a[i], b[i]))
+    a, b = st["btext"], orc.field("btext")
+    assert close(a, b, REL_TOL), "%s: t_ext beyond %g" % (where, REL_TOL)
+
+
+def make_pair(gpu, O, name, tmp, nucleation_draws=0):
+    _, _, keys, seed, mg = configs.CONFIGS[name]
+    ini = configs.write_ini(os.path.join(tmp, "run.ini"), name, os.path.join(tmp, "out"))
+    opt = gpu.load_ini(ini)
+    opt.min_grains = mg
+    oopt = O.parse_ini(ini)
+    oopt.min_grains = mg
+    eng = gpu.Engine.from_files(opt)
+    orc = O.Oracle.from_files(oopt)
+    if nucleation_draws:
+        orc.rng_table(gpu.rng_record(8192, nucleation_draws))
+    return eng, orc, keys
+
+
+def run_pair(gpu, O, name, tmp, steps=None, draws=0):
+    eng, orc, keys = make_pair(gpu, O, name, tmp, draws)
+    exact = float(keys["GB_eps"]) == 0.0
+    k, events = 0, {"flips": 0, "removals": 0, "two_three": 0, "nucleations": 0}
+    while orc.should_continue() and (steps is None or k < steps):
+        info = eng.step()
+        assert orc.step() == 0, "oracle status %d" % orc.s.status
+        where = "%s step %d" % (name, info.n)
+        compare(eng.get_state(), orc, exact, where)
+        s = orc.s
+        assert info.curr_n_grains == s.curr_n_grains, where
+        assert info.nucleated_area == s.nucleated_area or not exact, where
+        assert info.polling_iters == s.polling_iters, where
+        assert list(info.two_three_counts)[:info.n_two_three_iters] == \
+            [s.last_two_three[i] for i in range(s.n_two_three_iters)], where
+        assert (info.n_flips, info.n_removals, info.n_two_three, info.n_nucleations) == \
+            (s.ev_flips, s.ev_removals, s.ev_two_three, s.ev_nucleations), where
+        if info.nucleation_attempted:
+            assert info.nucleation_candidate == s.vrt_id_candidate, where
+        events["flips"] += info.n_flips
+        events["removals"] += info.n_removals
+        events["two_three"] += info.n_two_three
+        events["nucleations"] += info.n_nucleations
+        if not exact:
+            st = eng.get_state()
+            for f in RESYNC:
+                orc.field(f)[:] = st[f]
+        keep = orc.finish_step()
+        assert bool(info.keep_going) == keep, where
+        k += 1
+        if not keep:
+            break
+    return events, k
+
+
+def test_plain_unit_bit_exact_every_step(gpu, oracle_mod, tmp_path):
+    ev, k = run_pair(gpu, oracle_mod, "plain_unit", str(tmp_path))
+    assert k == 301 and ev["removals"] > 0 and ev["flips"] > 0
+
+
+def test_nucleation_bit_exact_every_step(gpu, oracle_mod, tmp_path):
+    ev, k = run_pair(gpu, oracle_mod, "perstep_nucl", str(tmp_path), draws=6 * 302 + 16)
+    assert k == 301 and ev["nucleations"] > 0 and ev["removals"] > 0
+
+
+def test_anisotropic_per_step_tolerance(gpu, oracle_mod, tmp_path):
+    ev, k = run_pair(gpu, oracle_mod, "nucl_aniso", str(tmp_path), draws=6 * 82 + 16)
+    assert k == 401 and ev["removals"] > 0
+
+
+def test_gpu_matches_reference_snapshots(gpu, tmp_path):
+    """GPU exports against the digests of the reference's own snapshots, for
+    every snapshot before the first nucleation attempt (after it the random
+    streams differ: the fixtures used the synthetic stream)."""
+    for name in ("plain_unit", "nucl_aniso"):
+        _, _, keys, _, mg = configs.CONFIGS[name]
+        ini = configs.write_ini(os.path.join(str(tmp_path), name + ".ini"), name, "/tmp/unused")
+        opt = gpu.load_ini(ini)
+        opt.min_grains = mg
+        eng = gpu.Engine.from_files(opt)
+        g = GOLDEN[name]
+        prog, checked = 0, 0
+        for ref in g["steps"]:
+            info = eng.step()
+            if info.nucleation_attempted:
+                break
+            assert info.curr_n_grains == ref["n_grains"], (name, ref["n"])
+            assert list(info.two_three_counts)[:info.n_two_three_iters] == ref["two_three"], (name, ref["n"])
+            if float(keys["GB_eps"]) == 0.0:
+                assert "%.16f" % info.nucleated_area == ref["nucl_area"]
+            if info.export_due:
+                path = os.path.join(str(tmp_path), "%s_%06d.txt" % (name, prog))
+                eng.export(path, info.t)
+                full, topo = snapshot.digests(path)
+                assert topo == g["snapshots"][prog][1], (name, prog)
+                prog += 1
+                checked += 1
+            if not info.keep_going:
+                break
+        assert checked >= 5, name
+        eng.close()
+
+
+def test_rng_record_is_curand_stream(gpu):
+    a = gpu.rng_record(8192, 8)
+    b = gpu.rng_record(16, 4)
+    assert np.array_equal(a[:16, :4], b)
+    assert a.min() > 0 and a.max() <= 1
+    assert len(np.unique(a[:, 0])) == 8192
+
+
+@pytest.mark.parametrize("n,steps", [(20000, 30)])
+def test_meshgen_mesh_bit_exact(gpu, oracle_mod, n, steps):
+    import meshgen
+    inp = meshgen.make_inputs(n, 21)
+    kw = dict(n_grains=n, dt=2e-5, dtau=2e-5, domain_bound=1.0, GB_eps=0.0, SE_min=0.0, SE_max=0.5, do_nucleation=0,
+              nmax=steps, min_grains=10, snap_gap=1000)
+    eng = gpu.Engine.from_arrays(gpu.default_options(**kw), inp["xy"], inp["ridges"], inp["oris"], inp["se"])
+    oopt = oracle_mod.finish_options(oracle_mod.default_options(**kw))
+    orc = oracle_mod.Oracle.from_arrays(oopt, inp["xy"], inp["ridges"], inp["oris"], inp["se"])
+    orc.set_threads(os.cpu_count() or 1)
+    for k in range(steps):
+        info = eng.step()
+        assert orc.step() == 0
+        compare(eng.get_state(), orc, True, "meshgen step %d" % k)
+        assert info.n_removals == orc.s.ev_removals and info.n_flips == orc.s.ev_flips
+        orc.finish_step()

@@ -1,0 +1,150 @@
+"""Host-side logic on the CPU: the C ABI library, option parsing, mesh
+loading, the mesh generator, and the oracle's own checks."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import configs
+from conftest import ROOT, gpu_available
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "sevc.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sevc_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(engine_mod):
+    lib = engine_mod.lib()
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(engine_mod.EXPORTS) == names
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the no-GPU error path")
+def test_compute_calls_fail_without_gpu(engine_mod):
+    opt = engine_mod.default_options(n_grains=2, dt=1e-3, dtau=1e-3, do_nucleation=0)
+    xy = np.zeros((4, 2))
+    with pytest.raises(engine_mod.SevcError) as e:
+        engine_mod.Engine.from_arrays(opt, xy, np.zeros((6, 2), np.int32), np.zeros(2), np.zeros(2))
+    assert e.value.code == 6
+    with pytest.raises(engine_mod.SevcError):
+        engine_mod.rng_record(4, 4)
+
+
+def write(tmp, name, text):
+    p = os.path.join(tmp, name)
+    with open(p, "w") as f:
+        f.write(text)
+    return p
+
+
+def options_dict(o):
+    return {k: getattr(o, k) for k, _ in o._fields_}
+
+
+@pytest.mark.parametrize("name", sorted(configs.CONFIGS))
+def test_ini_parser_matches_oracle(engine_mod, oracle_mod, name, tmp_path):
+    ini = configs.write_ini(str(tmp_path / "r.ini"), name, "/tmp/x")
+    a, b = options_dict(engine_mod.load_ini(ini)), options_dict(oracle_mod.parse_ini(ini))
+    assert a == b
+
+
+def test_ini_parser_quirks(engine_mod, oracle_mod, tmp_path):
+    # src/options.h:99-163: keys are not trimmed, '#'/'[' lines skipped,
+    # strings lose their last character, do_nucleation only for "true\n"
+    text = ("# comment\n[Temporal]\ndt=0.5\n dtau=9\ndtau =9\ndtau=1.5\nnmax=7\n"
+            "vertex_fname=abc.txt\nfolder=/out/dir\ndo_nucleation=True\nGB_eps=0.25\nSE_fname=last")
+    p = write(str(tmp_path), "q.ini", text)
+    for o in (engine_mod.load_ini(p), oracle_mod.parse_ini(p)):
+        assert o.dt == 0.5 and o.dtau == 1.5 and o.nmax == 7
+        assert o.vertex_fname == b"abc.txt" and o.output_folder == b"/out/dir"
+        assert o.SE_fname == b"las"          # no trailing newline: a real character is chopped
+        assert o.do_nucleation == 0          # "True\n" is not "true\n"
+        assert o.nucleation_gap == 3         # int(dtau / dt)
+        assert o.tmax == -1 and o.GB_eps == 0.25
+    p = write(str(tmp_path), "d.ini", "dt=1e-3\n")
+    for o in (engine_mod.load_ini(p), oracle_mod.parse_ini(p)):
+        assert o.tmax == 1.0 and o.nmax == -1 and o.do_nucleation == 1 and o.GB_eps == 0.02
+        assert o.SE_min == 999 and o.min_grains == 5000
+
+
+ORACLE_FIELDS = {"px": "px", "py": "py", "ven": "ven", "vb": "vb", "vg": "vg", "bini": "bini", "bend": "bend",
+                 "ben": "ben", "btext": "btext", "glist": "glist", "gvlen": "gvlen", "gori": "gori", "gse": "gse",
+                 "gen": "gen", "gtype": "gtype"}
+
+
+@pytest.mark.parametrize("name", sorted(configs.CONFIGS))
+def test_host_loader_matches_oracle(engine_mod, oracle_mod, name, tmp_path):
+    ini = configs.write_ini(str(tmp_path / "r.ini"), name, "/tmp/x")
+    mine = engine_mod.load_mesh_host(engine_mod.load_ini(ini))
+    o = oracle_mod.Oracle.from_files(oracle_mod.parse_ini(ini))
+    for k, ok in ORACLE_FIELDS.items():
+        np.testing.assert_array_equal(mine[k], o.field(ok), err_msg=k)
+
+
+def test_loader_rejects_bad_inputs(engine_mod, oracle_mod, tmp_path):
+    ini = configs.write_ini(str(tmp_path / "r.ini"), "perstep_nucl", "/tmp/x")
+    opt = engine_mod.load_ini(ini)
+    opt.n_grains = 299                       # src/io.h:182-186 grain-count check
+    with pytest.raises(engine_mod.SevcError) as e:
+        engine_mod.load_mesh_host(opt)
+    assert e.value.code == 2
+    opt = engine_mod.load_ini(ini)
+    opt.vertex_fname = str(tmp_path / "missing.txt").encode()
+    with pytest.raises(engine_mod.SevcError) as e:
+        engine_mod.load_mesh_host(opt)
+    assert e.value.code == 1
+
+
+@pytest.mark.parametrize("n,seed", [(50, 1), (777, 2), (5000, 3)])
+def test_meshgen_builds_valid_periodic_meshes(oracle_mod, n, seed):
+    import meshgen
+    inp = meshgen.make_inputs(n, seed)
+    assert inp["xy"].shape == (2 * n, 2) and inp["ridges"].shape == (3 * n, 2)
+    assert inp["xy"].min() >= 0 and inp["xy"].max() < 1
+    deg = np.bincount(inp["ridges"].ravel(), minlength=2 * n)
+    assert np.all(deg == 3)
+    opt = oracle_mod.finish_options(oracle_mod.default_options(n_grains=n, dt=1e-3, dtau=1e-3, domain_bound=1.0))
+    o = oracle_mod.Oracle.from_arrays(opt, inp["xy"], inp["ridges"], inp["oris"], inp["se"])
+    assert o.check_data() == 0
+    oracle_mod.lib().orc_compute_grain_areas(o._p)
+    assert abs(o.field("garea").sum() - 1.0) < 1e-9
+
+
+def test_meshgen_file_roundtrip(engine_mod, tmp_path):
+    import meshgen
+    inp = meshgen.make_inputs(64, 5)
+    paths = meshgen.write_files(str(tmp_path), inp)
+    back = meshgen.read_files(paths["vertices"], paths["ridges"], paths["oris"], paths["se"])
+    np.testing.assert_array_equal(back["ridges"], inp["ridges"])
+    np.testing.assert_allclose(back["xy"], inp["xy"], rtol=0, atol=1e-16)  # %.16f keeps 16 decimals
+    opt = engine_mod.default_options(n_grains=64, dt=1e-3, dtau=1e-3, vertex_fname=paths["vertices"],
+                                     boundary_fname=paths["ridges"], orientation_fname=paths["oris"],
+                                     SE_fname=paths["se"])
+    m = engine_mod.load_mesh_host(opt)
+    assert m["gvlen"].sum() == 3 * 128
+
+
+def test_check_data_flags_planted_faults(oracle_mod, tmp_path):
+    ini = configs.write_ini(str(tmp_path / "r.ini"), "perstep_nucl", "/tmp/x")
+    o = oracle_mod.Oracle.from_files(oracle_mod.parse_ini(ini))
+    assert o.check_data() == 0
+    o.field("bend")[5] = o.field("bini")[5]          # a self-loop boundary
+    assert o.check_data() > 0
+    o2 = oracle_mod.Oracle.from_files(oracle_mod.parse_ini(ini))
+    o2.field("gvlen")[3] -= 1                          # list length no longer matches
+    assert o2.check_data() > 0
+
+
+def test_synthetic_stream_range():
+    import ctypes
+    from oracle import oracle as O
+    o = O.Oracle.from_files(O.parse_ini(configs.write_ini("/tmp/_s.ini", "perstep_nucl", "/tmp/x")))
+    o.rng_synthetic(5)
+    pos = o.field("rng_pos")
+    assert pos.shape == (8192,) and pos.max() == 0
