@@ -69,26 +69,38 @@ struct DevMesh {
 
 enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
 
-/* ---- periodic geometry, src/geometry.h:133-331 ---- */
+/* ---- periodic geometry, src/geometry.h:133-331 ----
+ * Comparisons, absolute values and min/max work on the IEEE-754 bit
+ * patterns with integer instructions: for finite doubles the signed
+ * 64-bit order of the patterns of non-negative values is their numeric
+ * order, so every branch takes the same side as the floating-point
+ * comparison of the reference while the (scarce) FP64 pipe only executes
+ * the arithmetic.  Inputs are never NaN. */
+#define SEVC_ABSMASK 0x7FFFFFFFFFFFFFFFLL
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double dabs(double x) { return __longlong_as_double(dbits(x) & SEVC_ABSMASK); }
+
 __device__ __forceinline__ double dmod(double a, double D)        /* dom_mod :133 */
 {
-    if (a < 0) return a + D;
-    else if (a >= D) return a - D;
+    long long b = dbits(a);
+    if (b < 0 && (b & SEVC_ABSMASK) != 0) return a + D;          /* a < 0 */
+    else if (b >= dbits(D)) return a - D;                         /* a >= D (D > 0) */
     return a;
 }
 __device__ __forceinline__ double wrapd(double dest, double orig, double D) /* wrap_dist :147 */
 {
     double d = dest - orig;
-    if (d > +(D / 2.0)) return (d - D);
-    if (d < -(D / 2.0)) return (D + d);
+    long long b = dbits(d), h = dbits(D / 2.0);
+    if (b > h) return (d - D);                                    /* d > +D/2 */
+    if (b < 0 && (b & SEVC_ABSMASK) > h) return (D + d);          /* d < -D/2 */
     return d;
 }
 __device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :217 */
 {
-    double ax = fabs(x), ay = fabs(y);
-    double p = fmax(ax, ay);
-    if (p == 0) return 0;
-    double q = fmin(ax, ay);
+    long long ax = dbits(x) & SEVC_ABSMASK, ay = dbits(y) & SEVC_ABSMASK;
+    long long pb = ax > ay ? ax : ay, qb = ax > ay ? ay : ax;    /* fmax / fmin of |x|, |y| */
+    if (pb == 0) return 0;
+    double p = __longlong_as_double(pb), q = __longlong_as_double(qb);
     double r = q / p;
     return p * sqrt(1.0 + r * r);
 }

@@ -126,7 +126,8 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.extra, 1024 * 4 }, { (void **)&x.threadfail, (size_t)grid * 4 },
         { (void **)&x.block_area, (size_t)h->p.n_blocks * 8 }, { (void **)&x.counters, CTR_COUNT * 4 },
         { (void **)&x.rng, 8192 * sizeof(curandState) }, { (void **)&x.rng_saved, 8192 * sizeof(curandState) },
-        { (void **)&x.nucl_buf, 64 * 4 },
+        { (void **)&x.nucl_buf, 64 * 4 }, { (void **)&x.vbucket, 32 * 4 }, { (void **)&x.perm, G * 4 },
+        { (void **)&x.n_perm, 4 },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -331,7 +332,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
         { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :171-181 */
     }
-    { Prof pr(h, "grain_fd"); launch_grain_fd(m, s); }                                            /* :127,:203 */
+    { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, s); }                                         /* :127,:203 */
     { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, s); }                                          /* :133,:203 */
     { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, s); }                                        /* :206 */
     { Prof pr(h, "text_label"); launch_text_label(m, o.dt, s); }                                  /* :212-216 */

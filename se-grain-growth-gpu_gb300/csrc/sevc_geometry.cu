@@ -41,6 +41,178 @@ __global__ void k_boundary_geometry(DevMesh m, double eps, double scaling)
     m.benergy[b] = gamma;
 }
 
+/* Store the stored-energy finite-difference terms of list vertex v
+ * (SE * (|A'| - |A|), src/calculus.h:60) in v's slot for grain g. */
+__device__ __forceinline__ void put_contrib(const DevMesh &m, int g, int v, double se, double absA, double Ax,
+                                           double Ay)
+{
+    int4 sg = m.vg[v];
+    int j = sg.x == g ? 0 : (sg.y == g ? 1 : (sg.z == g ? 2 : -1));
+    if (j >= 0) m.contrib[3 * v + j] = make_double2(se * (dabs(Ax) - absA), se * (dabs(Ay) - absA));
+}
+
+/* Grain pass for a grain of N sides (compile-time), polygon in registers.
+ *
+ * compute_area of the polygon with vertex p moved (src/geometry.h:757,
+ * :908) differs from the unmoved one only from vertex p on: the unwrapped
+ * coordinates of vertices 0..p-1 and the partial shoelace sum of terms
+ * 0..p-2 are the same operations on the same values, so they are taken
+ * from the unmoved pass; the moved component's unwrapped chain and the
+ * terms from p-1 on are recomputed in the reference's order.  The other
+ * component is unchanged (its dom_mod is the identity; if it is not, the
+ * slot falls back to a full recomputation). */
+/* Area of the polygon with vertex p moved along component C (0 = x,
+ * 1 = y).  R/A0/DD are the moved component's raw positions, unwrapped
+ * coordinates and wrapped deltas, Ro/B0 the other component's. */
+template <int N, int C>
+__device__ __forceinline__ double moved_area(const DevMesh &m, const int *__restrict__ L, int p, const double (&R)[N],
+                                             const double (&Ro)[N], const double (&A0)[N], const double (&B0)[N],
+                                             const double (&DD)[N], const double (&S)[N])
+{
+    const double D = m.D;
+    double moved = dmod(R[p] + SEVC_GRAD_EPS_D, D);
+    double other = dmod(Ro[p], D);
+    if (dbits(other) != dbits(Ro[p])) {
+        double2 pp = C == 0 ? make_double2(moved, other) : make_double2(other, moved);
+        return area_stream(L, N, m.pos, p, pp, D);
+    }
+    double Pm[N];
+    Pm[0] = 0;
+#pragma unroll
+    for (int k = 1; k < N; k++) {
+        if (k < p) Pm[k] = A0[k];
+        else if (k == p) Pm[k] = A0[k - 1] + wrapd(moved, R[k - 1], D);
+        else if (k == p + 1) Pm[k] = Pm[k - 1] + wrapd(R[k], moved, D);
+        else Pm[k] = Pm[k - 1] + DD[k];
+    }
+    double a = (p >= 2) ? S[p - 2] : 0.0;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        if (k < p - 1) continue;
+        const int k1 = (k + 1) % N;
+        if (C == 0) a += Pm[k] * B0[k1] - B0[k] * Pm[k1];
+        else a += B0[k] * Pm[k1] - Pm[k] * B0[k1];
+    }
+    return a * 0.5;
+}
+
+template <int N>
+__device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const int *__restrict__ L)
+{
+    const double D = m.D;
+    int V[N];
+    double RX[N], RY[N], AX[N], AY[N], DX[N], DY[N], S[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        V[k] = L[k];
+        double2 q = m.pos[V[k]];
+        RX[k] = q.x;
+        RY[k] = q.y;
+    }
+    AX[0] = 0; AY[0] = 0; DX[0] = 0; DY[0] = 0;
+#pragma unroll
+    for (int k = 1; k < N; k++) {
+        DX[k] = wrapd(RX[k], RX[k - 1], D);
+        DY[k] = wrapd(RY[k], RY[k - 1], D);
+        AX[k] = AX[k - 1] + DX[k];
+        AY[k] = AY[k - 1] + DY[k];
+    }
+    double acc = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        const int k1 = (k + 1) % N;
+        acc += AX[k] * AY[k1] - AY[k] * AX[k1];
+        S[k] = acc;
+    }
+    double A = acc * 0.5;
+    m.garea[g] = A;
+    double se = m.gse[g];
+    m.gq[g] = se * A / N;
+    double absA = dabs(A);
+#pragma unroll
+    for (int p = 0; p < N; p++) {
+        double ax = moved_area<N, 0>(m, L, p, RX, RY, AX, AY, DX, S);
+        double ay = moved_area<N, 1>(m, L, p, RY, RX, AY, AX, DY, S);
+        put_contrib(m, g, V[p], se, absA, ax, ay);
+    }
+}
+
+/* Grain pass, any side count: each polygon streamed from memory. */
+__device__ __noinline__ void grain_fd_generic(const DevMesh &m, int g, const int *__restrict__ L, int n)
+{
+    double2 none = make_double2(0, 0);
+    double A = area_stream(L, n, m.pos, -1, none, m.D);
+    m.garea[g] = A;
+    double se = m.gse[g];
+    m.gq[g] = se * A / n;
+    double absA = dabs(A);
+    for (int p = 0; p < n; p++) {
+        int v = L[p];
+        double2 q = m.pos[v];
+        double2 px = make_double2(dmod(q.x + SEVC_GRAD_EPS_D, m.D), dmod(q.y, m.D));
+        double2 py = make_double2(dmod(q.x, m.D), dmod(q.y + SEVC_GRAD_EPS_D, m.D));
+        double Ax = area_stream(L, n, m.pos, p, px, m.D);
+        double Ay = area_stream(L, n, m.pos, p, py, m.D);
+        put_contrib(m, g, v, se, absA, Ax, Ay);
+    }
+}
+
+/* grain pass over grains ordered by side count (warps see one N) */
+__global__ void __launch_bounds__(128) k_grain_fd_sorted(DevMesh m, const int *perm, const int *total)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *total) return;
+    int g = perm[i];
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    switch (n) {
+    case 3: grain_fd_fixed<3>(m, g, L); break;
+    case 4: grain_fd_fixed<4>(m, g, L); break;
+    case 5: grain_fd_fixed<5>(m, g, L); break;
+    case 6: grain_fd_fixed<6>(m, g, L); break;
+    case 7: grain_fd_fixed<7>(m, g, L); break;
+    case 8: grain_fd_fixed<8>(m, g, L); break;
+    case 9: grain_fd_fixed<9>(m, g, L); break;
+    case 10: grain_fd_fixed<10>(m, g, L); break;
+    default: grain_fd_generic(m, g, L, n); break;
+    }
+}
+
+/* counting sort of the enabled grains by side count (16 buckets, the last
+ * one for 15 or more sides) */
+constexpr int NBUCKET = 16;
+__global__ void k_vlen_hist(DevMesh m, int *cnt)
+{
+    __shared__ int h[NBUCKET];
+    if (threadIdx.x < NBUCKET) h[threadIdx.x] = 0;
+    __syncthreads();
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < m.ng && m.gen[g]) atomicAdd(&h[min(m.gvlen[g], NBUCKET - 1)], 1);
+    __syncthreads();
+    if (threadIdx.x < NBUCKET && h[threadIdx.x]) atomicAdd(&cnt[threadIdx.x], h[threadIdx.x]);
+}
+__global__ void k_vlen_offsets(int *cnt, int *cursor, int *total)
+{
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < NBUCKET; b++) { cursor[b] = acc; acc += cnt[b]; cnt[b] = 0; }
+        *total = acc;
+    }
+}
+__global__ void k_vlen_scatter(DevMesh m, int *cursor, int *perm)
+{
+    __shared__ int h[NBUCKET], base[NBUCKET];
+    if (threadIdx.x < NBUCKET) h[threadIdx.x] = 0;
+    __syncthreads();
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = -1, r = 0;
+    if (g < m.ng && m.gen[g]) { b = min(m.gvlen[g], NBUCKET - 1); r = atomicAdd(&h[b], 1); }
+    __syncthreads();
+    if (threadIdx.x < NBUCKET) base[threadIdx.x] = h[threadIdx.x] ? atomicAdd(&cursor[threadIdx.x], h[threadIdx.x]) : 0;
+    __syncthreads();
+    if (b >= 0) perm[base[b] + r] = g;
+}
+
 /* grain pass of the finite-difference velocity, see file comment;
  * also compute_grain_areas (src/calculus.h:224) and the per-grain part of
  * vertex_compute_energy (src/geometry.h:476). */
@@ -235,7 +407,16 @@ void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cuda
 {
     k_boundary_geometry<<<nblk(m.nb), TPB, 0, s>>>(m, eps, scaling);
 }
-void launch_grain_fd(const DevMesh &m, cudaStream_t s) { k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
+void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s)
+{
+    k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
+    k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
+    k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
+    k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.n_perm);
+}
+
+/* the unsorted per-grain pass, kept for A/B timing */
+void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_vertex_fd(const DevMesh &m, cudaStream_t s) { k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m); }
 void launch_grain_dadt(const DevMesh &m, cudaStream_t s) { k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_text_label(const DevMesh &m, double dt, cudaStream_t s) { k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt); }

@@ -20,6 +20,8 @@ struct DevScratch {
     int *counters;                   /* small device counters, see CTR_* */
     curandState *rng, *rng_saved;    /* 8192 cuRAND states + pre-attempt copy */
     int *nucl_buf;                   /* 64 ints: per-block pick and alive count */
+    int *vbucket;                    /* 32 ints: side-count histogram + cursors */
+    int *perm, *n_perm;              /* enabled grains ordered by side count */
 };
 
 enum {
@@ -42,7 +44,7 @@ struct StepParams {
 
 /* geometry (sevc_geometry.cu) */
 void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s);
-void launch_grain_fd(const DevMesh &m, cudaStream_t s);
+void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_vertex_fd(const DevMesh &m, cudaStream_t s);
 void launch_grain_dadt(const DevMesh &m, cudaStream_t s);
 void launch_text_label(const DevMesh &m, double dt, cudaStream_t s);

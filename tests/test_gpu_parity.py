@@ -52,8 +52,20 @@ def compare(st, orc, exact_float, where):
         if not ok:
             i = int(np.argmax(np.abs(a - b)))
             raise AssertionError("%s: %s differs at %d: gpu %r oracle %r" % (where, f, i, a[i], b[i]))
-    a, b = st["btext"], orc.field("btext")
-    assert close(a, b, REL_TOL), "%s: t_ext beyond %g" % (where, REL_TOL)
+    check_text(st["btext"], orc.field("btext"), st["ben"], where)
+
+
+def check_text(a, b, en, where):
+    """t_ext = -|d| / (T.P): libm's error in the unit tangent T enters the
+    denominator linearly, so 1/t_ext is compared, against REL_TOL times the
+    99th percentile of |1/t_ext| over enabled boundaries (a denominator that
+    cancels makes the relative error of t_ext itself unbounded)."""
+    ra, rb = 1.0 / a, 1.0 / b
+    q = np.quantile(np.abs(ra[en > 0]), 0.99)
+    bad = ~((a == b) | (np.abs(ra - rb) <= REL_TOL * (q + np.maximum(np.abs(ra), np.abs(rb)))))
+    if bad.any():
+        i = int(np.nonzero(bad)[0][0])
+        raise AssertionError("%s: t_ext differs at %d: gpu %r oracle %r (1/t scale %g)" % (where, i, a[i], b[i], q))
 
 
 def make_pair(gpu, O, name, tmp, nucleation_draws=0):
