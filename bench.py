@@ -87,9 +87,17 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def make_mesh(n, seed):
+def make_mesh(n, seed, cache=None):
+    import numpy as np
+    if cache and os.path.exists(cache):
+        z = np.load(cache)
+        if int(z["n_grains"]) == n:
+            return {k: z[k] for k in z.files}
     import meshgen
-    return meshgen.make_inputs(n, seed, se="lognormal", se_params=(-1.0, 0.5))
+    mesh = meshgen.make_inputs(n, seed, se="lognormal", se_params=(-1.0, 0.5))
+    if cache:
+        np.savez(cache, **mesh)
+    return mesh
 
 
 def algorithmic_bytes_per_step(nv):
@@ -115,7 +123,7 @@ def run_engine(args):
     import sevc
     n = args.grains
     t0 = time.time()
-    mesh = make_mesh(n, args.seed)
+    mesh = make_mesh(n, args.seed, args.mesh_cache)
     gen_s = time.time() - t0
     opt = workload_options(sevc, n, args.steps)
     host_bytes = mesh["xy"].nbytes + mesh["ridges"].nbytes + mesh["oris"].nbytes + mesh["se"].nbytes
@@ -141,14 +149,14 @@ def run_engine(args):
 
     # ---------------- profiling pass (per-kernel event times) ----------------
     eng.set_profiling(True)
-    for _ in range(args.prof_steps):
+    for _ in range(max(1, args.prof_steps)):
         eng.step()
     prof = eng.profile()
     eng.close()
     tot = sum(v[0] for v in prof.values())
     dom = max((k for k in prof if k in KERNEL_BYTES), key=lambda k: prof[k][0])
     unit, per_unit = KERNEL_BYTES[dom]
-    units = {"grains": n, "vertices": 2 * n, "boundaries": 3 * n}[unit]
+    units = {"grains": g, "vertices": 2 * g, "boundaries": 3 * g}[unit]
     avg_ms = prof[dom][0] / prof[dom][1]
     achieved = per_unit * units / (avg_ms / 1e3) / 1e9
     peaks = {}
@@ -192,7 +200,8 @@ def run_engine(args):
                      "note": "FP64-pipe bound on GB300; see DESIGN.md"},
         "kernel_ms_share": {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "step_bytes_rate_gbs": algorithmic_bytes_per_step(2 * n) * args.steps / (ms / 1e3) / 1e9,
-        "gpu_launches": None,
+        "gpu_launches": sum(i.kernel_launches for i in infos),
+        "kernel_ms_per_step": {k: round(v[0] / v[1] if v[1] else 0, 4) for k, v in prof.items()},
         "clocks": ck,
     }
     if args.cpu_baseline:
@@ -224,7 +233,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    mesh = make_mesh(args.grains, args.seed)
+    mesh = make_mesh(args.grains, args.seed, args.mesh_cache)
     from oracle import oracle as O
     O.build()
     opt = workload_options(O, args.grains, args.steps)
@@ -264,6 +273,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--prof-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -89,6 +89,10 @@ typedef struct sevc_step_info {
     int nucleation_attempted;  /* src/main.cu:141 condition was true         */
     int nucleation_candidate;  /* vertex id kept by the Metropolis test, -1  */
     double gpu_ms;             /* device time of the step (CUDA events)      */
+    int outputs_complete;      /* 1: every enabled boundary's t_ext and every
+                                  enabled grain's dA/dt was computed this step
+                                  (always so on steps that can export) */
+    int kernel_launches;       /* CUDA kernels the step launched             */
 } sevc_step_info;
 
 typedef struct sevc_handle sevc_handle;
@@ -144,6 +148,12 @@ sevc_status sevc_run_program(const sevc_options *opt, int verbose);
  * records the first `ndraws` draws of streams 0..nstreams-1 into `out`
  * (stream-major), for replay by an independent checker. */
 sevc_status sevc_rng_record(int nstreams, int ndraws, double *out);
+
+/* Output-only fields (extinction times of boundaries that cannot flip,
+ * dA/dt of grains that cannot vanish) are computed only on steps that can
+ * export a snapshot (sevc_step_info.outputs_complete); exported snapshots
+ * are always complete.  on = 1 computes them on every step. */
+sevc_status sevc_set_exact_all(sevc_handle *h, int on);
 
 /* Per-kernel device time accumulated while profiling is on (CUDA events
  * around each launch on the handle's stream). */

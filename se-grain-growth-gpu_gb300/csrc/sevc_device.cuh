@@ -65,6 +65,14 @@ struct DevMesh {
     int *modlist, *nmod;
     int *err;            /* ERRB_* bits */
     int *evt;            /* event counters, EVT_* */
+    /* grains whose list changed since the step's grain pass (their area is
+     * recomputed after removals, src/main.cu:266) */
+    int *adirty, *nadirty;
+    uint8_t *gadirty;
+    /* slots that ever held a nucleated grain, ascending */
+    int *nlist, *nnlist;
+    /* boundaries whose extinction time must be exact this step */
+    uint8_t *bforce;
 };
 
 enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
@@ -115,6 +123,22 @@ __device__ __forceinline__ double gb_energy(double d_alpha, double eps)
     return (1 + 0.5 * eps * (1 - pow(cos(4 * d_alpha), 3)));
 }
 
+/* Shoelace terms that involve the origin point (0, 0), decided on the
+ * integer pipe with IEEE signed-zero rules:
+ *  - the first term +0*y1 - (+0)*x1 is +-0, and +0 + (+-0) is +0, so a
+ *    sum that starts at +0 is still +0 after it;
+ *  - the closing term x*(+0) - y*(+0) is -0 exactly when x has its sign
+ *    bit set and y has not (else +0); acc + (+-0) equals acc except that
+ *    -0 + +0 is +0. */
+__device__ __forceinline__ double add_closing_term(double acc, double x, double y)
+{
+    if (dbits(acc) == (long long)0x8000000000000000ULL) {
+        bool neg = dbits(x) < 0 && dbits(y) >= 0;
+        return neg ? acc : 0.0;
+    }
+    return acc;
+}
+
 /* compute_area (src/geometry.h:757-765, with adjust_origin_for_points
  * :908-931) streamed over a grain list: point 0 becomes the origin,
  * later points accumulate wrapped deltas, shoelace terms add in list
@@ -130,10 +154,10 @@ __device__ __forceinline__ double area_stream(const int *__restrict__ L, int n, 
             double2 r = (k == ps) ? pp : pos[L[k]];
             double nx = ax + wrapd(r.x, rx, D);
             double ny = ay + wrapd(r.y, ry, D);
-            area += ax * ny - ay * nx;
+            if (k > 1) area += ax * ny - ay * nx;   /* term k-1; term 0 leaves +0 */
             ax = nx; ay = ny; rx = r.x; ry = r.y;
         }
-        area += ax * 0.0 - ay * 0.0; /* closing term with point 0 = (0, 0) */
+        area = add_closing_term(area, ax, ay);
     }
     area *= 0.5;
     return area;

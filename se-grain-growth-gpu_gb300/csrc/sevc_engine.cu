@@ -24,6 +24,8 @@
 #include <unistd.h>
 #include <vector>
 
+long long sevc_kernel_launches = 0;
+
 struct ProfEntry { double ms = 0; int64_t launches = 0; };
 
 struct sevc_handle {
@@ -38,6 +40,7 @@ struct sevc_handle {
     int n = 0, curr_n_grains = 0, allow_nucleation = 0;
     double t = 0, nucleated_area = 0;
     int polling_cap = 100000;
+    int exact_all = 0;
     /* pinned readback */
     int *h_ctr = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -126,8 +129,9 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.extra, 1024 * 4 }, { (void **)&x.threadfail, (size_t)grid * 4 },
         { (void **)&x.block_area, (size_t)h->p.n_blocks * 8 }, { (void **)&x.counters, CTR_COUNT * 4 },
         { (void **)&x.rng, 8192 * sizeof(curandState) }, { (void **)&x.rng_saved, 8192 * sizeof(curandState) },
-        { (void **)&x.nucl_buf, 64 * 4 }, { (void **)&x.vbucket, 32 * 4 }, { (void **)&x.perm, G * 4 },
-        { (void **)&x.n_perm, 4 },
+        { (void **)&x.nucl_buf, 64 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
+        { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
+        { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, 4 }, { (void **)&m.bforce, B },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -321,9 +325,11 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     memset(&loc, 0, sizeof loc);
     loc.n = h->n;
     loc.t = h->t;
+    long long launches0 = sevc_kernel_launches;
     cudaEventRecord(h->ev0, s);
     cudaMemsetAsync(m.err, 0, 16, s);
     cudaMemsetAsync(m.evt, 0, 16, s);
+    launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
 
     { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :124-130 */
     if (h->curr_n_grains <= 5 * o.n_grains / 6) h->allow_nucleation = 1;                        /* :137 */
@@ -334,8 +340,26 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     }
     { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, s); }                                         /* :127,:203 */
     { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, s); }                                          /* :133,:203 */
-    { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, s); }                                        /* :206 */
-    { Prof pr(h, "text_label"); launch_text_label(m, o.dt, s); }                                  /* :212-216 */
+    /* The first count of the 2x3 loop (:228) depends only on the topology,
+     * which nothing changes before that loop: count now, and learn whether
+     * this step can disable boundaries other than 3-sided grains' or export.
+     * Otherwise only 3-sided grains' dA/dt and the extinction times that
+     * matter are computed (see k_text_label). */
+    int c23 = 0, n3 = 0;
+    { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
+    if (!cuda_ok(cudaMemcpyAsync(h->h_ctr, x.n_b, 4, cudaMemcpyDeviceToHost, s), "readback") ||
+        !cuda_ok(cudaMemcpyAsync(h->h_ctr + 1, x.vbucket + VB_COUNT(3), 4, cudaMemcpyDeviceToHost, s), "readback") ||
+        !cuda_ok(cudaStreamSynchronize(s), "sync"))
+        return SEVC_ERR_CUDA;
+    c23 = h->h_ctr[0];
+    n3 = h->h_ctr[1];
+    int mg = o.min_grains;
+    int full = h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0) || c23 > 0 ||
+               (mg > 0 && h->curr_n_grains + 1 - n3 <= mg);
+    loc.outputs_complete = full;
+    if (!full) { Prof pr(h, "text_label"); launch_mark_force(m, x, n3, s); }
+    { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, full, n3, s); }                           /* :206 */
+    { Prof pr(h, "text_label"); launch_text_label(m, o.dt, full, s); }                            /* :212-216 */
     { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
 
     int conv = 0, it = 0;                                                                          /* :219 */
@@ -349,9 +373,11 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     { Prof pr(h, "conflicts"); launch_conflicts(m, x.list_a, x.n_a, s); }                         /* :222-225 */
 
     for (int k = 0; k < 20; k++) {                                                                 /* :227-250 */
-        int c = 0;
-        { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
-        if (read_ints(h, x.n_b, 1, &c)) return SEVC_ERR_CUDA;
+        int c = c23;
+        if (k > 0) {
+            { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
+            if (read_ints(h, x.n_b, 1, &c)) return SEVC_ERR_CUDA;
+        }
         loc.two_three_counts[k] = c;
         loc.n_two_three_iters = k + 1;
         if (c == 0) break;
@@ -362,7 +388,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
     { Prof pr(h, "remove_grains"); launch_remove_grains(m, x.list_c, x.n_c, s); }                 /* :259 */
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
-    { Prof pr(h, "grain_area"); launch_grain_area(m, s); }                                        /* :266 */
+    { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
     { Prof pr(h, "unlabel_st2"); launch_unlabel_st2(m, x.list_a, x.n_a, s); }                     /* :282 */
     { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }                     /* :289 */
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :294 */
@@ -389,7 +415,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     loc.n_nucleations = ev[4 + EVT_NUCLEATIONS];
     loc.nucleation_candidate = loc.nucleation_attempted ? ctr[CTR_CANDIDATE] : -1;
     loc.gpu_ms = ms;
-    int mg = o.min_grains;
+    loc.kernel_launches = (int)(sevc_kernel_launches - launches0);
     loc.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (h->curr_n_grains <= mg && mg > 0); /* :328 */
     h->n++;                                                                                         /* :388-389 */
     h->t = h->n * o.dt;
@@ -490,6 +516,13 @@ sevc_status sevc_rng_record(int nstreams, int ndraws, double *out)
     int dev = 0;
     if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) { sevc_set_error("no CUDA device"); return SEVC_ERR_CUDA; }
     return rng_record(nstreams, ndraws, out) ? SEVC_ERR_CUDA : SEVC_OK;
+}
+
+sevc_status sevc_set_exact_all(sevc_handle *h, int on)
+{
+    if (!h) return SEVC_ERR_ARG;
+    h->exact_all = on != 0;
+    return SEVC_OK;
 }
 
 sevc_status sevc_set_profiling(sevc_handle *h, int on)

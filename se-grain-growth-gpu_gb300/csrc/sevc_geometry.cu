@@ -85,14 +85,14 @@ __device__ __forceinline__ double moved_area(const DevMesh &m, const int *__rest
         else if (k == p + 1) Pm[k] = Pm[k - 1] + wrapd(R[k], moved, D);
         else Pm[k] = Pm[k - 1] + DD[k];
     }
-    double a = (p >= 2) ? S[p - 2] : 0.0;
+    double a = (p >= 2) ? S[p - 2] : 0.0;  /* S[0] = +0: term 0 never changes the sum */
 #pragma unroll
-    for (int k = 0; k < N; k++) {
+    for (int k = 1; k < N - 1; k++) {
         if (k < p - 1) continue;
-        const int k1 = (k + 1) % N;
-        if (C == 0) a += Pm[k] * B0[k1] - B0[k] * Pm[k1];
-        else a += B0[k] * Pm[k1] - Pm[k] * B0[k1];
+        if (C == 0) a += Pm[k] * B0[k + 1] - B0[k] * Pm[k + 1];
+        else a += B0[k] * Pm[k + 1] - Pm[k] * B0[k + 1];
     }
+    a = C == 0 ? add_closing_term(a, Pm[N - 1], B0[N - 1]) : add_closing_term(a, B0[N - 1], Pm[N - 1]);
     return a * 0.5;
 }
 
@@ -117,13 +117,15 @@ __device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const in
         AX[k] = AX[k - 1] + DX[k];
         AY[k] = AY[k - 1] + DY[k];
     }
-    double acc = 0;
+    double acc = 0;                    /* terms 0 and N-1 involve the origin */
+    S[0] = 0;
 #pragma unroll
-    for (int k = 0; k < N; k++) {
-        const int k1 = (k + 1) % N;
-        acc += AX[k] * AY[k1] - AY[k] * AX[k1];
+    for (int k = 1; k < N - 1; k++) {
+        acc += AX[k] * AY[k + 1] - AY[k] * AX[k + 1];
         S[k] = acc;
     }
+    acc = add_closing_term(acc, AX[N - 1], AY[N - 1]);
+    S[N - 1] = acc;
     double A = acc * 0.5;
     m.garea[g] = A;
     double se = m.gse[g];
@@ -157,8 +159,12 @@ __device__ __noinline__ void grain_fd_generic(const DevMesh &m, int g, const int
     }
 }
 
-/* grain pass over grains ordered by side count (warps see one N) */
-__global__ void __launch_bounds__(128) k_grain_fd_sorted(DevMesh m, const int *perm, const int *total)
+/* grain pass over grains ordered by side count (warps see one N).  The
+ * pass is FP64-latency bound: capping registers at 128 (4 blocks of 128
+ * per SM) measured 9% faster on the 1M-grain mesh than the compiler's
+ * 218-register choice, despite a few spills; an 80-register cap gained
+ * nothing more. */
+__global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int *perm, const int *total)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *total) return;
@@ -191,12 +197,39 @@ __global__ void k_vlen_hist(DevMesh m, int *cnt)
     __syncthreads();
     if (threadIdx.x < NBUCKET && h[threadIdx.x]) atomicAdd(&cnt[threadIdx.x], h[threadIdx.x]);
 }
+/* cnt[0..15] -> cursor[16..31] (bucket starts, advanced by the scatter),
+ * start[32..47] and count[48..63] kept for later passes over one bucket */
 __global__ void k_vlen_offsets(int *cnt, int *cursor, int *total)
 {
     if (threadIdx.x == 0) {
         int acc = 0;
-        for (int b = 0; b < NBUCKET; b++) { cursor[b] = acc; acc += cnt[b]; cnt[b] = 0; }
+        for (int b = 0; b < NBUCKET; b++) {
+            cursor[b] = acc;
+            cnt[2 * NBUCKET + b] = acc;
+            cnt[3 * NBUCKET + b] = cnt[b];
+            acc += cnt[b];
+            cnt[b] = 0;
+        }
         *total = acc;
+    }
+}
+
+/* dA/dt of the 3-sided grains only (bucket 3 of the side-count order) */
+__global__ void k_grain_dadt_bucket(DevMesh m, const int *perm, const int *vbucket);
+
+/* boundaries of the vertices of 3-sided grains must get exact extinction
+ * times: they are the only ones a step without 2x3 pairs can disable */
+__global__ void k_mark_force(DevMesh m, const int *perm, const int *vbucket)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= vbucket[3 * NBUCKET + 3]) return;
+    int g = perm[vbucket[2 * NBUCKET + 3] + i];
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    for (int k = 0; k < 3; k++) {
+        int4 s = m.vb[L[k]];
+        m.bforce[s.x] = 1;
+        m.bforce[s.y] = 1;
+        m.bforce[s.z] = 1;
     }
 }
 __global__ void k_vlen_scatter(DevMesh m, int *cursor, int *perm)
@@ -288,10 +321,24 @@ __global__ void k_vertex_fd(DevMesh m)
 
 /* compute_grain_dAdts, src/calculus.h:243 with compute_dAdt
  * src/geometry.h:779-787 streamed over the list */
+__device__ void dadt_of(const DevMesh &m, int g);
+
 __global__ void k_grain_dadt(DevMesh m)
 {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= m.ng || !m.gen[g]) return;
+    dadt_of(m, g);
+}
+
+__global__ void k_grain_dadt_bucket(DevMesh m, const int *perm, const int *vbucket)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= vbucket[3 * NBUCKET + 3]) return;
+    dadt_of(m, perm[vbucket[2 * NBUCKET + 3] + i]);
+}
+
+__device__ void dadt_of(const DevMesh &m, int g)
+{
     const int *L = m.glist + (size_t)SEVC_MAXV * g;
     int n = m.gvlen[g];
     double d = 0;
@@ -314,18 +361,49 @@ __global__ void k_grain_dadt(DevMesh m)
 
 /* compute_t_ext (src/topological.h:303-334) then label_boundaries
  * (:343-353), which runs on every slot including disabled ones */
-__global__ void k_text_label(DevMesh m, double dt)
+/*
+ * When `full` is 0 a boundary that provably is not a candidate skips the
+ * transcendental evaluation and keeps its previous t_ext (the value is not
+ * observed: exports happen only on steps run with `full`, and every
+ * boundary a step can disable gets an exact value through `bforce`).
+ *
+ * Certificate.  With d the unwrapped edge vector, P = v_end - v_ini and
+ * s = d.P, the reference's denominator is aux = T.P with T = (cos, sin) of
+ * atan2(d): |aux - s/|d|| <= 16u(|Px|+|Py|) + rounding (u = 2^-53, a few
+ * ulp of libm error per component).  The boundary is a candidate iff
+ * aux <= -|d|/dt (then t = -|d|/aux lies in [0, dt]).  So if
+ *   s > -|d|^2/dt + margin,
+ *   margin = 1e-12 |d|^2/dt + 1e-14 (|dx|+|dy|)(|Px|+|Py|) + 1e-15 (|dx Px| + |dy Py|)
+ * (each term at least five times the error it covers) it is not one.
+ */
+__global__ void k_text_label(DevMesh m, double dt, double inv_dt, int full)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= m.nb) return;
     double text = m.btext[b];
     if (m.ben[b]) {
+        bool exact = full || m.bforce[b];
+        if (m.bforce[b]) m.bforce[b] = 0;
         int2 e = m.bv[b];
         double2 pi = m.pos[e.x], pe = m.pos[e.y];
         double dx = 0.0 + wrapd(pe.x, pi.x, m.D);  /* adjust_origin_for_points on 2 points */
         double dy = 0.0 + wrapd(pe.y, pi.y, m.D);
         dx = dx - 0.0;
         dy = dy - 0.0;
+        double2 vi = m.vel[e.x], ve = m.vel[e.y];
+        if (!exact) {
+            double px = ve.x - vi.x, py = ve.y - vi.y;
+            double s = dx * px + dy * py;
+            double n2 = dx * dx + dy * dy;
+            double thr = -(n2 * inv_dt);
+            double margin = 1e-12 * (n2 * inv_dt) + 1e-14 * (dabs(dx) + dabs(dy)) * (dabs(px) + dabs(py)) +
+                            1e-15 * (dabs(dx * px) + dabs(dy * py));
+            if (n2 > 0 && s > thr + margin) {
+                m.bcand[b] = 0;
+                m.bconf[b] = -1;
+                return;
+            }
+        }
         double norm = vmag(dx, dy);
         double tx = 0, ty = 0;
         if (norm != 0) {                            /* vector2_unitary, src/geometry.h:274 */
@@ -333,7 +411,6 @@ __global__ void k_text_label(DevMesh m, double dt)
             tx = cos(ang);
             ty = sin(ang);
         }
-        double2 vi = m.vel[e.x], ve = m.vel[e.y];
         double aux = tx * (ve.x - vi.x) + ty * (ve.y - vi.y);
         text = (aux == 0) ? 100 : -norm / aux;
         m.btext[b] = text;
@@ -350,6 +427,25 @@ __global__ void k_grain_area(DevMesh m)
     double2 none = make_double2(0, 0);
     m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
 }
+
+/* compute_grain_areas after the removals (src/main.cu:266): only grains
+ * whose vertex list changed since the grain pass can have a new area (the
+ * moved vertex of a removal belongs only to such grains); the others keep
+ * the identical value the grain pass computed.  compute = 0 just drops
+ * the list (marks made by the flips' fix-up after this point). */
+__global__ void k_area_dirty(DevMesh m, int compute)
+{
+    int n = *m.nadirty;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int g = m.adirty[i];
+        if (compute && m.gen[g]) {
+            double2 none = make_double2(0, 0);
+            m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
+        }
+        m.gadirty[g] = 0;
+    }
+}
+__global__ void k_reset_count(int *c) { *c = 0; }
 
 /* update_vertices_positions, src/calculus.h:391-404 */
 __global__ void k_update(DevMesh m, double dt)
@@ -382,8 +478,13 @@ __global__ void k_nucl_area_blocks(DevMesh m, double *block_out)
     int tid = blockIdx.x * blockDim.x + threadIdx.x;
     int stride = gridDim.x * blockDim.x;
     double a = 0.0;
-    for (int g = tid; g < m.ng; g += stride)
-        if (m.gen[g] && m.gtype[g] == GT_NUCLEATED) a += m.garea[g];
+    /* the thread's stride set in ascending order, restricted to the slots
+     * that can be NUCLEATED (m.nlist is ascending) */
+    int nn = *m.nnlist;
+    for (int i = 0; i < nn; i++) {
+        int g = m.nlist[i];
+        if (g % stride == tid && m.gen[g] && m.gtype[g] == GT_NUCLEATED) a += m.garea[g];
+    }
     t[threadIdx.x] = a;
     __syncthreads();
     for (int i = blockDim.x / 2; i != 0; i /= 2) {
@@ -405,29 +506,45 @@ __global__ void k_nucl_area_final(const double *block_out, int nblocks, double D
 
 void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s)
 {
-    k_boundary_geometry<<<nblk(m.nb), TPB, 0, s>>>(m, eps, scaling);
+    COUNT_LAUNCHES(1), k_boundary_geometry<<<nblk(m.nb), TPB, 0, s>>>(m, eps, scaling);
 }
 void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
-    k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
-    k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
-    k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.n_perm);
+    COUNT_LAUNCHES(1), k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
+    COUNT_LAUNCHES(1), k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
+    COUNT_LAUNCHES(1), k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
+    COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.n_perm);
 }
 
 /* the unsorted per-grain pass, kept for A/B timing */
-void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_vertex_fd(const DevMesh &m, cudaStream_t s) { k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m); }
-void launch_grain_dadt(const DevMesh &m, cudaStream_t s) { k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_text_label(const DevMesh &m, double dt, cudaStream_t s) { k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt); }
-void launch_grain_area(const DevMesh &m, cudaStream_t s) { k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { k_update<<<nblk(m.nv), TPB, 0, s>>>(m, dt); }
+void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
+void launch_vertex_fd(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m); }
+void launch_grain_dadt(const DevMesh &m, const DevScratch &x, int full, int n3, cudaStream_t s)
+{
+    if (full) COUNT_LAUNCHES(1), k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m);
+    else if (n3 > 0) COUNT_LAUNCHES(1), k_grain_dadt_bucket<<<nblk(n3), TPB, 0, s>>>(m, x.perm, x.vbucket);
+}
+void launch_mark_force(const DevMesh &m, const DevScratch &x, int n3, cudaStream_t s)
+{
+    if (n3 > 0) COUNT_LAUNCHES(1), k_mark_force<<<nblk(n3), TPB, 0, s>>>(m, x.perm, x.vbucket);
+}
+void launch_text_label(const DevMesh &m, double dt, int full, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt, 1.0 / dt, full);
+}
+void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
+void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_area_dirty<<<152, TPB, 0, s>>>(m, compute);
+    COUNT_LAUNCHES(1), k_reset_count<<<1, 1, 0, s>>>(m.nadirty);
+}
+void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { COUNT_LAUNCHES(1), k_update<<<nblk(m.nv), TPB, 0, s>>>(m, dt); }
 
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
 {
     cudaMemsetAsync(x.counters + CTR_NGRAINS, 0, sizeof(int), s);
-    k_count_grains<<<nblk(m.ng), TPB, 0, s>>>(m, x.counters + CTR_NGRAINS);
-    k_nucl_area_blocks<<<p.n_blocks, p.n_threads, 0, s>>>(m, x.block_area);
-    k_nucl_area_final<<<1, 1, 0, s>>>(x.block_area, p.n_blocks, m.D,
+    COUNT_LAUNCHES(1), k_count_grains<<<nblk(m.ng), TPB, 0, s>>>(m, x.counters + CTR_NGRAINS);
+    COUNT_LAUNCHES(1), k_nucl_area_blocks<<<p.n_blocks, p.n_threads, 0, s>>>(m, x.block_area);
+    COUNT_LAUNCHES(1), k_nucl_area_final<<<1, 1, 0, s>>>(x.block_area, p.n_blocks, m.D,
                                       reinterpret_cast<double *>(x.counters + CTR_NUCL_AREA_SLOT));
 }

@@ -46,9 +46,14 @@ struct StepParams {
 void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s);
 void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_vertex_fd(const DevMesh &m, cudaStream_t s);
-void launch_grain_dadt(const DevMesh &m, cudaStream_t s);
-void launch_text_label(const DevMesh &m, double dt, cudaStream_t s);
+/* side-count histogram layout in DevScratch::vbucket */
+#define VB_START(b) (32 + (b))
+#define VB_COUNT(b) (48 + (b))
+void launch_grain_dadt(const DevMesh &m, const DevScratch &x, int full, int n3, cudaStream_t s);
+void launch_mark_force(const DevMesh &m, const DevScratch &x, int n3, cudaStream_t s);
+void launch_text_label(const DevMesh &m, double dt, int full, cudaStream_t s);
 void launch_grain_area(const DevMesh &m, cudaStream_t s);
+void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s);
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s);
 
@@ -72,5 +77,9 @@ void launch_nucleation(const DevMesh &m, const DevScratch &x, const StepParams &
 int rng_record(int nstreams, int ndraws, double *host_out);
 
 #define SEVC_CUDA_OK(expr) ((expr) == cudaSuccess)
+
+/* kernels launched by this process (reported per step) */
+extern long long sevc_kernel_launches;
+#define COUNT_LAUNCHES(k) (sevc_kernel_launches += (k))
 
 #endif

@@ -305,6 +305,11 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     init_boundary_dev(m, BC, B, C);
     init_boundary_dev(m, CA, C, A);
     add_bnd_slot(m, A, o.AD);
+    if (m.gtype[g] != GT_NUCLEATED) {                      /* keep m.nlist ascending */
+        int k = (*m.nnlist)++;
+        while (k > 0 && m.nlist[k - 1] > g) { m.nlist[k] = m.nlist[k - 1]; k--; }
+        m.nlist[k] = g;
+    }
     int *L = m.glist + (size_t)SEVC_MAXV * g;              /* nucleate_grain :596 */
     for (int i = 0; i < SEVC_MAXV; i++) L[i] = -1;
     m.gvlen[g] = 0; m.garea[g] = 0; m.gse[g] = 0; m.gori[g] = 0;
@@ -343,13 +348,13 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
 
 void launch_rng_init(curandState *st, int n, cudaStream_t s)
 {
-    k_rng_init<<<(n + 255) / 256, 256, 0, s>>>(st, n);
+    COUNT_LAUNCHES(1), k_rng_init<<<(n + 255) / 256, 256, 0, s>>>(st, n);
 }
 
 void launch_nucleation(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
 {
-    k_nucl_blocks<<<NBLK, NTHR, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf);
-    k_nucl_finish<<<1, 1, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf, x.counters, p.eps, p.scaling, p.MC_k);
+    COUNT_LAUNCHES(1), k_nucl_blocks<<<NBLK, NTHR, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf);
+    COUNT_LAUNCHES(1), k_nucl_finish<<<1, 1, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf, x.counters, p.eps, p.scaling, p.MC_k);
 }
 
 int rng_record(int nstreams, int ndraws, double *host_out)
@@ -359,8 +364,8 @@ int rng_record(int nstreams, int ndraws, double *host_out)
     size_t bytes = (size_t)nstreams * ndraws * sizeof(double);
     if (cudaMalloc(&st, sizeof(curandState) * nstreams) != cudaSuccess) return 1;
     if (cudaMalloc(&d, bytes) != cudaSuccess) { cudaFree(st); return 1; }
-    k_rng_init<<<(nstreams + 255) / 256, 256>>>(st, nstreams);
-    k_rng_draw<<<(nstreams + 255) / 256, 256>>>(st, nstreams, ndraws, d);
+    COUNT_LAUNCHES(1), k_rng_init<<<(nstreams + 255) / 256, 256>>>(st, nstreams);
+    COUNT_LAUNCHES(1), k_rng_draw<<<(nstreams + 255) / 256, 256>>>(st, nstreams, ndraws, d);
     cudaError_t e = cudaMemcpy(host_out, d, bytes, cudaMemcpyDeviceToHost);
     cudaFree(st);
     cudaFree(d);

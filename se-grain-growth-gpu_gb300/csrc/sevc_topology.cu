@@ -678,7 +678,14 @@ __global__ void k_fix_clear(DevMesh m)
     int nf = *m.nfix, nm = *m.nmod;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
         int g = m.fixlist[w];
-        if (m.gen[g]) m.gfix[g] = 0;
+        if (m.gen[g]) {
+            m.gfix[g] = 0;
+            if (!m.gadirty[g]) {              /* its area must be recomputed */
+                m.gadirty[g] = 1;
+                int i = atomicAdd(m.nadirty, 1);
+                if (i < m.ng) m.adirty[i] = g; else raise_err(m, ERRB_WORKLIST);
+            }
+        }
     }
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nm; w += gridDim.x * blockDim.x) {
         int v = m.modlist[w];
@@ -726,55 +733,55 @@ void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *can
                            const StepParams &p, cudaStream_t s)
 {
     int g = listgrid(m.nb);
-    k_poll_vote<<<g, TPB, 0, s>>>(m, cand, ncand);
-    k_poll_count<<<g, TPB, 0, s>>>(m, cand, ncand);
-    k_poll_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
+    COUNT_LAUNCHES(1), k_poll_vote<<<g, TPB, 0, s>>>(m, cand, ncand);
+    COUNT_LAUNCHES(1), k_poll_count<<<g, TPB, 0, s>>>(m, cand, ncand);
+    COUNT_LAUNCHES(1), k_poll_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
     int grid = p.n_blocks * p.n_threads;
     int one = 1;
     cudaMemcpyAsync(x.counters + CTR_CONVERGED, &one, sizeof(int), cudaMemcpyHostToDevice, s);
-    k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
-    k_poll_final<<<p.n_blocks, p.n_threads, 0, s>>>(x.threadfail, x.counters + CTR_CONVERGED);
+    COUNT_LAUNCHES(1), k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+    COUNT_LAUNCHES(1), k_poll_final<<<p.n_blocks, p.n_threads, 0, s>>>(x.threadfail, x.counters + CTR_CONVERGED);
 }
 
 void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
 {
     int g = listgrid(m.nb);
-    k_conflict_check<<<g, TPB, 0, s>>>(m, cand, ncand);
-    k_conflict_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
+    COUNT_LAUNCHES(1), k_conflict_check<<<g, TPB, 0, s>>>(m, cand, ncand);
+    COUNT_LAUNCHES(1), k_conflict_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
 }
 
 void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s)
 {
-    k_remove_two_three<<<1, 1, 0, s>>>(m, list, n, x.extra);
+    COUNT_LAUNCHES(1), k_remove_two_three<<<1, 1, 0, s>>>(m, list, n, x.extra);
 }
 
 void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s)
 {
-    k_label_3sided<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, dt);
+    COUNT_LAUNCHES(1), k_label_3sided<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, dt);
 }
 
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
 {
-    k_remove_grains<<<1, 1, 0, s>>>(m, list, n);
+    COUNT_LAUNCHES(1), k_remove_grains<<<1, 1, 0, s>>>(m, list, n);
 }
 
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
 {
-    k_unlabel_st2<<<listgrid(m.nb), TPB, 0, s>>>(m, cand, ncand);
+    COUNT_LAUNCHES(1), k_unlabel_st2<<<listgrid(m.nb), TPB, 0, s>>>(m, cand, ncand);
 }
 
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s)
 {
     (void)x;
-    k_flips<<<1, 1, 0, s>>>(m, eps, cand, ncand);
+    COUNT_LAUNCHES(1), k_flips<<<1, 1, 0, s>>>(m, eps, cand, ncand);
 }
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)
 {
-    k_fix_add<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    k_fix_remove<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    k_fix_replace<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    k_fix_reset<<<1, 1, 0, s>>>(m);
+    COUNT_LAUNCHES(1), k_fix_add<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    COUNT_LAUNCHES(1), k_fix_remove<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    COUNT_LAUNCHES(1), k_fix_replace<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    COUNT_LAUNCHES(1), k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    COUNT_LAUNCHES(1), k_fix_reset<<<1, 1, 0, s>>>(m);
 }

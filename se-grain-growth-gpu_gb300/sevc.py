@@ -20,7 +20,7 @@ STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "CAPACITY", 4: "NONCONVERGED", 5: "TO
 EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_from_arrays", "sevc_destroy", "sevc_load_mesh_host",
            "sevc_step", "sevc_run_steps", "sevc_should_continue", "sevc_export_text", "sevc_get_state",
            "sevc_mesh_sizes", "sevc_check_data", "sevc_run_program", "sevc_rng_record", "sevc_set_profiling",
-           "sevc_get_profile", "sevc_last_error"]
+           "sevc_get_profile", "sevc_last_error", "sevc_set_exact_all"]
 
 
 class SevcError(RuntimeError):
@@ -66,6 +66,7 @@ class StepInfo(C.Structure):
         ("n_two_three_iters", C.c_int), ("two_three_counts", C.c_int * 20), ("n_flips", C.c_int),
         ("n_removals", C.c_int), ("n_two_three", C.c_int), ("n_nucleations", C.c_int),
         ("nucleation_attempted", C.c_int), ("nucleation_candidate", C.c_int), ("gpu_ms", C.c_double),
+        ("outputs_complete", C.c_int), ("kernel_launches", C.c_int),
     ]
 
     def as_dict(self):
@@ -214,6 +215,10 @@ class Engine:
         mh = MeshHost(self.nv, self.nb, self.ng, *[arrs[f].ctypes.data for f, _, _ in _MESH_FIELDS])
         _check(lib().sevc_get_state(self._h, C.byref(mh)))
         return arrs
+
+    def set_exact_all(self, on):
+        lib().sevc_set_exact_all.argtypes = [C.c_void_p, C.c_int]
+        _check(lib().sevc_set_exact_all(self._h, 1 if on else 0))
 
     def set_profiling(self, on):
         _check(lib().sevc_set_profiling(self._h, 1 if on else 0))

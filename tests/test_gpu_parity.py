@@ -29,7 +29,7 @@ GOLDEN = json.load(open(os.path.join(configs.HERE, "golden.json")))
 
 INT_FIELDS = ["ven", "vb", "vg", "bini", "bend", "ben", "bcand", "glist", "gvlen", "gen", "gtype"]
 FLOAT_FIELDS = ["px", "py", "vx", "vy", "venergy", "vel_bnd_x", "vel_grn_x", "vel_bnd_y", "vel_grn_y", "blen",
-                "benergy", "garea", "gdadt", "gori", "gse"]
+                "benergy", "garea", "gori", "gse"]
 RESYNC = ["px", "py", "vx", "vy", "venergy", "vel_bnd_x", "vel_grn_x", "vel_bnd_y", "vel_grn_y", "blen", "benergy",
           "btext", "garea", "gdadt", "gori"]
 
@@ -40,7 +40,11 @@ def close(a, b, rel):
     return np.all((d <= rel * scale) | (a == b))
 
 
-def compare(st, orc, exact_float, where):
+def compare(st, orc, exact_float, where, complete=True):
+    """complete: the step computed every output-only value (t_ext of every
+    enabled boundary, dA/dt of every enabled grain); otherwise those are
+    compared where the engine must have them: t_ext of candidates and of
+    disabled boundaries, dA/dt of disabled grains."""
     for f in INT_FIELDS:
         a, b = st[f], orc.field(f)
         if not np.array_equal(a, b):
@@ -52,10 +56,15 @@ def compare(st, orc, exact_float, where):
         if not ok:
             i = int(np.argmax(np.abs(a - b)))
             raise AssertionError("%s: %s differs at %d: gpu %r oracle %r" % (where, f, i, a[i], b[i]))
-    check_text(st["btext"], orc.field("btext"), st["ben"], where)
+    a, b = st["gdadt"], orc.field("gdadt")
+    sel = np.ones(len(a), bool) if complete else st["gen"] == 0
+    ok = np.array_equal(a[sel], b[sel]) if exact_float else close(a[sel], b[sel], REL_TOL)
+    assert ok, "%s: dA/dt differs" % where
+    sel = np.ones(len(st["btext"]), bool) if complete else (st["bcand"] > 0) | (st["ben"] == 0)
+    check_text(st["btext"], orc.field("btext"), st["ben"], where, sel)
 
 
-def check_text(a, b, en, where):
+def check_text(a, b, en, where, sel=None):
     """t_ext = -|d| / (T.P): libm's error in the unit tangent T enters the
     denominator linearly, so 1/t_ext is compared, against REL_TOL times the
     99th percentile of |1/t_ext| over enabled boundaries (a denominator that
@@ -63,6 +72,8 @@ def check_text(a, b, en, where):
     ra, rb = 1.0 / a, 1.0 / b
     q = np.quantile(np.abs(ra[en > 0]), 0.99)
     bad = ~((a == b) | (np.abs(ra - rb) <= REL_TOL * (q + np.maximum(np.abs(ra), np.abs(rb)))))
+    if sel is not None:
+        bad &= sel
     if bad.any():
         i = int(np.nonzero(bad)[0][0])
         raise AssertionError("%s: t_ext differs at %d: gpu %r oracle %r (1/t scale %g)" % (where, i, a[i], b[i], q))
@@ -90,7 +101,7 @@ def run_pair(gpu, O, name, tmp, steps=None, draws=0):
         info = eng.step()
         assert orc.step() == 0, "oracle status %d" % orc.s.status
         where = "%s step %d" % (name, info.n)
-        compare(eng.get_state(), orc, exact, where)
+        compare(eng.get_state(), orc, exact, where, complete=bool(info.outputs_complete))
         s = orc.s
         assert info.curr_n_grains == s.curr_n_grains, where
         assert info.nucleated_area == s.nucleated_area or not exact, where
@@ -165,6 +176,37 @@ def test_gpu_matches_reference_snapshots(gpu, tmp_path):
         eng.close()
 
 
+@pytest.mark.parametrize("name", ["plain_unit", "nucl_aniso"])
+def test_skipped_outputs_change_nothing_else(gpu, name, tmp_path):
+    """Steps that skip t_ext of provable non-candidates and dA/dt of grains
+    that cannot vanish must leave every other value bit-identical to steps
+    that compute everything, and must be complete whenever they can export."""
+    _, _, _, _, mg = configs.CONFIGS[name]
+    ini = configs.write_ini(os.path.join(str(tmp_path), "r.ini"), name, "/tmp/unused")
+    opt = gpu.load_ini(ini)
+    opt.min_grains = mg
+    a, b = gpu.Engine.from_files(opt), gpu.Engine.from_files(opt)
+    b.set_exact_all(True)
+    skipped = 0
+    while True:
+        ia, ib = a.step(), b.step()
+        assert ib.outputs_complete
+        if ia.export_due:
+            assert ia.outputs_complete
+        sa, sb = a.get_state(), b.get_state()
+        for f in INT_FIELDS + FLOAT_FIELDS:
+            assert np.array_equal(sa[f], sb[f]), (name, ia.n, f)
+        if ia.outputs_complete:
+            assert np.array_equal(sa["btext"], sb["btext"]) and np.array_equal(sa["gdadt"], sb["gdadt"])
+        else:
+            skipped += 1
+            c = (sa["bcand"] > 0) | (sa["ben"] == 0)
+            assert np.array_equal(sa["btext"][c], sb["btext"][c])
+        if not ia.keep_going:
+            break
+    assert skipped > 0
+
+
 def test_rng_record_is_curand_stream(gpu):
     a = gpu.rng_record(8192, 8)
     b = gpu.rng_record(16, 4)
@@ -186,6 +228,6 @@ def test_meshgen_mesh_bit_exact(gpu, oracle_mod, n, steps):
     for k in range(steps):
         info = eng.step()
         assert orc.step() == 0
-        compare(eng.get_state(), orc, True, "meshgen step %d" % k)
+        compare(eng.get_state(), orc, True, "meshgen step %d" % k, complete=bool(info.outputs_complete))
         assert info.n_removals == orc.s.ev_removals and info.n_flips == orc.s.ev_flips
         orc.finish_step()
