@@ -149,6 +149,22 @@ sevc_status sevc_run_program(const sevc_options *opt, int verbose);
  * (stream-major), for replay by an independent checker. */
 sevc_status sevc_rng_record(int nstreams, int ndraws, double *out);
 
+/* The same record without any allocation.  No counterpart in the
+ * reference.  For callers that cannot let a library call cudaMalloc: a
+ * host framework that hands out device memory only from its own pool, a
+ * process whose device-memory budget is already taken by the simulation,
+ * or code that must not trigger the implicit synchronisation cudaMalloc
+ * can cause.  The caller passes the output: d_out is DEVICE memory for
+ * nstreams x ndraws doubles (stream-major); work is enqueued on `stream`
+ * (a cudaStream_t, NULL = default stream) and the call returns without
+ * waiting.  Scratch is a fixed device array of 8192 generator states
+ * (384 KiB per GPU, kept until exit); nstreams > 8192 is rejected with
+ * SEVC_ERR_ARG.  The first call on each device resolves that array's
+ * device address (with the device current); make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
+sevc_status sevc_rng_record_noalloc(int nstreams, int ndraws, double *d_out, void *stream);
+
 /* Output-only fields (extinction times of boundaries that cannot flip,
  * dA/dt of grains that cannot vanish) are computed only on steps that can
  * export a snapshot (sevc_step_info.outputs_complete); exported snapshots

@@ -18,8 +18,10 @@
  * taken before the attempt.
  */
 #include "sevc_internal.h"
+#include "sevc_host.h"
 
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -370,4 +372,60 @@ int rng_record(int nstreams, int ndraws, double *host_out)
     cudaFree(st);
     cudaFree(d);
     return e == cudaSuccess ? 0 : 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* Allocation-free recording of the random stream                      */
+/* ------------------------------------------------------------------ */
+/* Scratch of sevc_rng_record_noalloc: one cuRAND XORWOW state per stream,
+ * 8192 x 48 bytes = 384 KiB, held by every GPU that loads the library
+ * until the process exits.  8192 is the reference's whole 32 x 256 grid,
+ * so every stream it uses fits. */
+#define SEVC_NOALLOC_MAX_STREAMS 8192
+static __device__ __align__(256) curandState g_noalloc_rng[SEVC_NOALLOC_MAX_STREAMS];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+curandState *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   /* device address per device, set once */
+} // namespace
+
+extern "C" sevc_status sevc_rng_record_noalloc(int nstreams, int ndraws, double *d_out, void *stream)
+{
+    if (nstreams <= 0 || ndraws <= 0 || !d_out) {
+        sevc_set_error("sevc_rng_record_noalloc: need nstreams > 0, ndraws > 0 and an output buffer");
+        return SEVC_ERR_ARG;
+    }
+    if (nstreams > SEVC_NOALLOC_MAX_STREAMS) {
+        sevc_set_error("sevc_rng_record_noalloc: nstreams %d exceeds the fixed scratch of %d streams", nstreams,
+                       SEVC_NOALLOC_MAX_STREAMS);
+        return SEVC_ERR_ARG;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { sevc_set_error("no CUDA device"); return SEVC_ERR_CUDA; }
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) { sevc_set_error("device index %d out of range", dev); return SEVC_ERR_ARG; }
+    curandState *scratch;
+    {
+        /* the array's host-side name is not a device address: resolve it
+         * once per device, with that device current */
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            curandState *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_rng);
+            if (e != cudaSuccess || !p) {
+                sevc_set_error("cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+                return SEVC_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    /* every state is re-seeded by curand_init, so nothing left by an
+     * earlier call survives into the draws */
+    COUNT_LAUNCHES(1), k_rng_init<<<(nstreams + 255) / 256, 256, 0, s>>>(scratch, nstreams);
+    COUNT_LAUNCHES(1), k_rng_draw<<<(nstreams + 255) / 256, 256, 0, s>>>(scratch, nstreams, ndraws, d_out);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { sevc_set_error("sevc_rng_record_noalloc: %s", cudaGetErrorString(e)); return SEVC_ERR_CUDA; }
+    return SEVC_OK;
 }

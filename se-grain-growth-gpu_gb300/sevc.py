@@ -20,7 +20,7 @@ STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "CAPACITY", 4: "NONCONVERGED", 5: "TO
 EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_from_arrays", "sevc_destroy", "sevc_load_mesh_host",
            "sevc_step", "sevc_run_steps", "sevc_should_continue", "sevc_export_text", "sevc_get_state",
            "sevc_mesh_sizes", "sevc_check_data", "sevc_run_program", "sevc_rng_record", "sevc_set_profiling",
-           "sevc_get_profile", "sevc_last_error", "sevc_set_exact_all"]
+           "sevc_get_profile", "sevc_last_error", "sevc_set_exact_all", "sevc_rng_record_noalloc"]
 
 
 class SevcError(RuntimeError):
@@ -147,6 +147,14 @@ def rng_record(nstreams, ndraws):
     out = np.empty((nstreams, ndraws), np.float64)
     _check(lib().sevc_rng_record(nstreams, ndraws, out.ctypes.data))
     return out
+
+
+def rng_record_noalloc(nstreams, ndraws, d_out, stream=None):
+    """Allocation-free record into caller-owned DEVICE memory `d_out`
+    (an integer device address); asynchronous on `stream`."""
+    L = lib()
+    L.sevc_rng_record_noalloc.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    _check(L.sevc_rng_record_noalloc(nstreams, ndraws, C.c_void_p(d_out), C.c_void_p(stream)))
 
 
 class Engine:
