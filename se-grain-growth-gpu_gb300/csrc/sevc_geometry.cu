@@ -159,16 +159,19 @@ __device__ __noinline__ void grain_fd_generic(const DevMesh &m, int g, const int
     }
 }
 
-/* grain pass over grains ordered by side count (warps see one N).  The
- * pass is FP64-latency bound: capping registers at 128 (4 blocks of 128
- * per SM) measured 9% faster on the 1M-grain mesh than the compiler's
- * 218-register choice, despite a few spills; an 80-register cap gained
- * nothing more. */
-__global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int *perm, const int *total)
+/* grain pass over the grains of fewer than WIDE_SIDES sides, ordered by
+ * side count (warps see one N), most sides first so that the longest
+ * blocks start in the first wave.  The pass is FP64-latency bound:
+ * capping registers at 128 (4 blocks of 128 per SM) measured 9% faster on
+ * the 1M-grain mesh than the compiler's 218-register choice, despite a few
+ * spills; an 80-register cap gained nothing more. */
+constexpr int WIDE_SIDES = 11;
+__global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int *perm, const int *vbucket)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *total) return;
-    int g = perm[i];
+    int total = vbucket[VB_START(WIDE_SIDES)];
+    if (i >= total) return;
+    int g = perm[total - 1 - i];
     const int *L = m.glist + (size_t)SEVC_MAXV * g;
     int n = m.gvlen[g];
     switch (n) {
@@ -181,6 +184,76 @@ __global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int
     case 9: grain_fd_fixed<9>(m, g, L); break;
     case 10: grain_fd_fixed<10>(m, g, L); break;
     default: grain_fd_generic(m, g, L, n); break;
+    }
+}
+
+/* area_stream over a polygon staged in shared memory (raw positions P[k]
+ * of vertex k), same operations in the same order. */
+__device__ __forceinline__ double area_shared(const double2 *P, int n, int ps, double2 pp, double D)
+{
+    double area = 0;
+    if (n > 0) {
+        double2 r0 = (ps == 0) ? pp : P[0];
+        double ax = 0, ay = 0, rx = r0.x, ry = r0.y;
+        for (int k = 1; k < n; k++) {
+            double2 r = (k == ps) ? pp : P[k];
+            double nx = ax + wrapd(r.x, rx, D);
+            double ny = ay + wrapd(r.y, ry, D);
+            if (k > 1) area += ax * ny - ay * nx;
+            ax = nx; ay = ny; rx = r.x; ry = r.y;
+        }
+        area = add_closing_term(area, ax, ay);
+    }
+    return area * 0.5;
+}
+
+/* grain pass over the grains of WIDE_SIDES or more sides (the tail of the
+ * side-count order): one warp per grain, polygon staged in shared memory.
+ * The 2n+1 areas of a grain (vertex p moved along x: task 2p, along y:
+ * task 2p+1, unmoved: task 2n) are spread over the lanes, so a grain of
+ * up to 15 sides costs one polygon walk per lane.  A thread per grain
+ * would walk 2n+1 polygons of n dependent loads each and hold up the
+ * whole pass. */
+constexpr int WIDE_WARPS = 4;
+__global__ void __launch_bounds__(32 * WIDE_WARPS) k_grain_fd_wide(DevMesh m, const int *perm, const int *vbucket,
+                                                                  const int *total)
+{
+    __shared__ double2 poly[WIDE_WARPS][SEVC_MAXV];
+    __shared__ double area[WIDE_WARPS][2 * SEVC_MAXV + 1];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double2 *P = poly[w];
+    double *R = area[w];
+    int first = vbucket[VB_START(WIDE_SIDES)], end = *total;
+    int nwarps = gridDim.x * WIDE_WARPS;
+    const double D = m.D;
+    for (int i = first + blockIdx.x * WIDE_WARPS + w; i < end; i += nwarps) {
+        int g = perm[i];
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        int n = m.gvlen[g];
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) P[k] = m.pos[L[k]];
+        __syncwarp();
+        for (int t = lane; t <= 2 * n; t += 32) {
+            int p = t >> 1;
+            double2 pp = make_double2(0, 0);
+            if (t < 2 * n) {
+                double2 q = P[p];
+                pp = (t & 1) ? make_double2(dmod(q.x, D), dmod(q.y + SEVC_GRAD_EPS_D, D))
+                             : make_double2(dmod(q.x + SEVC_GRAD_EPS_D, D), dmod(q.y, D));
+            } else {
+                p = -1;
+            }
+            R[t] = area_shared(P, n, p, pp, D);
+        }
+        __syncwarp();
+        double A = R[2 * n];
+        double se = m.gse[g];
+        if (lane == 0) {
+            m.garea[g] = A;
+            m.gq[g] = se * A / n;
+        }
+        double absA = dabs(A);
+        for (int p = lane; p < n; p += 32) put_contrib(m, g, L[p], se, absA, R[2 * p], R[2 * p + 1]);
     }
 }
 
@@ -513,7 +586,8 @@ void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s)
     COUNT_LAUNCHES(1), k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
     COUNT_LAUNCHES(1), k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
     COUNT_LAUNCHES(1), k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
-    COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.n_perm);
+    COUNT_LAUNCHES(1), k_grain_fd_wide<<<2 * 152, 32 * WIDE_WARPS, 0, s>>>(m, x.perm, x.vbucket, x.n_perm);
+    COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.vbucket);
 }
 
 /* the unsorted per-grain pass, kept for A/B timing */
