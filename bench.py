@@ -100,6 +100,120 @@ def make_mesh(n, seed, cache=None):
     return mesh
 
 
+def make_ensemble(n_inst, lo, hi, seed, cache=None):
+    """n_inst periodic Voronoi meshes, grain counts uniform in [lo, hi],
+    per-instance seeds, stored energy U[0,1) (rescaled to [0, 0.5] by
+    SE_min/SE_max in the options)."""
+    import numpy as np
+    key = "%d_%d_%d_%d" % (n_inst, lo, hi, seed)
+    if cache and os.path.exists(cache):
+        z = np.load(cache)
+        if str(z["key"]) == key:
+            return [{f: z["%s%d" % (f, i)] for f in ("xy", "ridges", "oris", "se")} for i in range(n_inst)]
+    import meshgen
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(lo, hi + 1, n_inst)
+    meshes = [meshgen.make_inputs(int(n), seed * 100003 + i) for i, n in enumerate(sizes)]
+    if cache:
+        np.savez(cache, key=key, **{"%s%d" % (f, i): m[f] for i, m in enumerate(meshes)
+                                    for f in ("xy", "ridges", "oris", "se")})
+    return meshes
+
+
+def ensemble_options(mod, n):
+    """Unit square, gamma = 1, SE U[0, 0.5], dt = 1e-6; nucleation on with
+    dtau = 0.1 (a rate of 1e-3 per grain per unit time at 10,000 grains, one
+    Metropolis attempt per dtau as the reference does)."""
+    kw = dict(n_grains=n, dt=1e-6, dtau=0.1, nucleation_gap=100000, domain_bound=1.0, GB_eps=0.0, GB_scaling=1.0,
+              SE_eps=1.0, SE_min=0.0, SE_max=0.5, do_nucleation=1, MC_k=1.0, nmax=10 ** 8, tmax=-1,
+              snap_gap=10 ** 8, min_grains=-1, n_blocks=32, n_threads=256)
+    o = mod.default_options(**kw)
+    o.min_grains = -1
+    return o
+
+
+def run_ensemble(n_inst, lo, hi, steps, warmup, seed=7, cache=None):
+    """Batched handle against the same instances run one after another as
+    plain handles (each computing every output, like the batch).  Times are
+    wall clock around the steps (the host round trips of every step are
+    part of what batching removes)."""
+    import sevc
+    t0 = time.time()
+    meshes = make_ensemble(n_inst, lo, hi, seed, cache)
+    gen_s = time.time() - t0
+    grains = [len(m["oris"]) for m in meshes]
+    opt = ensemble_options(sevc, grains[0])
+    batch = sevc.Engine.from_batch(opt, meshes)
+    g = sum(grains)
+    for _ in range(warmup):
+        g = batch.step().curr_n_grains
+    vs, ms = 0, 0.0
+    w0 = time.time()
+    for _ in range(steps):
+        vs += 2 * g
+        info = batch.step()
+        ms += info.gpu_ms
+        g = info.curr_n_grains
+    batch_wall = time.time() - w0
+    batch.close()
+    seq_wall, seq_vs = 0.0, 0
+    for m in meshes:
+        o = ensemble_options(sevc, len(m["oris"]))
+        e = sevc.Engine.from_arrays(o, m["xy"], m["ridges"], m["oris"], m["se"])
+        e.set_exact_all(True)
+        gi = len(m["oris"])
+        for _ in range(warmup):
+            gi = e.step().curr_n_grains
+        w0 = time.time()
+        for _ in range(steps):
+            seq_vs += 2 * gi
+            gi = e.step().curr_n_grains
+        seq_wall += time.time() - w0
+        e.close()
+    return {"instances": n_inst, "grains_range": [lo, hi], "total_grains": int(sum(grains)), "steps": steps,
+            "warmup": warmup, "batch_ms_per_step": 1e3 * batch_wall / steps,
+            "batch_device_ms_per_step": ms / steps, "sequential_ms_per_step": 1e3 * seq_wall / steps,
+            "batch_vertex_steps_per_s": vs / batch_wall, "sequential_vertex_steps_per_s": seq_vs / seq_wall,
+            "speedup": seq_wall / batch_wall, "mesh_generation_s": round(gen_s, 1),
+            "timing": "wall clock around the steps, inputs resident on the device"}
+
+
+def run_adjoint(n=10000, steps=2000, every=100, dt=1e-6, seed=17, nbins=20, amax=3.0):
+    """Forward + adjoint of the 10,000-grain differentiable workload: unit
+    square, SE U[0, 0.5], gamma = mu = 1, histogram loss after `steps`
+    steps, checkpoints every `every` steps.  Wall-clock times of the steps
+    (forward, with the tape) and of the adjoint call (replay + backward)."""
+    import numpy as np
+    import sevc
+    import meshgen
+    mesh = meshgen.make_inputs(n, seed)
+    se = np.random.default_rng(seed).uniform(0.0, 0.5, n)
+    o = sevc.default_options(n_grains=n, dt=dt, dtau=1.0, domain_bound=1.0, GB_eps=0.0, GB_scaling=1.0, SE_eps=1.0,
+                             SE_min=999.0, SE_max=999.0, do_nucleation=0, nmax=10 ** 8, tmax=-1, snap_gap=10 ** 8,
+                             n_blocks=32, n_threads=256)
+    o.min_grains = -1
+    eng = sevc.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    eng.set_stored_energy(se)
+    eng.tape_start(every)
+    ev = np.zeros(3, np.int64)
+    t0 = time.time()
+    for _ in range(steps):
+        i = eng.step()
+        ev += (i.n_flips, i.n_removals, i.n_two_three)
+    fwd = time.time() - t0
+    h = eng.area_histogram(nbins, amax)
+    target = np.full(nbins, 1.0 / nbins)
+    t0 = time.time()
+    gse, ggam, gmu = eng.adjoint_histogram(nbins, amax, 2.0 * (h - target) / nbins)
+    bwd = time.time() - t0
+    eng.close()
+    return {"grains": n, "steps": steps, "checkpoint_every": every, "dt": dt, "forward_s": fwd, "backward_s": bwd,
+            "backward_forward_ratio": bwd / fwd, "events": {"flips": int(ev[0]), "removals": int(ev[1]),
+                                                           "two_three": int(ev[2])},
+            "grad_gb_scaling": ggam, "grad_mu": gmu,
+            "timing": "wall clock; forward = the taped steps, backward = sevc_adjoint_histogram"}
+
+
 def algorithmic_bytes_per_step(nv):
     """Compulsory traffic of one step per vertex (131.5 B per vertex-step:
     72*V + 25*B + 20*G + 4*sum(vlen) with B = 1.5V, G = V/2, sum(vlen) = 3V)."""
@@ -117,6 +231,17 @@ KERNEL_BYTES = {
     # per boundary: ends 8 + positions 32 + velocities 32 + t_ext 8 + flags 2
     "text_label": ("boundaries", 8 + 32 + 32 + 8 + 2),
 }
+
+# DRAM bytes (read + write) per unit measured by ncu for each kernel phase on
+# the 200K-grain mesh (profiles/k_grain_fd_sorted_200k_grains.md,
+# profiles/k_vertex_fd_200k_grains.md); traffic grows with the units
+# processed, so a full launch is scaled by its units.
+NCU_TRAFFIC_PER_UNIT = {
+    "grain_fd": (52.14e6 + 8.06e6) / 200000,
+    "vertex_fd": (54.86e6 + 1.71e6) / 400000,
+}
+# FP64 pipe activity of the same captures (of elapsed cycles)
+NCU_FP64_ACTIVE = {"grain_fd": 0.726, "vertex_fd": 0.783}
 
 
 def run_engine(args):
@@ -196,8 +321,14 @@ def run_engine(args):
         "e2e": {"value": e_vsteps / e_wall, "unit": UNIT, "h2d_bytes_per_step": host_bytes / args.steps,
                 "d2h_bytes_per_step": step_info_bytes + state_bytes / args.steps},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
-                     "note": "FP64-pipe bound on GB300; see DESIGN.md"},
+                     "frac": achieved / peak,
+                     "traffic": NCU_TRAFFIC_PER_UNIT[dom] * units if dom in NCU_TRAFFIC_PER_UNIT else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on the 200K-grain mesh, "
+                                       "scaled by units per launch",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                     "fp64_pipe_active_ncu": NCU_FP64_ACTIVE.get(dom),
+                     "note": "FP64-issue bound on GB300 (DRAM idle); fp64_pipe_active_ncu is the fraction "
+                             "of elapsed cycles the FP64 pipe was busy in the ncu capture"},
         "kernel_ms_share": {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "step_bytes_rate_gbs": algorithmic_bytes_per_step(2 * n) * args.steps / (ms / 1e3) / 1e9,
         "gpu_launches": sum(i.kernel_launches for i in infos),
@@ -206,6 +337,11 @@ def run_engine(args):
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(mesh, n, args.cpu_steps)
+    if args.ensemble_sample > 0:
+        line["ensemble"] = run_ensemble(args.ensemble_sample, args.ensemble_grains[0], args.ensemble_grains[1],
+                                        10, 3, cache=args.ensemble_cache)
+    if args.adjoint_sample:
+        line["adjoint"] = run_adjoint()
     print(json.dumps(line))
 
 
@@ -275,6 +411,15 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble"],
+                    help="ensemble: batched ensemble against sequential plain runs, its own JSON line")
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--ensemble-grains", type=int, nargs=2, default=[500, 20000])
+    ap.add_argument("--ensemble-sample", type=int, default=64,
+                    help="instances of the ensemble measurement added to the single-run line (0: none)")
+    ap.add_argument("--ensemble-cache", default=None, help="npz file to reuse the generated ensemble")
+    ap.add_argument("--no-adjoint-sample", dest="adjoint_sample", action="store_false",
+                    help="skip the forward/adjoint timing added to the single-run line")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -283,6 +428,15 @@ def main():
         return
     import __graft_entry__
     __graft_entry__.build()
+    if args.workload == "ensemble":
+        r = run_ensemble(args.instances, args.ensemble_grains[0], args.ensemble_grains[1], args.steps, args.warmup,
+                         cache=args.ensemble_cache)
+        print(json.dumps({"metric": "ensemble speedup vs sequential plain runs", "value": r["speedup"],
+                          "unit": "x", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": r["batch_ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded periodic Voronoi)",
+                          "config": {"workload": "batched ensemble", **r}}))
+        return
     run_engine(args)
 
 

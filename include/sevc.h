@@ -165,6 +165,88 @@ sevc_status sevc_rng_record(int nstreams, int ndraws, double *out);
  * the GPU race and must be serialised by the caller. */
 sevc_status sevc_rng_record_noalloc(int nstreams, int ndraws, double *d_out, void *stream);
 
+/* ---- batched ensembles (no counterpart in the reference) ----
+ *
+ * One handle advancing `ninst` independent microstructures together: the
+ * meshes are stored one after another in every device array and each
+ * kernel launch of a step covers all of them, so hundreds of small runs
+ * cost one run's launches and host round trips.  Every instance follows
+ * exactly the plain method: instance i, stepped in a batch, produces bit
+ * for bit what a plain handle created from the same arrays produces with
+ * sevc_set_exact_all(1) (its own polling convergence, 2x3 loop, event
+ * order and its own copy of the 8192 random streams).  Options are shared
+ * except n_grains, which is each instance's grain count.  The batch runs
+ * until the shared tmax / nmax; min_grains is reported per instance
+ * (keep_going of sevc_instance_info) but stops nothing.  Outputs are
+ * complete on every step.
+ *
+ * Arrays of instance i: nv[i] positions xy[i] (interleaved), nb[i] ridges
+ * ridges[i] (pairs), ng[i] orientations oris[i] and stored energies se[i],
+ * as in sevc_create_from_arrays. */
+sevc_status sevc_create_batch(const sevc_options *opt, int ninst, const int *nv, const double *const *xy,
+                              const int *nb, const int32_t *const *ridges, const int *ng, const double *const *oris,
+                              const double *const *se, sevc_handle **out);
+sevc_status sevc_instance_count(const sevc_handle *h, int *ninst);
+/* ninst+1 offsets each: instance i owns global vertex indices
+ * [voff[i], voff[i+1]) etc. of sevc_get_state (any pointer may be NULL) */
+sevc_status sevc_instance_ranges(const sevc_handle *h, int32_t *voff, int32_t *boff, int32_t *goff);
+/* the summary of the last step for one instance */
+sevc_status sevc_instance_info(const sevc_handle *h, int inst, sevc_step_info *info);
+/* export_data (src/io.h:280-377) of one instance, in its own indices */
+sevc_status sevc_export_instance_text(sevc_handle *h, int inst, const char *path, double time);
+
+/* ---- checkpoint files and statistics (no counterpart in the reference) ----
+ *
+ * A checkpoint is the handle's whole device state (mesh, scratch, random
+ * streams, polling buffers) plus its host run state, in one binary file;
+ * loading it into a handle created from the same inputs and options
+ * resumes the run bit for bit. */
+sevc_status sevc_checkpoint_save(sevc_handle *h, const char *path);
+sevc_status sevc_checkpoint_load(sevc_handle *h, const char *path);
+
+typedef struct sevc_grain_stats_t {
+    int n_grains;        /* enabled grains (current_n_grains, src/calculus.h:264) */
+    int n_three_sided;
+    double mean_area, std_area, min_area, max_area;   /* of |A| */
+    double mean_sides;
+} sevc_grain_stats_t;
+/* grain-size statistics of one instance (inst = -1: all grains) */
+sevc_status sevc_grain_stats(sevc_handle *h, int inst, sevc_grain_stats_t *out);
+
+/* ---- parameters and the adjoint (no counterpart in the reference) ----
+ *
+ * Mobility mu multiplies every vertex velocity (the reference has none:
+ * mu = 1, which changes no bit).  GB_scaling and the per-grain stored
+ * energies (after the loader's scaling) can be replaced between runs.
+ * None of the three may change while a tape is recording. */
+sevc_status sevc_set_mobility(sevc_handle *h, double mu);
+sevc_status sevc_set_gb_scaling(sevc_handle *h, double gb_scaling);
+sevc_status sevc_set_stored_energy(sevc_handle *h, const double *se /* ng values */);
+
+/* Gradients of a grain-size statistic with respect to the per-grain stored
+ * energies, GB_scaling and the mobility, by a hand-written adjoint of the
+ * velocity, event and translation kernels.  sevc_tape_start checkpoints
+ * the whole device state now and every `checkpoint_every` steps after; the
+ * adjoint replays one segment at a time from its checkpoint, recording the
+ * mesh and the position-moving events of each step, and runs the steps
+ * backward.  Topology changes are followed (flips, 2x3 and 3-sided
+ * removals move or disable vertices; their discrete decisions carry no
+ * gradient).  Runs with nucleation are not covered (SEVC_ERR_ARG).
+ * Memory: one copy of the device state per checkpoint plus about 600 bytes
+ * per grain per step of one segment. */
+sevc_status sevc_tape_start(sevc_handle *h, int checkpoint_every);
+sevc_status sevc_tape_stop(sevc_handle *h);
+/* Smoothed histogram of normalised grain areas a = |A| N / (domain area)
+ * (N enabled grains, so a has mean 1 when all grains are counted):
+ * hist[k] = (1/N) sum_g B2(a_g / w - k - 1/2), w = amax / nbins, B2 the
+ * quadratic B-spline; nbins <= 1024. */
+sevc_status sevc_area_histogram(sevc_handle *h, int nbins, double amax, double *hist);
+/* Given dloss/dhist (nbins values) at the current state, write dloss/dSE
+ * (ng values, may be NULL), dloss/dGB_scaling and dloss/dmu, for the steps
+ * taken since sevc_tape_start.  The handle's state is left unchanged. */
+sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const double *dloss_dhist,
+                                   double *grad_se, double *grad_gb_scaling, double *grad_mu);
+
 /* Output-only fields (extinction times of boundaries that cannot flip,
  * dA/dt of grains that cannot vanish) are computed only on steps that can
  * export a snapshot (sevc_step_info.outputs_complete); exported snapshots

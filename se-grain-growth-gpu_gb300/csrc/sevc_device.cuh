@@ -64,18 +64,52 @@ struct DevMesh {
     int *fixlist, *nfix;
     int *modlist, *nmod;
     int *err;            /* ERRB_* bits */
-    int *evt;            /* event counters, EVT_* */
+    int *evt;            /* event counters, EVT_COUNT per instance */
+    /* Instances.  A batched handle holds several independent meshes one
+     * after another in every array (indices are global, no edge crosses an
+     * instance); instance i owns vertices [voff[i], voff[i+1]) and likewise
+     * boundaries and grains.  A plain handle is one instance. */
+    int ninst;
+    int *voff, *boff, *goff;
+    int *binst, *ginst;  /* instance of every boundary / grain */
+    int *pdone;          /* per instance: polling has converged this step */
+    /* position-moving events of the step in application order, recorded
+     * only while an adjoint tape replays a segment (elog == nullptr else) */
+    struct EventRec *elog;
+    int *nelog;
+    int elog_cap;
     /* grains whose list changed since the step's grain pass (their area is
      * recomputed after removals, src/main.cu:266) */
     int *adirty, *nadirty;
     uint8_t *gadirty;
-    /* slots that ever held a nucleated grain, ascending */
+    /* slots that ever held a nucleated grain, ascending; instance i's
+     * entries start at nlist[goff[i]], nnlist[i] of them */
     int *nlist, *nnlist;
     /* boundaries whose extinction time must be exact this step */
     uint8_t *bforce;
 };
 
 enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
+
+/* one position-moving event: a T1 flip (vertices a, b move to their
+ * midpoint) or a 3-sided grain removal (a moves to the length-weighted
+ * point of a, b, c; b and c are disabled), with the positions it read */
+enum { EV_FLIP = 1, EV_REMOVE = 2 };
+struct EventRec {
+    int type, a, b, c;
+    double2 pa, pb, pc;
+};
+
+__device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int b, int c, double2 pa, double2 pb,
+                                          double2 pc)
+{
+    if (!m.elog) return;
+    int i = atomicAdd(m.nelog, 1);
+    if (i >= m.elog_cap) { atomicOr(m.err, ERRB_WORKLIST); return; }
+    EventRec r;
+    r.type = type; r.a = a; r.b = b; r.c = c; r.pa = pa; r.pb = pb; r.pc = pc;
+    m.elog[i] = r;
+}
 
 /* ---- periodic geometry, src/geometry.h:133-331 ----
  * Comparisons, absolute values and min/max work on the IEEE-754 bit
@@ -203,5 +237,16 @@ __device__ __forceinline__ void set_slot3(int4 &s, int i, int v)
 __device__ __forceinline__ int other_end(int2 e, int v) { return e.x == v ? e.y : e.x; }
 
 __device__ __forceinline__ void raise_err(const DevMesh &m, int bits) { atomicOr(m.err, bits); }
+
+/* first position of an ascending list whose value is >= x */
+__device__ __forceinline__ int lower_bound_i(const int *a, int n, int x)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
 
 #endif

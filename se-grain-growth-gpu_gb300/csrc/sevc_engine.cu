@@ -11,6 +11,7 @@
 #include "sevc_internal.h"
 #include "sevc_host.h"
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -28,6 +29,30 @@ long long sevc_kernel_launches = 0;
 
 struct ProfEntry { double ms = 0; int64_t launches = 0; };
 
+/* host part of the run state (the device part is the handle's block) */
+struct RunState {
+    int n = 0, curr_n_grains = 0;
+    double t = 0, nucleated_area = 0;
+    std::vector<int> icurr, iallow;
+    std::vector<double> iarea;
+};
+
+/* Adjoint tape: checkpoints of the whole device block every `every` steps;
+ * the backward pass replays one segment at a time from its checkpoint,
+ * recording what the adjoint of each step needs. */
+struct Tape {
+    int every = 0;                 /* 0: not taping */
+    long long nsteps = 0;          /* steps taken since the tape started */
+    bool replaying = false;
+    std::vector<void *> ckpt;      /* device copies, state after k*every steps */
+    std::vector<RunState> runs;
+    void *rec = nullptr;           /* per-step records of one segment */
+    size_t rec_step_bytes = 0;
+    int rec_steps = 0, log_cap = 0;
+    void *adj = nullptr;           /* AdjointBuffers storage */
+    size_t adj_bytes = 0;
+};
+
 struct sevc_handle {
     sevc_options opt;
     int nv = 0, nb = 0, ng = 0;
@@ -37,12 +62,24 @@ struct sevc_handle {
     DevScratch x{};
     StepParams p{};
     /* run state, src/main.cu:29-113 */
-    int n = 0, curr_n_grains = 0, allow_nucleation = 0;
+    int n = 0, curr_n_grains = 0;
     double t = 0, nucleated_area = 0;
     int polling_cap = 100000;
     int exact_all = 0;
-    /* pinned readback */
+    /* instances (one for a plain handle): entity offsets, initial grain
+     * count (the n_grains of src/main.cu:137), per-instance run state and
+     * the per-instance summary of the last step */
+    int ninst = 1;
+    std::vector<int> voff, boff, goff, ng0, icurr, iallow;
+    std::vector<double> iarea;
+    std::vector<sevc_step_info> iinfo;
+    /* pinned readback / upload buffers */
     int *h_ctr = nullptr;
+    int *h_big = nullptr;
+    size_t h_big_ints = 0;
+    int *h_on = nullptr;   /* per instance: nucleation attempt this step */
+    size_t dbytes = 0;     /* size of the device block */
+    Tape tape;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool profiling = false;
     std::map<std::string, ProfEntry> prof;
@@ -104,14 +141,19 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 /* one device allocation carved into every array */
 bool alloc_device(sevc_handle *h)
 {
-    size_t V = h->nv, B = h->nb, G = h->ng;
-    int grid = h->p.n_blocks * h->p.n_threads;
+    size_t V = h->nv, B = h->nb, G = h->ng, I = h->ninst;
+    size_t grid = (size_t)h->p.n_blocks * h->p.n_threads;
     size_t maxn = B > G ? B : G;
     size_t tiles = (maxn + 4095) / 4096 + 1;
+    size_t nrng = h->opt.do_nucleation ? (size_t)RNG_GRID * I : RNG_GRID;
     struct Req { void **p; size_t bytes; };
     DevMesh &m = h->m;
     DevScratch &x = h->x;
     std::vector<Req> r = {
+        { (void **)&m.voff, (I + 1) * 4 }, { (void **)&m.boff, (I + 1) * 4 }, { (void **)&m.goff, (I + 1) * 4 },
+        { (void **)&m.binst, B * 4 }, { (void **)&m.ginst, G * 4 }, { (void **)&m.pdone, I * 4 },
+        { (void **)&x.pblock, I * h->p.n_blocks * 4 }, { (void **)&x.piters, I * 4 }, { (void **)&x.nrun, 4 },
+        { (void **)&x.segcnt, I * TWO_THREE_PASSES * 4 }, { (void **)&x.nucl_on, I * 4 },
         { (void **)&m.pos, V * 16 }, { (void **)&m.vel, V * 16 }, { (void **)&m.terms, V * 32 },
         { (void **)&m.contrib, V * 48 }, { (void **)&m.venergy, V * 8 }, { (void **)&m.ven, V },
         { (void **)&m.vb, V * 16 }, { (void **)&m.vg, V * 16 }, { (void **)&m.vmod, V * 64 },
@@ -123,15 +165,15 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.gdadt, G * 8 }, { (void **)&m.gori, G * 8 }, { (void **)&m.gse, G * 8 },
         { (void **)&m.gq, G * 8 }, { (void **)&m.gen, G }, { (void **)&m.gcand, G }, { (void **)&m.gfix, G },
         { (void **)&m.gtype, G }, { (void **)&m.fixlist, G * 4 }, { (void **)&m.nfix, 4 }, { (void **)&m.nmod, 4 },
-        { (void **)&m.err, 16 }, { (void **)&m.evt, 16 },
+        { (void **)&m.err, 16 }, { (void **)&m.evt, I * EVT_COUNT * 4 },
         { (void **)&x.list_a, maxn * 4 }, { (void **)&x.list_b, maxn * 4 }, { (void **)&x.list_c, maxn * 4 },
         { (void **)&x.n_a, 4 }, { (void **)&x.n_b, 4 }, { (void **)&x.n_c, 4 }, { (void **)&x.blockcnt, tiles * 4 },
-        { (void **)&x.extra, 1024 * 4 }, { (void **)&x.threadfail, (size_t)grid * 4 },
-        { (void **)&x.block_area, (size_t)h->p.n_blocks * 8 }, { (void **)&x.counters, CTR_COUNT * 4 },
-        { (void **)&x.rng, 8192 * sizeof(curandState) }, { (void **)&x.rng_saved, 8192 * sizeof(curandState) },
-        { (void **)&x.nucl_buf, 64 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
+        { (void **)&x.extra, I * EXTRA_CAP * 4 }, { (void **)&x.threadfail, I * grid * 4 },
+        { (void **)&x.block_area, I * h->p.n_blocks * 8 }, { (void **)&x.counters, I * CTR_COUNT * 4 },
+        { (void **)&x.rng, nrng * sizeof(curandState) }, { (void **)&x.rng_saved, nrng * sizeof(curandState) },
+        { (void **)&x.nucl_buf, I * 64 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
         { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
-        { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, 4 }, { (void **)&m.bforce, B },
+        { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.bforce, B },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -139,8 +181,10 @@ bool alloc_device(sevc_handle *h)
     if (!cuda_ok(cudaMalloc(&base, total), "cudaMalloc mesh")) return false;
     if (!cuda_ok(cudaMemsetAsync(base, 0, total, h->stream), "memset")) return false;
     h->dblock = base;
+    h->dbytes = total;
     for (auto &q : r) { *q.p = base; base += align256(q.bytes); }
     m.nv = h->nv; m.nb = h->nb; m.ng = h->ng; m.D = h->opt.domain_bound;
+    m.ninst = h->ninst;
     return true;
 }
 
@@ -183,7 +227,9 @@ bool upload(sevc_handle *h, const sevc_mesh_host &hm)
         !put(h->m.garea, hm.garea, G * 8) || !put(h->m.gdadt, hm.gdadt, G * 8) || !put(h->m.gori, hm.gori, G * 8) ||
         !put(h->m.gse, hm.gse, G * 8) || !put(h->m.gen, hm.gen, G) || !put(h->m.gtype, hm.gtype, G))
         return false;
-    return true;
+    size_t I1 = h->ninst + 1;
+    return put(h->m.voff, h->voff.data(), I1 * 4) && put(h->m.boff, h->boff.data(), I1 * 4) &&
+           put(h->m.goff, h->goff.data(), I1 * 4);
 }
 
 sevc_status validate(const sevc_options *o)
@@ -214,24 +260,65 @@ sevc_status require_device()
     return SEVC_OK;
 }
 
-sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handle **out)
+/* `offs` = 3 x (ninst + 1) entity offsets (vertices, boundaries, grains)
+ * and `ng0` the initial grain count of each instance; NULL for a plain
+ * handle (one instance holding everything, n_grains from the options). */
+sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handle **out, int ninst = 1,
+                             const std::vector<int> *offs = nullptr, const std::vector<int> *ng0 = nullptr)
 {
     *out = nullptr;
     if (require_device()) return SEVC_ERR_CUDA;
     sevc_handle *h = new sevc_handle();
     h->opt = *opt;
     h->nv = hm->m.nv; h->nb = hm->m.nb; h->ng = hm->m.ng;
+    h->ninst = ninst;
+    if (offs) {
+        h->voff.assign(offs->begin(), offs->begin() + ninst + 1);
+        h->boff.assign(offs->begin() + ninst + 1, offs->begin() + 2 * (ninst + 1));
+        h->goff.assign(offs->begin() + 2 * (ninst + 1), offs->end());
+        h->ng0 = *ng0;
+    } else {
+        h->voff = { 0, h->nv };
+        h->boff = { 0, h->nb };
+        h->goff = { 0, h->ng };
+        h->ng0 = { opt->n_grains };
+    }
+    h->icurr.resize(ninst);
+    h->iallow.assign(ninst, 0);
+    h->iarea.assign(ninst, 0.0);
+    h->iinfo.assign(ninst, sevc_step_info{});
+    int max_ng = 0;
+    for (int i = 0; i < ninst; i++) {
+        h->icurr[i] = h->goff[i + 1] - h->goff[i];
+        if (h->icurr[i] > max_ng) max_ng = h->icurr[i];
+    }
     h->p.dt = opt->dt; h->p.eps = opt->GB_eps; h->p.scaling = opt->GB_scaling; h->p.MC_k = opt->MC_k;
     h->p.n_blocks = opt->n_blocks; h->p.n_threads = opt->n_threads;
+    h->p.ninst = ninst;
+    h->p.max_inst_ng = max_ng;
+    h->p.mu = 1.0;
     h->curr_n_grains = h->ng;
+    /* readback: counters, events, polling iterations, 2x3 counts per instance */
+    h->h_big_ints = (size_t)ninst * (CTR_COUNT + EVT_COUNT + 1 + TWO_THREE_PASSES) + 64;
     if (!cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream") ||
-        !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") || !alloc_device(h) || !upload(h, hm->m)) {
+        !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") ||
+        !cuda_ok(cudaMallocHost(&h->h_big, h->h_big_ints * sizeof(int)), "pinned") ||
+        !cuda_ok(cudaMallocHost(&h->h_on, ninst * sizeof(int)), "pinned") || !alloc_device(h) ||
+        !upload(h, hm->m)) {
         sevc_destroy(h);
         return SEVC_ERR_CUDA;
     }
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
-    launch_rng_init(h->x.rng, 8192, h->stream);                           /* src/main.cu:81 */
+    launch_fill_instance_ids(h->m, h->stream);
+    launch_rng_init(h->x.rng, RNG_GRID, h->stream);                       /* src/main.cu:81 */
+    if (h->opt.do_nucleation)                                             /* every instance gets the same streams */
+        for (int i = 1; i < ninst; i++)
+            if (!cuda_ok(cudaMemcpyAsync(h->x.rng + (size_t)i * RNG_GRID, h->x.rng, RNG_GRID * sizeof(curandState),
+                                         cudaMemcpyDeviceToDevice, h->stream), "rng copy")) {
+                sevc_destroy(h);
+                return SEVC_ERR_CUDA;
+            }
     if (!cuda_ok(cudaStreamSynchronize(h->stream), "init")) { sevc_destroy(h); return SEVC_ERR_CUDA; }
     *out = h;
     return SEVC_OK;
@@ -244,6 +331,50 @@ sevc_status read_ints(sevc_handle *h, const int *dsrc, int n, int *dst)
         return SEVC_ERR_CUDA;
     memcpy(dst, h->h_ctr, n * sizeof(int));
     return SEVC_OK;
+}
+
+RunState save_run(const sevc_handle *h)
+{
+    RunState r;
+    r.n = h->n;
+    r.curr_n_grains = h->curr_n_grains;
+    r.t = h->t;
+    r.nucleated_area = h->nucleated_area;
+    r.icurr = h->icurr;
+    r.iallow = h->iallow;
+    r.iarea = h->iarea;
+    return r;
+}
+void load_run(sevc_handle *h, const RunState &r)
+{
+    h->n = r.n;
+    h->curr_n_grains = r.curr_n_grains;
+    h->t = r.t;
+    h->nucleated_area = r.nucleated_area;
+    h->icurr = r.icurr;
+    h->iallow = r.iallow;
+    h->iarea = r.iarea;
+}
+bool tape_checkpoint(sevc_handle *h)
+{
+    void *ck = nullptr;
+    if (!cuda_ok(cudaMalloc(&ck, h->dbytes), "cudaMalloc checkpoint")) return false;
+    if (!cuda_ok(cudaMemcpyAsync(ck, h->dblock, h->dbytes, cudaMemcpyDeviceToDevice, h->stream), "checkpoint")) {
+        cudaFree(ck);
+        return false;
+    }
+    h->tape.ckpt.push_back(ck);
+    h->tape.runs.push_back(save_run(h));
+    return true;
+}
+void tape_free(sevc_handle *h)
+{
+    Tape &tp = h->tape;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void *p : tp.ckpt) cudaFree(p);
+    if (tp.rec) cudaFree(tp.rec);
+    if (tp.adj) cudaFree(tp.adj);
+    tp = Tape();
 }
 
 sevc_status err_bits_to_status(int bits)
@@ -292,12 +423,113 @@ sevc_status sevc_create_from_arrays(const sevc_options *opt, int nv, const doubl
     return st;
 }
 
+sevc_status sevc_create_batch(const sevc_options *opt, int ninst, const int *nv, const double *const *xy,
+                              const int *nb, const int32_t *const *ridges, const int *ng, const double *const *oris,
+                              const double *const *se, sevc_handle **out)
+{
+    if (!opt || !out || ninst < 1 || !nv || !xy || !nb || !ridges || !ng || !oris || !se) return SEVC_ERR_ARG;
+    if (require_device()) return SEVC_ERR_CUDA;
+    sevc_status st = validate(opt);
+    if (st) return st;
+    std::vector<sevc_hmesh> parts(ninst);
+    int built = 0;
+    auto free_parts = [&]() { for (int i = 0; i < built; i++) sevc_hmesh_free(&parts[i]); };
+    std::vector<int> offs(3 * (ninst + 1), 0), ng0(ninst);
+    int *vo = offs.data(), *bo = vo + ninst + 1, *go = bo + ninst + 1;
+    for (int i = 0; i < ninst; i++) {
+        if (!xy[i] || !ridges[i] || !oris[i] || !se[i]) { free_parts(); return SEVC_ERR_ARG; }
+        sevc_options oi = *opt;
+        oi.n_grains = ng[i];
+        int rc = sevc_host_build(&oi, nv[i], xy[i], nb[i], ridges[i], ng[i], oris[i], ng[i], se[i], &parts[i]);
+        if (rc) {
+            std::string why = sevc_last_error();
+            free_parts();
+            sevc_set_error("instance %d: %s", i, why.c_str());
+            return (sevc_status)rc;
+        }
+        built++;
+        const sevc_mesh_host &p = parts[i].m;
+        if ((long long)vo[i] + p.nv > 0x7fffffffLL || (long long)bo[i] + p.nb > 0x7fffffffLL ||
+            (long long)go[i] + p.ng > 0x7fffffffLL / SEVC_MAXV) {
+            free_parts();
+            sevc_set_error("batch too large for 32-bit indices");
+            return SEVC_ERR_ARG;
+        }
+        vo[i + 1] = vo[i] + p.nv;
+        bo[i + 1] = bo[i] + p.nb;
+        go[i + 1] = go[i] + p.ng;
+        ng0[i] = ng[i];
+    }
+    sevc_hmesh all;
+    if (sevc_hmesh_alloc(&all, vo[ninst], bo[ninst], go[ninst])) { free_parts(); return SEVC_ERR_CAPACITY; }
+    sevc_mesh_host &a = all.m;
+    auto shift = [](int32_t *dst, const int32_t *src, size_t n, int off) {
+        for (size_t k = 0; k < n; k++) dst[k] = src[k] >= 0 ? src[k] + off : src[k];
+    };
+    for (int i = 0; i < ninst; i++) {
+        const sevc_mesh_host &p = parts[i].m;
+        size_t v = vo[i], b = bo[i], g = go[i], V = p.nv, B = p.nb, G = p.ng;
+        double *vd[] = { a.px, a.py, a.vx, a.vy, a.venergy, a.vel_bnd_x, a.vel_grn_x, a.vel_bnd_y, a.vel_grn_y };
+        const double *vs[] = { p.px, p.py, p.vx, p.vy, p.venergy, p.vel_bnd_x, p.vel_grn_x, p.vel_bnd_y, p.vel_grn_y };
+        for (int f = 0; f < 9; f++) memcpy(vd[f] + v, vs[f], V * 8);
+        memcpy(a.ven + v, p.ven, V);
+        shift(a.vb + 3 * v, p.vb, 3 * V, bo[i]);
+        shift(a.vg + 3 * v, p.vg, 3 * V, go[i]);
+        shift(a.bini + b, p.bini, B, vo[i]);
+        shift(a.bend + b, p.bend, B, vo[i]);
+        double *bd[] = { a.benergy, a.blen, a.btext };
+        const double *bs[] = { p.benergy, p.blen, p.btext };
+        for (int f = 0; f < 3; f++) memcpy(bd[f] + b, bs[f], B * 8);
+        memcpy(a.ben + b, p.ben, B);
+        memcpy(a.bcand + b, p.bcand, B);
+        shift(a.glist + SEVC_MAXV * g, p.glist, SEVC_MAXV * G, vo[i]);
+        memcpy(a.gvlen + g, p.gvlen, G * 4);
+        double *gd[] = { a.garea, a.gdadt, a.gori, a.gse };
+        const double *gs[] = { p.garea, p.gdadt, p.gori, p.gse };
+        for (int f = 0; f < 4; f++) memcpy(gd[f] + g, gs[f], G * 8);
+        memcpy(a.gen + g, p.gen, G);
+        memcpy(a.gtype + g, p.gtype, G);
+    }
+    free_parts();
+    st = create_from_host(opt, &all, out, ninst, &offs, &ng0);
+    sevc_hmesh_free(&all);
+    return st;
+}
+
+sevc_status sevc_instance_count(const sevc_handle *h, int *ninst)
+{
+    if (!h || !ninst) return SEVC_ERR_ARG;
+    *ninst = h->ninst;
+    return SEVC_OK;
+}
+
+sevc_status sevc_instance_ranges(const sevc_handle *h, int32_t *voff, int32_t *boff, int32_t *goff)
+{
+    if (!h) return SEVC_ERR_ARG;
+    for (int i = 0; i <= h->ninst; i++) {
+        if (voff) voff[i] = h->voff[i];
+        if (boff) boff[i] = h->boff[i];
+        if (goff) goff[i] = h->goff[i];
+    }
+    return SEVC_OK;
+}
+
+sevc_status sevc_instance_info(const sevc_handle *h, int inst, sevc_step_info *info)
+{
+    if (!h || !info || inst < 0 || inst >= h->ninst) return SEVC_ERR_ARG;
+    *info = h->iinfo[inst];
+    return SEVC_OK;
+}
+
 void sevc_destroy(sevc_handle *h)
 {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->dblock) cudaFree(h->dblock);
     if (h->h_ctr) cudaFreeHost(h->h_ctr);
+    if (h->h_big) cudaFreeHost(h->h_big);
+    if (h->h_on) cudaFreeHost(h->h_on);
+    tape_free(h);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (auto e : h->evpool) cudaEventDestroy(e);
@@ -310,8 +542,9 @@ int sevc_should_continue(const sevc_handle *h)
 {
     const sevc_options &o = h->opt;
     int mg = o.min_grains;
-    return ((h->t <= o.tmax && o.tmax > 0) || (h->n <= o.nmax && o.nmax > 0)) &&
-           (h->curr_n_grains >= mg && mg > 0);
+    bool time_left = (h->t <= o.tmax && o.tmax > 0) || (h->n <= o.nmax && o.nmax > 0);
+    if (h->ninst > 1) return time_left;   /* a batch runs to the shared tmax / nmax */
+    return time_left && (h->curr_n_grains >= mg && mg > 0);
 }
 
 sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
@@ -321,6 +554,8 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     const sevc_options &o = h->opt;
     DevMesh &m = h->m;
     DevScratch &x = h->x;
+    const int I = h->ninst;
+    const bool batch = I > 1;
     sevc_step_info loc;
     memset(&loc, 0, sizeof loc);
     loc.n = h->n;
@@ -328,23 +563,32 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     long long launches0 = sevc_kernel_launches;
     cudaEventRecord(h->ev0, s);
     cudaMemsetAsync(m.err, 0, 16, s);
-    cudaMemsetAsync(m.evt, 0, 16, s);
+    cudaMemsetAsync(m.evt, 0, (size_t)I * EVT_COUNT * sizeof(int), s);
+    cudaMemsetAsync(x.segcnt, 0, (size_t)I * TWO_THREE_PASSES * sizeof(int), s);
     launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
 
     { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :124-130 */
-    if (h->curr_n_grains <= 5 * o.n_grains / 6) h->allow_nucleation = 1;                        /* :137 */
-    if (o.do_nucleation && o.nucleation_gap > 0 && (h->n % o.nucleation_gap) == 0 && h->allow_nucleation) {
+    int n_on = 0;                                                                                  /* :137-141 */
+    for (int i = 0; i < I; i++) {
+        if (h->icurr[i] <= 5 * h->ng0[i] / 6) h->iallow[i] = 1;
+        h->h_on[i] = o.do_nucleation && o.nucleation_gap > 0 && (h->n % o.nucleation_gap) == 0 && h->iallow[i];
+        n_on += h->h_on[i];
+    }
+    if (n_on) {
         loc.nucleation_attempted = 1;
+        if (!cuda_ok(cudaMemcpyAsync(x.nucl_on, h->h_on, I * sizeof(int), cudaMemcpyHostToDevice, s), "upload"))
+            return SEVC_ERR_CUDA;
         { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
         { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :171-181 */
     }
     { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, s); }                                         /* :127,:203 */
-    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, s); }                                          /* :133,:203 */
+    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, s); }                                 /* :133,:203 */
     /* The first count of the 2x3 loop (:228) depends only on the topology,
      * which nothing changes before that loop: count now, and learn whether
      * this step can disable boundaries other than 3-sided grains' or export.
      * Otherwise only 3-sided grains' dA/dt and the extinction times that
-     * matter are computed (see k_text_label). */
+     * matter are computed (see k_text_label).  A batched handle computes
+     * every output on every step. */
     int c23 = 0, n3 = 0;
     { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
     if (!cuda_ok(cudaMemcpyAsync(h->h_ctr, x.n_b, 4, cudaMemcpyDeviceToHost, s), "readback") ||
@@ -354,7 +598,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     c23 = h->h_ctr[0];
     n3 = h->h_ctr[1];
     int mg = o.min_grains;
-    int full = h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0) || c23 > 0 ||
+    int full = batch || h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0) || c23 > 0 ||
                (mg > 0 && h->curr_n_grains + 1 - n3 <= mg);
     loc.outputs_complete = full;
     if (!full) { Prof pr(h, "text_label"); launch_mark_force(m, x, n3, s); }
@@ -362,17 +606,19 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     { Prof pr(h, "text_label"); launch_text_label(m, o.dt, full, s); }                            /* :212-216 */
     { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
 
-    int conv = 0, it = 0;                                                                          /* :219 */
-    while (!conv) {
+    cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
+    cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);
+    int running = 1, it = 0;
+    while (running) {
         if (it >= h->polling_cap) { sevc_set_error("polling did not converge"); return SEVC_ERR_NONCONVERGED; }
         it++;
         { Prof pr(h, "polling"); launch_poll_iteration(m, x, x.list_a, x.n_a, h->p, s); }
-        if (read_ints(h, x.counters + CTR_CONVERGED, 1, &conv)) return SEVC_ERR_CUDA;
+        if (read_ints(h, x.nrun, 1, &running)) return SEVC_ERR_CUDA;
     }
     loc.polling_iters = it;
     { Prof pr(h, "conflicts"); launch_conflicts(m, x.list_a, x.n_a, s); }                         /* :222-225 */
 
-    for (int k = 0; k < 20; k++) {                                                                 /* :227-250 */
+    for (int k = 0; k < TWO_THREE_PASSES; k++) {                                                   /* :227-250 */
         int c = c23;
         if (k > 0) {
             { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
@@ -381,7 +627,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         loc.two_three_counts[k] = c;
         loc.n_two_three_iters = k + 1;
         if (c == 0) break;
-        { Prof pr(h, "two_three_remove"); launch_remove_two_three(m, x, x.list_b, x.n_b, s); }
+        { Prof pr(h, "two_three_remove"); launch_remove_two_three(m, x, x.list_b, x.n_b, k, s); }
         { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }
     }
     { Prof pr(h, "label_3sided"); launch_label_3sided(m, o.dt, s); }                              /* :252-255 */
@@ -396,32 +642,83 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }                                       /* :317-325 */
     cudaEventRecord(h->ev1, s);
 
-    int ctr[CTR_COUNT];
-    if (read_ints(h, x.counters, CTR_COUNT, ctr)) return SEVC_ERR_CUDA;
-    int ev[8];
-    if (read_ints(h, m.err, 4, ev) || read_ints(h, m.evt, 4, ev + 4)) return SEVC_ERR_CUDA;
+    /* one readback: counters, events, error bits, polling iterations and
+     * 2x3 counts of every instance */
+    int *hb = h->h_big;
+    const size_t o_evt = (size_t)I * CTR_COUNT, o_err = o_evt + (size_t)I * EVT_COUNT, o_pit = o_err + 4,
+                 o_seg = o_pit + I;
+    auto get = [&](int *dst, const int *src, size_t n) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, n * sizeof(int), cudaMemcpyDeviceToHost, s), "readback");
+    };
+    if (!get(hb, x.counters, (size_t)I * CTR_COUNT) || !get(hb + o_evt, m.evt, (size_t)I * EVT_COUNT) ||
+        !get(hb + o_err, m.err, 4) || !get(hb + o_pit, x.piters, I) ||
+        !get(hb + o_seg, x.segcnt, (size_t)I * TWO_THREE_PASSES) || !cuda_ok(cudaStreamSynchronize(s), "readback sync"))
+        return SEVC_ERR_CUDA;
     float ms = 0;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     if (h->profiling) prof_collect(h);
-    h->curr_n_grains = ctr[CTR_NGRAINS];
-    double na;
-    memcpy(&na, ctr + CTR_NUCL_AREA_SLOT, sizeof(double));
-    h->nucleated_area = na;
-    loc.curr_n_grains = h->curr_n_grains;
-    loc.nucleated_area = na;
-    loc.n_two_three = ev[4 + EVT_TWO_THREE];
-    loc.n_removals = ev[4 + EVT_REMOVALS];
-    loc.n_flips = ev[4 + EVT_FLIPS];
-    loc.n_nucleations = ev[4 + EVT_NUCLEATIONS];
-    loc.nucleation_candidate = loc.nucleation_attempted ? ctr[CTR_CANDIDATE] : -1;
+    int launches = (int)(sevc_kernel_launches - launches0);
+    int total = 0;
+    double area_sum = 0;
+    for (int i = 0; i < I; i++) {
+        const int *ctr = hb + (size_t)i * CTR_COUNT, *ev = hb + o_evt + (size_t)i * EVT_COUNT;
+        double na;
+        memcpy(&na, ctr + CTR_NUCL_AREA_SLOT, sizeof(double));
+        h->icurr[i] = ctr[CTR_NGRAINS];
+        h->iarea[i] = na;
+        total += h->icurr[i];
+        area_sum += na;
+        sevc_step_info &ii = h->iinfo[i];
+        memset(&ii, 0, sizeof ii);
+        ii.n = loc.n;
+        ii.t = loc.t;
+        ii.curr_n_grains = h->icurr[i];
+        ii.nucleated_area = na;
+        ii.polling_iters = hb[o_pit + i];
+        for (int k = 0; k < TWO_THREE_PASSES; k++) {
+            int c = hb[o_seg + (size_t)k * I + i];
+            ii.two_three_counts[k] = c;
+            ii.n_two_three_iters = k + 1;
+            if (c == 0) break;
+        }
+        ii.n_two_three = ev[EVT_TWO_THREE];
+        ii.n_removals = ev[EVT_REMOVALS];
+        ii.n_flips = ev[EVT_FLIPS];
+        ii.n_nucleations = ev[EVT_NUCLEATIONS];
+        ii.nucleation_attempted = h->h_on[i];
+        /* reported in the instance's own vertex indices */
+        ii.nucleation_candidate = (h->h_on[i] && ctr[CTR_CANDIDATE] >= 0) ? ctr[CTR_CANDIDATE] - h->voff[i] : -1;
+        ii.gpu_ms = ms;
+        ii.outputs_complete = full;
+        ii.kernel_launches = launches;
+        ii.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (h->icurr[i] <= mg && mg > 0); /* :328 */
+        loc.n_two_three += ii.n_two_three;
+        loc.n_removals += ii.n_removals;
+        loc.n_flips += ii.n_flips;
+        loc.n_nucleations += ii.n_nucleations;
+    }
+    h->curr_n_grains = total;
+    h->nucleated_area = batch ? area_sum / I : area_sum;
+    loc.curr_n_grains = total;
+    loc.nucleated_area = h->nucleated_area;
+    loc.nucleation_candidate = (!batch && loc.nucleation_attempted) ? h->iinfo[0].nucleation_candidate : -1;
     loc.gpu_ms = ms;
-    loc.kernel_launches = (int)(sevc_kernel_launches - launches0);
-    loc.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (h->curr_n_grains <= mg && mg > 0); /* :328 */
+    loc.kernel_launches = launches;
+    loc.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (!batch && h->curr_n_grains <= mg && mg > 0);
     h->n++;                                                                                         /* :388-389 */
     h->t = h->n * o.dt;
-    loc.keep_going = (h->curr_n_grains <= mg && mg > 0) ? 0 : sevc_should_continue(h);             /* :391 */
+    for (int i = 0; i < I; i++) {
+        int cont = ((h->t <= o.tmax && o.tmax > 0) || (h->n <= o.nmax && o.nmax > 0)) && (h->icurr[i] >= mg && mg > 0);
+        h->iinfo[i].keep_going = (h->icurr[i] <= mg && mg > 0) ? 0 : cont;                          /* :391 */
+    }
+    loc.keep_going = batch ? sevc_should_continue(h) : h->iinfo[0].keep_going;
     if (info) *info = loc;
-    return err_bits_to_status(ev[0]);
+    sevc_status st = err_bits_to_status(hb[o_err]);
+    if (!st && h->tape.every > 0 && !h->tape.replaying) {
+        h->tape.nsteps++;
+        if (h->tape.nsteps % h->tape.every == 0 && !tape_checkpoint(h)) return SEVC_ERR_CUDA;
+    }
+    return st;
 }
 
 sevc_status sevc_run_steps(sevc_handle *h, int nsteps, int *done, sevc_step_info *last)
@@ -499,6 +796,50 @@ sevc_status sevc_export_text(sevc_handle *h, const char *path, double time)
     return st;
 }
 
+sevc_status sevc_export_instance_text(sevc_handle *h, int inst, const char *path, double time)
+{
+    if (!h || !path || inst < 0 || inst >= h->ninst) return SEVC_ERR_ARG;
+    sevc_hmesh all, one;
+    if (sevc_hmesh_alloc(&all, h->nv, h->nb, h->ng)) return SEVC_ERR_CAPACITY;
+    sevc_status st = sevc_get_state(h, &all.m);
+    int vo = h->voff[inst], bo = h->boff[inst], go = h->goff[inst];
+    size_t V = h->voff[inst + 1] - vo, B = h->boff[inst + 1] - bo, G = h->goff[inst + 1] - go;
+    if (!st && sevc_hmesh_alloc(&one, (int)V, (int)B, (int)G)) st = SEVC_ERR_CAPACITY;
+    if (!st) {
+        const sevc_mesh_host &a = all.m;
+        sevc_mesh_host &p = one.m;
+        auto unshift = [](int32_t *dst, const int32_t *src, size_t n, int off) {
+            for (size_t k = 0; k < n; k++) dst[k] = src[k] >= 0 ? src[k] - off : src[k];
+        };
+        double *vd[] = { p.px, p.py, p.vx, p.vy, p.venergy, p.vel_bnd_x, p.vel_grn_x, p.vel_bnd_y, p.vel_grn_y };
+        const double *vs[] = { a.px, a.py, a.vx, a.vy, a.venergy, a.vel_bnd_x, a.vel_grn_x, a.vel_bnd_y, a.vel_grn_y };
+        for (int f = 0; f < 9; f++) memcpy(vd[f], vs[f] + vo, V * 8);
+        memcpy(p.ven, a.ven + vo, V);
+        unshift(p.vb, a.vb + 3 * (size_t)vo, 3 * V, bo);
+        unshift(p.vg, a.vg + 3 * (size_t)vo, 3 * V, go);
+        unshift(p.bini, a.bini + bo, B, vo);
+        unshift(p.bend, a.bend + bo, B, vo);
+        double *bd[] = { p.benergy, p.blen, p.btext };
+        const double *bs[] = { a.benergy, a.blen, a.btext };
+        for (int f = 0; f < 3; f++) memcpy(bd[f], bs[f] + bo, B * 8);
+        memcpy(p.ben, a.ben + bo, B);
+        memcpy(p.bcand, a.bcand + bo, B);
+        unshift(p.glist, a.glist + (size_t)SEVC_MAXV * go, SEVC_MAXV * G, vo);
+        memcpy(p.gvlen, a.gvlen + go, G * 4);
+        double *gd[] = { p.garea, p.gdadt, p.gori, p.gse };
+        const double *gs[] = { a.garea, a.gdadt, a.gori, a.gse };
+        for (int f = 0; f < 4; f++) memcpy(gd[f], gs[f] + go, G * 8);
+        memcpy(p.gen, a.gen + go, G);
+        memcpy(p.gtype, a.gtype + go, G);
+        sevc_options oi = h->opt;
+        oi.n_grains = h->ng0[inst];
+        st = (sevc_status)sevc_host_export(&p, &oi, path, time);
+        sevc_hmesh_free(&one);
+    }
+    sevc_hmesh_free(&all);
+    return st;
+}
+
 sevc_status sevc_check_data(sevc_handle *h, int *n_bad)
 {
     if (!h || !n_bad) return SEVC_ERR_ARG;
@@ -516,6 +857,269 @@ sevc_status sevc_rng_record(int nstreams, int ndraws, double *out)
     int dev = 0;
     if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) { sevc_set_error("no CUDA device"); return SEVC_ERR_CUDA; }
     return rng_record(nstreams, ndraws, out) ? SEVC_ERR_CUDA : SEVC_OK;
+}
+
+/* ---------------- parameters and the adjoint ---------------- */
+sevc_status sevc_set_mobility(sevc_handle *h, double mu)
+{
+    if (!h || !(mu > 0) || h->tape.every > 0) return SEVC_ERR_ARG;
+    h->p.mu = mu;
+    return SEVC_OK;
+}
+
+sevc_status sevc_set_gb_scaling(sevc_handle *h, double s)
+{
+    if (!h || h->tape.every > 0) return SEVC_ERR_ARG;
+    h->opt.GB_scaling = s;
+    h->p.scaling = s;
+    return SEVC_OK;
+}
+
+sevc_status sevc_set_stored_energy(sevc_handle *h, const double *se)
+{
+    if (!h || !se || h->tape.every > 0) return SEVC_ERR_ARG;
+    if (!cuda_ok(cudaMemcpyAsync(h->m.gse, se, (size_t)h->ng * 8, cudaMemcpyHostToDevice, h->stream), "upload") ||
+        !cuda_ok(cudaStreamSynchronize(h->stream), "sync"))
+        return SEVC_ERR_CUDA;
+    return SEVC_OK;
+}
+
+sevc_status sevc_tape_start(sevc_handle *h, int checkpoint_every)
+{
+    if (!h || checkpoint_every < 1) return SEVC_ERR_ARG;
+    if (h->opt.do_nucleation) {
+        sevc_set_error("the adjoint covers runs without nucleation (do_nucleation = 0)");
+        return SEVC_ERR_ARG;
+    }
+    tape_free(h);
+    h->tape.every = checkpoint_every;
+    return tape_checkpoint(h) ? SEVC_OK : SEVC_ERR_CUDA;
+}
+
+sevc_status sevc_tape_stop(sevc_handle *h)
+{
+    if (!h) return SEVC_ERR_ARG;
+    tape_free(h);
+    return SEVC_OK;
+}
+
+sevc_status sevc_area_histogram(sevc_handle *h, int nbins, double amax, double *hist)
+{
+    if (!h || nbins < 1 || nbins > 1024 || !(amax > 0) || !hist) return SEVC_ERR_ARG;
+    int nb = histogram_blocks(h->m);
+    double *d = nullptr;
+    if (!cuda_ok(cudaMalloc(&d, ((size_t)nb + 1) * nbins * 8), "cudaMalloc")) return SEVC_ERR_CUDA;
+    double nnorm = h->curr_n_grains, sc = nnorm / (h->ninst * h->opt.domain_bound * h->opt.domain_bound);
+    launch_histogram(h->m, nbins, amax, sc, nnorm, d + nbins, d, h->stream);
+    bool ok = cuda_ok(cudaMemcpyAsync(hist, d, nbins * 8, cudaMemcpyDeviceToHost, h->stream), "readback") &&
+              cuda_ok(cudaStreamSynchronize(h->stream), "sync");
+    cudaFree(d);
+    return ok ? SEVC_OK : SEVC_ERR_CUDA;
+}
+
+sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const double *dloss_dhist,
+                                   double *grad_se, double *grad_gb_scaling, double *grad_mu)
+{
+    if (!h || nbins < 1 || nbins > 1024 || !(amax > 0) || !dloss_dhist) return SEVC_ERR_ARG;
+    Tape &tp = h->tape;
+    if (tp.every <= 0) { sevc_set_error("no tape: call sevc_tape_start before the steps"); return SEVC_ERR_ARG; }
+    cudaStream_t s = h->stream;
+    size_t V = h->nv, B = h->nb, G = h->ng;
+    /* adjoint buffers */
+    AdjointBuffers a{};
+    double *d_dldh = nullptr;
+    {
+        struct Req { void **p; size_t bytes; };
+        std::vector<Req> r = { { (void **)&a.lam, V * 16 }, { (void **)&a.lx, V * 16 }, { (void **)&a.lv, V * 16 },
+                               { (void **)&a.mark, V }, { (void **)&a.sgn, G * 8 }, { (void **)&a.gse, G * 8 },
+                               { (void **)&a.gmu, V * 8 }, { (void **)&a.ggam, V * 8 }, { (void **)&a.dlda, G * 8 },
+                               { (void **)&a.scalars, 16 }, { (void **)&d_dldh, 1024 * 8 } };
+        size_t total = 0;
+        for (auto &q : r) total += align256(q.bytes);
+        if (!tp.adj) {
+            if (!cuda_ok(cudaMalloc(&tp.adj, total), "cudaMalloc adjoint")) return SEVC_ERR_CUDA;
+            tp.adj_bytes = total;
+        }
+        char *base = (char *)tp.adj;
+        for (auto &q : r) { *q.p = base; base += align256(q.bytes); }
+    }
+    /* per-step records of one segment */
+    tp.log_cap = 4096 + (int)(V / 16);
+    size_t off_pos = 0, off_vb = off_pos + align256(V * 16), off_vg = off_vb + align256(V * 16),
+           off_vel1 = off_vg + align256(V * 16), off_ven = off_vel1 + align256(V * 16), off_ven1 = off_ven + align256(V),
+           off_bv = off_ven1 + align256(V), off_ben = off_bv + align256(B * 8), off_gl = off_ben + align256(B),
+           off_gvl = off_gl + align256(G * SEVC_MAXV * 4), off_gen = off_gvl + align256(G * 4),
+           off_log = off_gen + align256(G), off_nlog = off_log + align256((size_t)tp.log_cap * sizeof(EventRec)),
+           step_bytes = off_nlog + 256;
+    if (!tp.rec || tp.rec_step_bytes != step_bytes || tp.rec_steps < tp.every) {
+        if (tp.rec) cudaFree(tp.rec);
+        tp.rec = nullptr;
+        if (!cuda_ok(cudaMalloc(&tp.rec, step_bytes * tp.every), "cudaMalloc tape records")) return SEVC_ERR_CUDA;
+        tp.rec_step_bytes = step_bytes;
+        tp.rec_steps = tp.every;
+    }
+    auto rec = [&](int k, size_t off) { return (char *)tp.rec + (size_t)k * step_bytes + off; };
+    auto d2d = [&](void *dst, const void *src, size_t n) {
+        return cuda_ok(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, s), "tape copy");
+    };
+
+    /* seed: dL/dx of the statistic at the final state */
+    if (!cuda_ok(cudaMemcpyAsync(d_dldh, dloss_dhist, nbins * 8, cudaMemcpyHostToDevice, s), "upload")) return SEVC_ERR_CUDA;
+    cudaMemsetAsync(a.gse, 0, G * 8, s);
+    cudaMemsetAsync(a.gmu, 0, V * 8, s);
+    cudaMemsetAsync(a.ggam, 0, V * 8, s);
+    double nnorm = h->curr_n_grains, sc = nnorm / (h->ninst * h->opt.domain_bound * h->opt.domain_bound);
+    launch_hist_seed(h->m, nbins, amax, sc, nnorm, d_dldh, a.dlda, a.lam, s);
+
+    void *fin = nullptr;
+    if (!cuda_ok(cudaMalloc(&fin, h->dbytes), "cudaMalloc") || !d2d(fin, h->dblock, h->dbytes)) return SEVC_ERR_CUDA;
+    RunState rfin = save_run(h);
+    sevc_status st = SEVC_OK;
+    tp.replaying = true;
+    long long nseg = (tp.nsteps + tp.every - 1) / tp.every;
+    for (long long seg = nseg - 1; seg >= 0 && !st; seg--) {
+        if (!d2d(h->dblock, tp.ckpt[seg], h->dbytes)) { st = SEVC_ERR_CUDA; break; }
+        load_run(h, tp.runs[seg]);
+        int K = (int)std::min<long long>(tp.every, tp.nsteps - seg * tp.every);
+        for (int k = 0; k < K && !st; k++) {
+            DevMesh &m = h->m;
+            bool ok = d2d(rec(k, off_pos), m.pos, V * 16) && d2d(rec(k, off_vb), m.vb, V * 16) &&
+                      d2d(rec(k, off_vg), m.vg, V * 16) && d2d(rec(k, off_ven), m.ven, V) &&
+                      d2d(rec(k, off_bv), m.bv, B * 8) && d2d(rec(k, off_ben), m.ben, B) &&
+                      d2d(rec(k, off_gl), m.glist, G * SEVC_MAXV * 4) && d2d(rec(k, off_gvl), m.gvlen, G * 4) &&
+                      d2d(rec(k, off_gen), m.gen, G) &&
+                      cuda_ok(cudaMemsetAsync(rec(k, off_nlog), 0, 4, s), "memset");
+            if (!ok) { st = SEVC_ERR_CUDA; break; }
+            m.elog = (EventRec *)rec(k, off_log);
+            m.nelog = (int *)rec(k, off_nlog);
+            m.elog_cap = tp.log_cap;
+            st = sevc_step(h, nullptr);
+            m.elog = nullptr;
+            m.nelog = nullptr;
+            m.elog_cap = 0;
+            if (!st && !(d2d(rec(k, off_vel1), m.vel, V * 16) && d2d(rec(k, off_ven1), m.ven, V))) st = SEVC_ERR_CUDA;
+        }
+        for (int k = K - 1; k >= 0 && !st; k--) {
+            DevMesh view = h->m;
+            view.pos = (double2 *)rec(k, off_pos);
+            view.vb = (int4 *)rec(k, off_vb);
+            view.vg = (int4 *)rec(k, off_vg);
+            view.ven = (uint8_t *)rec(k, off_ven);
+            view.bv = (int2 *)rec(k, off_bv);
+            view.ben = (uint8_t *)rec(k, off_ben);
+            view.glist = (int *)rec(k, off_gl);
+            view.gvlen = (int *)rec(k, off_gvl);
+            view.gen = (uint8_t *)rec(k, off_gen);
+            launch_adjoint_step(view, a, h->opt.dt, h->p.mu, h->opt.GB_eps, h->opt.GB_scaling,
+                                (const EventRec *)rec(k, off_log), (const int *)rec(k, off_nlog),
+                                (const uint8_t *)rec(k, off_ven1), (const double2 *)rec(k, off_vel1), s);
+        }
+    }
+    tp.replaying = false;
+    if (!d2d(h->dblock, fin, h->dbytes)) st = SEVC_ERR_CUDA;
+    load_run(h, rfin);
+    launch_sum_ordered(a.gmu, (int)V, a.scalars, s);
+    launch_sum_ordered(a.ggam, (int)V, a.scalars + 1, s);
+    double sc2[2] = { 0, 0 };
+    if (!st && grad_se && !cuda_ok(cudaMemcpyAsync(grad_se, a.gse, G * 8, cudaMemcpyDeviceToHost, s), "readback"))
+        st = SEVC_ERR_CUDA;
+    if (!st && !cuda_ok(cudaMemcpyAsync(sc2, a.scalars, 16, cudaMemcpyDeviceToHost, s), "readback")) st = SEVC_ERR_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), "sync") && !st) st = SEVC_ERR_CUDA;
+    cudaFree(fin);
+    if (st) return st;
+    if (grad_mu) *grad_mu = sc2[0];
+    if (grad_gb_scaling) *grad_gb_scaling = sc2[1];
+    return SEVC_OK;
+}
+
+/* ---------------- checkpoint files ---------------- */
+namespace {
+const char CKPT_MAGIC[8] = { 'S', 'E', 'V', 'C', 'C', 'K', 'P', '1' };
+struct CkptHeader {
+    char magic[8];
+    int32_t nv, nb, ng, ninst;
+    uint64_t dbytes;
+    int32_t n, curr_n_grains;
+    double t, nucleated_area, mu, gb_scaling;
+};
+} // namespace
+
+sevc_status sevc_checkpoint_save(sevc_handle *h, const char *path)
+{
+    if (!h || !path) return SEVC_ERR_ARG;
+    std::vector<char> blk(h->dbytes);
+    if (!cuda_ok(cudaMemcpyAsync(blk.data(), h->dblock, h->dbytes, cudaMemcpyDeviceToHost, h->stream), "download") ||
+        !cuda_ok(cudaStreamSynchronize(h->stream), "sync"))
+        return SEVC_ERR_CUDA;
+    CkptHeader hd{};
+    memcpy(hd.magic, CKPT_MAGIC, 8);
+    hd.nv = h->nv; hd.nb = h->nb; hd.ng = h->ng; hd.ninst = h->ninst;
+    hd.dbytes = h->dbytes;
+    hd.n = h->n; hd.curr_n_grains = h->curr_n_grains;
+    hd.t = h->t; hd.nucleated_area = h->nucleated_area; hd.mu = h->p.mu; hd.gb_scaling = h->opt.GB_scaling;
+    FILE *f = fopen(path, "wb");
+    if (!f) { sevc_set_error("cannot write %s", path); return SEVC_ERR_IO; }
+    size_t I = h->ninst;
+    bool ok = fwrite(&hd, sizeof hd, 1, f) == 1 && fwrite(h->icurr.data(), 4, I, f) == I &&
+              fwrite(h->iallow.data(), 4, I, f) == I && fwrite(h->iarea.data(), 8, I, f) == I &&
+              fwrite(blk.data(), 1, blk.size(), f) == blk.size();
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) { sevc_set_error("short write to %s", path); return SEVC_ERR_IO; }
+    return SEVC_OK;
+}
+
+sevc_status sevc_checkpoint_load(sevc_handle *h, const char *path)
+{
+    if (!h || !path) return SEVC_ERR_ARG;
+    if (h->tape.every > 0) { sevc_set_error("stop the adjoint tape before loading a checkpoint"); return SEVC_ERR_ARG; }
+    FILE *f = fopen(path, "rb");
+    if (!f) { sevc_set_error("cannot read %s", path); return SEVC_ERR_IO; }
+    CkptHeader hd{};
+    size_t I = h->ninst;
+    std::vector<int> icurr(I), iallow(I);
+    std::vector<double> iarea(I);
+    std::vector<char> blk(h->dbytes);
+    bool ok = fread(&hd, sizeof hd, 1, f) == 1;
+    if (ok && (memcmp(hd.magic, CKPT_MAGIC, 8) || hd.nv != h->nv || hd.nb != h->nb || hd.ng != h->ng ||
+               hd.ninst != h->ninst || hd.dbytes != h->dbytes)) {
+        fclose(f);
+        sevc_set_error("%s is not a checkpoint of a handle of this shape", path);
+        return SEVC_ERR_PARSE;
+    }
+    ok = ok && fread(icurr.data(), 4, I, f) == I && fread(iallow.data(), 4, I, f) == I &&
+         fread(iarea.data(), 8, I, f) == I && fread(blk.data(), 1, blk.size(), f) == blk.size();
+    fclose(f);
+    if (!ok) { sevc_set_error("truncated checkpoint %s", path); return SEVC_ERR_PARSE; }
+    if (!cuda_ok(cudaMemcpyAsync(h->dblock, blk.data(), h->dbytes, cudaMemcpyHostToDevice, h->stream), "upload") ||
+        !cuda_ok(cudaStreamSynchronize(h->stream), "sync"))
+        return SEVC_ERR_CUDA;
+    h->n = hd.n; h->curr_n_grains = hd.curr_n_grains; h->t = hd.t; h->nucleated_area = hd.nucleated_area;
+    h->p.mu = hd.mu; h->opt.GB_scaling = hd.gb_scaling; h->p.scaling = hd.gb_scaling;
+    h->icurr = icurr; h->iallow = iallow; h->iarea = iarea;
+    return SEVC_OK;
+}
+
+sevc_status sevc_grain_stats(sevc_handle *h, int inst, sevc_grain_stats_t *out)
+{
+    if (!h || !out || inst < -1 || inst >= h->ninst) return SEVC_ERR_ARG;
+    int lo = inst < 0 ? 0 : h->goff[inst], hi = inst < 0 ? h->ng : h->goff[inst + 1];
+    double *d = nullptr;
+    if (!cuda_ok(cudaMalloc(&d, 8 * 8), "cudaMalloc")) return SEVC_ERR_CUDA;
+    launch_grain_stats(h->m, lo, hi, d, h->stream);
+    double r[8];
+    bool ok = cuda_ok(cudaMemcpyAsync(r, d, sizeof r, cudaMemcpyDeviceToHost, h->stream), "readback") &&
+              cuda_ok(cudaStreamSynchronize(h->stream), "sync");
+    cudaFree(d);
+    if (!ok) return SEVC_ERR_CUDA;
+    double n = r[0];
+    out->n_grains = (int)n;
+    out->mean_area = n > 0 ? r[1] / n : 0;
+    out->std_area = n > 1 ? sqrt(std::max(0.0, r[2] / n - out->mean_area * out->mean_area)) : 0;
+    out->mean_sides = n > 0 ? r[3] / n : 0;
+    out->n_three_sided = (int)r[4];
+    out->min_area = r[5];
+    out->max_area = r[6];
+    return SEVC_OK;
 }
 
 sevc_status sevc_set_exact_all(sevc_handle *h, int on)

@@ -349,7 +349,7 @@ __global__ void k_grain_fd(DevMesh m)
 
 /* vertex pass: src/calculus.h:19-73 (boundary part) and :143-154;
  * vertex_compute_energy src/geometry.h:472-479 */
-__global__ void k_vertex_fd(DevMesh m)
+__global__ void k_vertex_fd(DevMesh m, double mu)
 {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= m.nv || !m.ven[v]) return;
@@ -379,7 +379,7 @@ __global__ void k_vertex_fd(DevMesh m)
             gt += (c == 0 ? cg[j].x : cg[j].y);
         }
         if (c == 0) { t.bx = bt; t.gx = gt; } else { t.by = bt; t.gy = gt; }
-        vel[c] = -(bt + gt) / SEVC_GRAD_EPS_D;
+        vel[c] = mu * (-(bt + gt) / SEVC_GRAD_EPS_D);   /* mobility; mu = 1 multiplies exactly */
     }
     m.terms[v] = t;
     m.vel[v] = make_double2(vel[0], vel[1]);
@@ -519,6 +519,11 @@ __global__ void k_area_dirty(DevMesh m, int compute)
     }
 }
 __global__ void k_reset_count(int *c) { *c = 0; }
+__global__ void k_reset_ngrains(int *counters, int ninst)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ninst) counters[(size_t)i * CTR_COUNT + CTR_NGRAINS] = 0;
+}
 
 /* update_vertices_positions, src/calculus.h:391-404 */
 __global__ void k_update(DevMesh m, double dt)
@@ -533,30 +538,44 @@ __global__ void k_update(DevMesh m, double dt)
     m.pos[v] = p;
 }
 
-/* current_n_grains (src/calculus.h:264-313): an integer count */
-__global__ void k_count_grains(DevMesh m, int *out)
+/* current_n_grains (src/calculus.h:264-313): an integer count per
+ * instance (blockIdx.y), added into counters[inst * CTR_COUNT + CTR_NGRAINS] */
+__global__ void k_count_grains(DevMesh m, int *counters)
 {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    int c = (g < m.ng && m.gen[g]) ? 1 : 0;
-    c = __syncthreads_count(c);
-    if (threadIdx.x == 0 && c) atomicAdd(out, c);
+    int inst = blockIdx.y;
+    int lo = m.goff[inst], hi = m.goff[inst + 1];
+    int c = 0;
+    for (int g = lo + blockIdx.x * blockDim.x + threadIdx.x; g < hi; g += gridDim.x * blockDim.x) c += m.gen[g] ? 1 : 0;
+    __shared__ int part[32];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+        if (t) atomicAdd(counters + (size_t)inst * CTR_COUNT + CTR_NGRAINS, t);
+    }
 }
 
 /* nucl_area_per_block (src/calculus.h:322-348): launched on the
- * reference's grid so that the floating-point sum order is the same:
- * per-thread strided partial sums, then the shared-memory tree. */
+ * reference's grid (blockIdx.y = instance) so that the floating-point sum
+ * order is the same: per-thread strided partial sums over the instance's
+ * grain indices, then the shared-memory tree. */
 __global__ void k_nucl_area_blocks(DevMesh m, double *block_out)
 {
     __shared__ double t[256];
+    int inst = blockIdx.y;
+    int go = m.goff[inst];
     int tid = blockIdx.x * blockDim.x + threadIdx.x;
     int stride = gridDim.x * blockDim.x;
     double a = 0.0;
     /* the thread's stride set in ascending order, restricted to the slots
-     * that can be NUCLEATED (m.nlist is ascending) */
-    int nn = *m.nnlist;
+     * that can be NUCLEATED (the instance's nlist part is ascending) */
+    int nn = m.nnlist[inst];
+    const int *nl = m.nlist + go;
     for (int i = 0; i < nn; i++) {
-        int g = m.nlist[i];
-        if (g % stride == tid && m.gen[g] && m.gtype[g] == GT_NUCLEATED) a += m.garea[g];
+        int g = nl[i];
+        if ((g - go) % stride == tid && m.gen[g] && m.gtype[g] == GT_NUCLEATED) a += m.garea[g];
     }
     t[threadIdx.x] = a;
     __syncthreads();
@@ -564,15 +583,18 @@ __global__ void k_nucl_area_blocks(DevMesh m, double *block_out)
         if ((int)threadIdx.x < i) t[threadIdx.x] += t[threadIdx.x + i];
         __syncthreads();
     }
-    if (threadIdx.x == 0) block_out[blockIdx.x] = t[0];
+    if (threadIdx.x == 0) block_out[(size_t)inst * gridDim.x + blockIdx.x] = t[0];
 }
 
-/* host loop of nucleated_fraction_area, src/calculus.h:373-377 */
-__global__ void k_nucl_area_final(const double *block_out, int nblocks, double D, double *out)
+/* host loop of nucleated_fraction_area, src/calculus.h:373-377, one
+ * thread per instance */
+__global__ void k_nucl_area_final(const double *block_out, int nblocks, int ninst, double D, int *counters)
 {
+    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= ninst) return;
     double s = 0.0;
-    for (int i = 0; i < nblocks; i++) s += block_out[i];
-    *out = 100 * s / (D * D);
+    for (int i = 0; i < nblocks; i++) s += block_out[(size_t)inst * nblocks + i];
+    *reinterpret_cast<double *>(counters + (size_t)inst * CTR_COUNT + CTR_NUCL_AREA_SLOT) = 100 * s / (D * D);
 }
 
 } // namespace
@@ -592,7 +614,10 @@ void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 
 /* the unsorted per-grain pass, kept for A/B timing */
 void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_vertex_fd(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m); }
+void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m, mu);
+}
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, int full, int n3, cudaStream_t s)
 {
     if (full) COUNT_LAUNCHES(1), k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m);
@@ -616,9 +641,12 @@ void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { COUN
 
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
 {
-    cudaMemsetAsync(x.counters + CTR_NGRAINS, 0, sizeof(int), s);
-    COUNT_LAUNCHES(1), k_count_grains<<<nblk(m.ng), TPB, 0, s>>>(m, x.counters + CTR_NGRAINS);
-    COUNT_LAUNCHES(1), k_nucl_area_blocks<<<p.n_blocks, p.n_threads, 0, s>>>(m, x.block_area);
-    COUNT_LAUNCHES(1), k_nucl_area_final<<<1, 1, 0, s>>>(x.block_area, p.n_blocks, m.D,
-                                      reinterpret_cast<double *>(x.counters + CTR_NUCL_AREA_SLOT));
+    COUNT_LAUNCHES(1), k_reset_ngrains<<<(p.ninst + 127) / 128, 128, 0, s>>>(x.counters, p.ninst);
+    int gx = nblk(p.max_inst_ng);
+    if (gx > 4096) gx = 4096;
+    if (gx < 1) gx = 1;
+    COUNT_LAUNCHES(1), k_count_grains<<<dim3(gx, p.ninst), TPB, 0, s>>>(m, x.counters);
+    COUNT_LAUNCHES(1), k_nucl_area_blocks<<<dim3(p.n_blocks, p.ninst), p.n_threads, 0, s>>>(m, x.block_area);
+    COUNT_LAUNCHES(1), k_nucl_area_final<<<(p.ninst + 127) / 128, 128, 0, s>>>(x.block_area, p.n_blocks, p.ninst, m.D,
+                                                                              x.counters);
 }

@@ -10,19 +10,29 @@
 #include <curand_kernel.h>
 
 /* scratch shared by launches of one handle */
+/* Scratch shared by launches of one handle.  Arrays marked "per instance"
+ * hold one block for each instance of a batched handle. */
 struct DevScratch {
     int *list_a, *list_b, *list_c;   /* ordered index lists (capacity max(nb, ng)) */
     int *n_a, *n_b, *n_c;            /* their lengths */
     int *blockcnt;                   /* per-tile counts for ordered compaction */
-    int *extra;                      /* dynamic insertions of the 2x3 pass */
-    int *threadfail;                 /* polling predicate: one flag per grid thread */
-    double *block_area;              /* nucleated-area partial per block */
-    int *counters;                   /* small device counters, see CTR_* */
-    curandState *rng, *rng_saved;    /* 8192 cuRAND states + pre-attempt copy */
-    int *nucl_buf;                   /* 64 ints: per-block pick and alive count */
-    int *vbucket;                    /* 32 ints: side-count histogram + cursors */
+    int *extra;                      /* dynamic insertions of the 2x3 pass, EXTRA_CAP per instance */
+    int *threadfail;                 /* polling predicate: one flag per grid thread, per instance */
+    int *pblock;                     /* polling predicate: one result per grid block, per instance */
+    int *piters;                     /* polling iterations this step, per instance */
+    int *nrun;                       /* instances whose polling has not converged */
+    int *segcnt;                     /* 2x3 count of each pass (20), per instance */
+    double *block_area;              /* nucleated-area partial per block, per instance */
+    int *counters;                   /* CTR_COUNT device counters per instance, see CTR_* */
+    curandState *rng, *rng_saved;    /* 8192 cuRAND states + pre-attempt copy, per instance */
+    int *nucl_buf;                   /* 64 ints per instance: per-block pick and alive count */
+    int *nucl_on;                    /* per instance: attempt a nucleation this step */
+    int *vbucket;                    /* 64 ints: side-count histogram + cursors */
     int *perm, *n_perm;              /* enabled grains ordered by side count */
 };
+constexpr int EXTRA_CAP = 1024;
+constexpr int TWO_THREE_PASSES = 20;  /* src/main.cu:227 */
+constexpr int RNG_GRID = 8192;        /* the reference's 32 x 256 nucleation grid */
 
 enum {
     CTR_NGRAINS = 0,     /* current_n_grains */
@@ -40,12 +50,15 @@ enum {
 struct StepParams {
     double dt, eps, scaling, MC_k;
     int n_blocks, n_threads; /* reference launch grid, drives observable partitions */
+    int ninst;               /* instances in the handle */
+    int max_inst_ng;         /* grains of the largest instance */
+    double mu;               /* mobility (velocity factor); 1 in the reference */
 };
 
 /* geometry (sevc_geometry.cu) */
 void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s);
 void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s);
-void launch_vertex_fd(const DevMesh &m, cudaStream_t s);
+void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s);
 /* side-count histogram layout in DevScratch::vbucket */
 #define VB_START(b) (32 + (b))
 #define VB_COUNT(b) (48 + (b))
@@ -60,21 +73,54 @@ void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, c
 /* topology (sevc_topology.cu) */
 enum CompactKind { CK_CAND = 0, CK_TWO_THREE = 1, CK_GRAIN_CAND = 2, CK_GVLEN3 = 3 };
 void launch_compact(const DevMesh &m, const DevScratch &x, CompactKind kind, int *out, int *n_out, cudaStream_t s);
+/* one polling iteration for every instance not yet converged; leaves the
+ * number still running in x.nrun */
 void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *cand, const int *ncand,
                            const StepParams &p, cudaStream_t s);
 void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s);
-void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s);
+/* pass `pass` of the 2x3 loop (per-instance counts go to x.segcnt) */
+void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, int pass,
+                             cudaStream_t s);
 void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s);
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s);
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s);
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s);
 void launch_fix_lists(const DevMesh &m, cudaStream_t s);
+void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s);
 
 /* nucleation (sevc_nucleation.cu) */
 void launch_rng_init(curandState *st, int n, cudaStream_t s);
 void launch_nucleation(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s);
 int rng_record(int nstreams, int ndraws, double *host_out);
+
+/* adjoint (sevc_adjoint.cu) */
+struct AdjointBuffers {
+    double2 *lam;    /* adjoint of the positions (current step boundary) */
+    double2 *lx, *lv;/* adjoint of the post-event positions / of the velocities */
+    uint8_t *mark;   /* vertices moved by an event in the step */
+    double *sgn;     /* sign of each grain's area at the step's start */
+    double *gse;     /* dL/dSE per grain (accumulated) */
+    double *gmu;     /* dL/dmu per vertex (accumulated) */
+    double *ggam;    /* dL/dGB_scaling per vertex (accumulated) */
+    double *dlda;    /* dL/dA per grain of the statistic */
+    double *scalars; /* reduced dL/dmu, dL/dGB_scaling */
+};
+/* soft histogram of a_g = |A_g| sc over nbins bins of [0, amax), divided by nnorm */
+void launch_histogram(const DevMesh &m, int nbins, double amax, double sc, double nnorm, double *blockbins,
+                      double *hist, cudaStream_t s);
+int histogram_blocks(const DevMesh &m);
+/* lam = d(sum_k dldh_k h_k)/dx at the current state */
+void launch_hist_seed(const DevMesh &m, int nbins, double amax, double sc, double nnorm, const double *dldh,
+                      double *dlda, double2 *lam, cudaStream_t s);
+/* one step backward: `rec` views the mesh as recorded at the step's start,
+ * log / ven1 / vel1 its events and the enabled flags and velocities after it */
+void launch_adjoint_step(const DevMesh &rec, const AdjointBuffers &a, double dt, double mu, double eps, double s_gb,
+                         const EventRec *log, const int *nlog, const uint8_t *ven1, const double2 *vel1,
+                         cudaStream_t s);
+void launch_sum_ordered(const double *a, int n, double *out, cudaStream_t s);
+/* out[0..6] = count, sum |A|, sum A^2, sum vlen, 3-sided count, min |A|, max |A| over grains [lo, hi) */
+void launch_grain_stats(const DevMesh &m, int lo, int hi, double *out, cudaStream_t s);
 
 #define SEVC_CUDA_OK(expr) ((expr) == cudaSuccess)
 

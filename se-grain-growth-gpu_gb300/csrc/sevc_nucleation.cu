@@ -44,24 +44,32 @@ __global__ void k_rng_draw(curandState *st, int n, int ndraws, double *out)
 }
 
 /* compute_nucleation_factor's draws + get_vertex_id_per_block
- * (src/nucleation2.cu:239-363), on the reference's 32x256 grid */
-__global__ void __launch_bounds__(NTHR) k_nucl_blocks(DevMesh m, curandState *rng, curandState *saved, int *buf)
+ * (src/nucleation2.cu:239-363), on the reference's 32x256 grid; blockIdx.y
+ * is the instance, whose own 8192 streams walk its own vertex indices */
+__global__ void __launch_bounds__(NTHR) k_nucl_blocks(DevMesh m, curandState *rng, curandState *saved, int *buf,
+                                                     const int *nucl_on)
 {
     __shared__ int alive[NTHR], pick[NTHR];
+    int inst = blockIdx.y;
+    if (!nucl_on[inst]) return;
+    int vo = m.voff[inst], nvi = m.voff[inst + 1] - vo;
+    rng += (size_t)inst * GRID;
+    saved += (size_t)inst * GRID;
+    buf += 64 * inst;
     int tid = blockIdx.x * NTHR + threadIdx.x;
     curandState s = rng[tid];
     saved[tid] = s;
     int n_alive = 0;
-    for (int v = tid; v < m.nv; v += GRID) n_alive += m.ven[v] ? 1 : 0;
+    for (int v = tid; v < nvi; v += GRID) n_alive += m.ven[vo + v] ? 1 : 0;
     for (int k = 0; k < 2 * n_alive; k++) (void)curand_uniform_double(&s);
     alive[threadIdx.x] = n_alive;
     int rid = -1;
     if (n_alive > 0) {
         int n_steps = (int)(curand_uniform_double(&s) * (n_alive - 1));
         int k = 0;
-        for (int v = tid; v < m.nv; v += GRID)
-            if (m.ven[v]) {
-                if (k == n_steps) { rid = v; break; }
+        for (int v = tid; v < nvi; v += GRID)
+            if (m.ven[vo + v]) {
+                if (k == n_steps) { rid = vo + v; break; }
                 k++;
             }
     }
@@ -226,10 +234,20 @@ __device__ void init_boundary_dev(const DevMesh &m, int b, int ini, int end) /* 
 
 /* get_vertex_id2 (:375-443), the chosen vertex's factor
  * (compute_nucleation_factor for that vertex), get_nucleation_ids (:33-72)
- * and nucleate (:474-676) */
+ * and nucleate (:474-676); one thread per instance */
 __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *saved, const int *buf, int *ctr,
-                              double eps, double scaling, double MC_k)
+                              const int *nucl_on, double eps, double scaling, double MC_k)
 {
+    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= m.ninst || !nucl_on[inst]) return;
+    int vo = m.voff[inst], v_end = m.voff[inst + 1];
+    int bo = m.boff[inst], b_end = m.boff[inst + 1];
+    int go = m.goff[inst], g_end = m.goff[inst + 1];
+    rng += (size_t)inst * GRID;
+    saved += (size_t)inst * GRID;
+    buf += 64 * inst;
+    ctr += (size_t)inst * CTR_COUNT;
+    int *nlist = m.nlist + go, *nnlist = m.nnlist + inst;
     int tot = 0;
     for (int i = 0; i < NBLK; i++) tot += buf[NBLK + i];
     curandState s0 = rng[0];
@@ -242,7 +260,7 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
         pc += pn;
     }
     int v = cand;
-    if (v < 0 || v >= m.nv || !m.ven[v]) {
+    if (v < vo || v >= v_end || !m.ven[v]) {
         /* the reference would read a stale or out-of-range vertex here */
         raise_err(m, ERRB_RNG);
         ctr[CTR_CANDIDATE] = -1;
@@ -250,9 +268,9 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
         return;
     }
     /* the two draws compute_nucleation_factor made for v: v is the k-th
-     * enabled vertex of stream (v mod 8192) */
-    int t = v % GRID, k = 0;
-    for (int u = t; u < v; u += GRID) k += m.ven[u] ? 1 : 0;
+     * enabled vertex of stream ((v - vo) mod 8192) */
+    int t = (v - vo) % GRID, k = 0;
+    for (int u = vo + t; u < v; u += GRID) k += m.ven[u] ? 1 : 0;
     curandState s = saved[t];
     for (int j = 0; j < 2 * k; j++) (void)curand_uniform_double(&s);
     double u1 = curand_uniform_double(&s);
@@ -285,9 +303,9 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
 
     /* get_nucleation_ids: lowest free slots */
     int gfree = -1, bfree[3] = { -1, -1, -1 }, vfree[2] = { -1, -1 };
-    for (int i = 0; i < m.ng; i++) if (!m.gen[i]) { gfree = i; break; }
-    for (int i = 0, f = 0; i < m.nb && f < 3; i++) if (!m.ben[i]) bfree[f++] = i;
-    for (int i = 0, f = 0; i < m.nv && f < 2; i++) if (!m.ven[i]) vfree[f++] = i;
+    for (int i = go; i < g_end; i++) if (!m.gen[i]) { gfree = i; break; }
+    for (int i = bo, f = 0; i < b_end && f < 3; i++) if (!m.ben[i]) bfree[f++] = i;
+    for (int i = vo, f = 0; i < v_end && f < 2; i++) if (!m.ven[i]) vfree[f++] = i;
     bool diff_vrt = vfree[0] != vfree[1];
     bool diff_bnd = bfree[0] != bfree[1] && bfree[1] != bfree[2] && bfree[2] != bfree[0];
     if (!diff_bnd || !diff_vrt || gfree == -1) return;      /* :496-499 */
@@ -307,10 +325,10 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     init_boundary_dev(m, BC, B, C);
     init_boundary_dev(m, CA, C, A);
     add_bnd_slot(m, A, o.AD);
-    if (m.gtype[g] != GT_NUCLEATED) {                      /* keep m.nlist ascending */
-        int k = (*m.nnlist)++;
-        while (k > 0 && m.nlist[k - 1] > g) { m.nlist[k] = m.nlist[k - 1]; k--; }
-        m.nlist[k] = g;
+    if (m.gtype[g] != GT_NUCLEATED) {                      /* keep nlist ascending */
+        int k = (*nnlist)++;
+        while (k > 0 && nlist[k - 1] > g) { nlist[k] = nlist[k - 1]; k--; }
+        nlist[k] = g;
     }
     int *L = m.glist + (size_t)SEVC_MAXV * g;              /* nucleate_grain :596 */
     for (int i = 0; i < SEVC_MAXV; i++) L[i] = -1;
@@ -343,7 +361,7 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     if (af.x == A) af.x = C; else af.y = C;
     m.bv[o.AF] = af;
     t4 = m.vb[C]; t4.z = o.AF; m.vb[C] = t4;
-    m.evt[EVT_NUCLEATIONS]++;
+    m.evt[EVT_COUNT * inst + EVT_NUCLEATIONS]++;
 }
 
 } // namespace
@@ -355,8 +373,9 @@ void launch_rng_init(curandState *st, int n, cudaStream_t s)
 
 void launch_nucleation(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_nucl_blocks<<<NBLK, NTHR, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf);
-    COUNT_LAUNCHES(1), k_nucl_finish<<<1, 1, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf, x.counters, p.eps, p.scaling, p.MC_k);
+    COUNT_LAUNCHES(1), k_nucl_blocks<<<dim3(NBLK, p.ninst), NTHR, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf, x.nucl_on);
+    COUNT_LAUNCHES(1), k_nucl_finish<<<(p.ninst + 31) / 32, 32, 0, s>>>(m, x.rng, x.rng_saved, x.nucl_buf, x.counters,
+                                                                      x.nucl_on, p.eps, p.scaling, p.MC_k);
 }
 
 int rng_record(int nstreams, int ndraws, double *host_out)

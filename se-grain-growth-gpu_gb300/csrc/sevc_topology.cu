@@ -178,6 +178,7 @@ __global__ void k_compact_scatter(DevMesh m, int n, const int *blockcnt, int *ou
 __global__ void k_poll_vote(DevMesh m, const int *list, const int *n)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+    if (m.pdone[m.binst[list[i]]]) continue;
     int2 e = m.bv[list[i]];
     for (int k = 0; k < 2; k++) {
         int v = k == 0 ? e.x : e.y;
@@ -198,7 +199,7 @@ __global__ void k_poll_count(DevMesh m, const int *list, const int *n)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int b = list[i];
-        if (!(m.ben[b] && m.bcand[b])) continue;
+        if (!(m.ben[b] && m.bcand[b]) || m.pdone[m.binst[b]]) continue;
         int2 e = m.bv[b];
         m.bvotes[b] = (m.voted[e.x] == b) + (m.voted[e.y] == b);
     }
@@ -210,7 +211,7 @@ __global__ void k_poll_unlabel(DevMesh m, const int *list, const int *n)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int b = list[i];
-        if (!(m.ben[b] && m.bcand[b] && m.bvotes[b] == 2)) continue;
+        if (!(m.ben[b] && m.bcand[b] && m.bvotes[b] == 2) || m.pdone[m.binst[b]]) continue;
         int2 e = m.bv[b];
         int4 si = m.vb[e.x], se = m.vb[e.y];
         for (int j = 0; j < 3; j++) {
@@ -221,24 +222,28 @@ __global__ void k_poll_unlabel(DevMesh m, const int *list, const int *n)
     }
 }
 /* flips_per_block (:486-511) part one: a mismatch of boundary b marks
- * grid thread (b mod grid) as failed; then write_candidate_results
- * (:466-477) for the same element. */
+ * grid thread (b mod grid) as failed, b counted within its instance; then
+ * write_candidate_results (:466-477) for the same element. */
 __global__ void k_poll_compare_write(DevMesh m, int *threadfail, int grid)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= m.nb) return;
+    int inst = m.binst[b];
+    if (m.pdone[inst]) return;
     uint8_t en = m.ben[b], c = m.bcand[b];
-    if (en && c != m.bcandbuf[b]) threadfail[b % grid] = 1;
+    if (en && c != m.bcandbuf[b]) threadfail[(size_t)inst * grid + (b - m.boff[inst]) % grid] = 1;
     m.bcandbuf[b] = en ? c : 0;
 }
-/* part two, on the reference's grid: per thread AND over its stride set
- * (already folded into threadfail), per block the shared-memory tree
- * whose bool += acts as OR, then AND over blocks (compare_candidates
- * :526-537). */
-__global__ void k_poll_final(int *threadfail, int *converged)
+/* part two, on the reference's grid (blockIdx.y = instance): per thread
+ * AND over its stride set (already folded into threadfail), per block the
+ * shared-memory tree whose bool += acts as OR (compare_candidates
+ * :526-537) */
+__global__ void k_poll_final(DevMesh m, int *threadfail, int *pblock)
 {
     __shared__ int t[256];
-    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    int inst = blockIdx.y;
+    if (m.pdone[inst]) return;
+    size_t tid = (size_t)inst * gridDim.x * blockDim.x + blockIdx.x * blockDim.x + threadIdx.x;
     t[threadIdx.x] = threadfail[tid] ? 0 : 1;
     threadfail[tid] = 0;
     __syncthreads();
@@ -246,7 +251,19 @@ __global__ void k_poll_final(int *threadfail, int *converged)
         if ((int)threadIdx.x < i) t[threadIdx.x] = (t[threadIdx.x] || t[threadIdx.x + i]) ? 1 : 0;
         __syncthreads();
     }
-    if (threadIdx.x == 0 && !t[0]) atomicAnd(converged, 0);
+    if (threadIdx.x == 0) pblock[(size_t)inst * gridDim.x + blockIdx.x] = t[0];
+}
+/* then the host's AND over blocks (:533-535): an instance whose blocks all
+ * passed has converged and takes no further iteration this step */
+__global__ void k_poll_status(DevMesh m, const int *pblock, int nblocks, int *piters, int *nrun)
+{
+    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= m.ninst || m.pdone[inst]) return;
+    piters[inst]++;
+    int ok = 1;
+    for (int i = 0; i < nblocks; i++) ok &= pblock[(size_t)inst * nblocks + i] != 0;
+    if (ok) m.pdone[inst] = 1;
+    else atomicAdd(nrun, 1);
 }
 
 /* ------------------------------------------------------------------ */
@@ -377,10 +394,17 @@ __device__ bool sorted_contains(const int *a, int lo, int hi, int x)
  * boundary in index order.  Only listed boundaries (those qualifying at the
  * count) and boundaries re-wired during the scan (CE) can qualify, so the
  * scan visits exactly those, in index order, re-testing each on visit. */
-constexpr int EXTRA_CAP = 1024;
-__global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int *extra)
+/* One thread per instance, each over its own part of the ascending list. */
+__global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int *extra, int *segcnt)
 {
-    int N = *n, i = 0, ne = 0;
+    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= m.ninst) return;
+    int i = lower_bound_i(list, *n, m.boff[inst]);
+    int N = lower_bound_i(list, *n, m.boff[inst + 1]);
+    segcnt[inst] = N - i;
+    extra += (size_t)inst * EXTRA_CAP;
+    int *evt = m.evt + EVT_COUNT * inst;
+    int ne = 0;
     while (i < N || ne > 0) {
         int b;
         if (ne > 0 && (i >= N || extra[0] < list[i])) {
@@ -398,7 +422,7 @@ __global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int
         int CE = remove_two_grains_dev(m, b, gnic);
         m.gen[gic[0]] = 0;
         m.gen[gic[1]] = 0;
-        m.evt[EVT_TWO_THREE]++;
+        evt[EVT_TWO_THREE]++;
         if (CE > b && !sorted_contains(list, i, N, CE)) {
             int g2[2];
             if (two_three_qualifies(m, CE, g2)) {
@@ -453,6 +477,7 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
     int A = L[0], B = L[1], C = L[2];
     double D = m.D;
     double2 pa = m.pos[A], pb = m.pos[B], pc = m.pos[C];
+    log_event(m, EV_REMOVE, A, B, C, pa, pb, pc);
     double nAB = arclen(pa, pb, D), nBC = arclen(pb, pc, D), nCA = arclen(pc, pa, D);
     double denom = nAB + nBC + nCA;
     double x0 = 0, y0 = 0;                                      /* adjust_origin_for_points, 3 points */
@@ -521,12 +546,15 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
  * ascending index order */
 __global__ void k_remove_grains(DevMesh m, const int *list, const int *n)
 {
-    int N = *n;
-    for (int i = 0; i < N; i++) {
+    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= m.ninst) return;
+    int lo = lower_bound_i(list, *n, m.goff[inst]);
+    int hi = lower_bound_i(list, *n, m.goff[inst + 1]);
+    for (int i = lo; i < hi; i++) {
         int g = list[i];
         if (m.gen[g] && m.gcand[g]) {
             remove_grain_dev(m, g);
-            m.evt[EVT_REMOVALS]++;
+            m.evt[EVT_COUNT * inst + EVT_REMOVALS]++;
         }
     }
 }
@@ -583,6 +611,7 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
     m.vg[A] = ga;
     m.vg[B] = gb;
     double2 pa = m.pos[A], pb = m.pos[B];                 /* vector2_mean, src/geometry.h:311 */
+    log_event(m, EV_FLIP, A, B, -1, pa, pb, pb);
     double2 c = pa;
     c.x += wrapd(pb.x, pa.x, m.D) / 2;
     c.y += wrapd(pb.y, pa.y, m.D) / 2;
@@ -608,12 +637,15 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
  * rest are applied in ascending boundary order */
 __global__ void k_flips(DevMesh m, double eps, const int *list, const int *n)
 {
-    int N = *n;
-    for (int i = 0; i < N; i++) {
+    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= m.ninst) return;
+    int lo = lower_bound_i(list, *n, m.boff[inst]);
+    int hi = lower_bound_i(list, *n, m.boff[inst + 1]);
+    for (int i = lo; i < hi; i++) {
         int b = list[i];
         if (m.ben[b] && m.bcand[b]) {
             flip_dev(m, b, eps);
-            m.evt[EVT_FLIPS]++;
+            m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
         }
     }
 }
@@ -706,6 +738,16 @@ __global__ void k_fix_reset(DevMesh m)
     *m.nmod = 0;
 }
 
+/* instance of every boundary and grain from the offset tables */
+__global__ void k_fill_instance_ids(DevMesh m)
+{
+    int stride = gridDim.x * blockDim.x;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < m.nb; b += stride)
+        m.binst[b] = lower_bound_i(m.boff, m.ninst + 1, b + 1) - 1;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.ng; g += stride)
+        m.ginst[g] = lower_bound_i(m.goff, m.ninst + 1, g + 1) - 1;
+}
+
 template <int KIND>
 void compact_impl(const DevMesh &m, const DevScratch &x, int n, int *out, int *n_out, cudaStream_t s)
 {
@@ -737,10 +779,10 @@ void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *can
     COUNT_LAUNCHES(1), k_poll_count<<<g, TPB, 0, s>>>(m, cand, ncand);
     COUNT_LAUNCHES(1), k_poll_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
     int grid = p.n_blocks * p.n_threads;
-    int one = 1;
-    cudaMemcpyAsync(x.counters + CTR_CONVERGED, &one, sizeof(int), cudaMemcpyHostToDevice, s);
     COUNT_LAUNCHES(1), k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
-    COUNT_LAUNCHES(1), k_poll_final<<<p.n_blocks, p.n_threads, 0, s>>>(x.threadfail, x.counters + CTR_CONVERGED);
+    COUNT_LAUNCHES(1), k_poll_final<<<dim3(p.n_blocks, p.ninst), p.n_threads, 0, s>>>(m, x.threadfail, x.pblock);
+    cudaMemsetAsync(x.nrun, 0, sizeof(int), s);
+    COUNT_LAUNCHES(1), k_poll_status<<<(p.ninst + 127) / 128, 128, 0, s>>>(m, x.pblock, p.n_blocks, x.piters, x.nrun);
 }
 
 void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
@@ -750,9 +792,13 @@ void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaS
     COUNT_LAUNCHES(1), k_conflict_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
 }
 
-void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s)
+inline int instgrid(const DevMesh &m) { return (m.ninst + 31) / 32; }
+
+void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, int pass,
+                             cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_remove_two_three<<<1, 1, 0, s>>>(m, list, n, x.extra);
+    COUNT_LAUNCHES(1), k_remove_two_three<<<instgrid(m), 32, 0, s>>>(m, list, n, x.extra,
+                                                                     x.segcnt + (size_t)pass * m.ninst);
 }
 
 void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s)
@@ -762,7 +808,7 @@ void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s)
 
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_remove_grains<<<1, 1, 0, s>>>(m, list, n);
+    COUNT_LAUNCHES(1), k_remove_grains<<<instgrid(m), 32, 0, s>>>(m, list, n);
 }
 
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
@@ -774,7 +820,7 @@ void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncan
                   cudaStream_t s)
 {
     (void)x;
-    COUNT_LAUNCHES(1), k_flips<<<1, 1, 0, s>>>(m, eps, cand, ncand);
+    COUNT_LAUNCHES(1), k_flips<<<instgrid(m), 32, 0, s>>>(m, eps, cand, ncand);
 }
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)
@@ -784,4 +830,9 @@ void launch_fix_lists(const DevMesh &m, cudaStream_t s)
     COUNT_LAUNCHES(1), k_fix_replace<<<WL_BLOCKS, TPB, 0, s>>>(m);
     COUNT_LAUNCHES(1), k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
     COUNT_LAUNCHES(1), k_fix_reset<<<1, 1, 0, s>>>(m);
+}
+
+void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_fill_instance_ids<<<4 * WL_BLOCKS, TPB, 0, s>>>(m);
 }

@@ -20,7 +20,11 @@ STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "CAPACITY", 4: "NONCONVERGED", 5: "TO
 EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_from_arrays", "sevc_destroy", "sevc_load_mesh_host",
            "sevc_step", "sevc_run_steps", "sevc_should_continue", "sevc_export_text", "sevc_get_state",
            "sevc_mesh_sizes", "sevc_check_data", "sevc_run_program", "sevc_rng_record", "sevc_set_profiling",
-           "sevc_get_profile", "sevc_last_error", "sevc_set_exact_all", "sevc_rng_record_noalloc"]
+           "sevc_get_profile", "sevc_last_error", "sevc_set_exact_all", "sevc_rng_record_noalloc",
+           "sevc_create_batch", "sevc_instance_count", "sevc_instance_ranges", "sevc_instance_info",
+           "sevc_export_instance_text", "sevc_set_mobility", "sevc_set_gb_scaling", "sevc_set_stored_energy",
+           "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
+           "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats"]
 
 
 class SevcError(RuntimeError):
@@ -57,6 +61,12 @@ _MESH_FIELDS = [
 
 class MeshHost(C.Structure):
     _fields_ = [("nv", C.c_int), ("nb", C.c_int), ("ng", C.c_int)] + [(f, C.c_void_p) for f, _, _ in _MESH_FIELDS]
+
+
+class GrainStats(C.Structure):
+    _fields_ = [("n_grains", C.c_int), ("n_three_sided", C.c_int), ("mean_area", C.c_double),
+                ("std_area", C.c_double), ("min_area", C.c_double), ("max_area", C.c_double),
+                ("mean_sides", C.c_double)]
 
 
 class StepInfo(C.Structure):
@@ -184,6 +194,66 @@ class Engine:
                                              len(oris), oris.ctypes.data, se.ctypes.data, C.byref(h)))
         return cls(h, opt)
 
+    @classmethod
+    def from_batch(cls, opt, meshes):
+        """A batched handle over `meshes`, each a dict with xy, ridges, oris, se
+        (the arrays of from_arrays)."""
+        n = len(meshes)
+        xy = [np.ascontiguousarray(m["xy"], np.float64) for m in meshes]
+        rd = [np.ascontiguousarray(m["ridges"], np.int32) for m in meshes]
+        ori = [np.ascontiguousarray(m["oris"], np.float64) for m in meshes]
+        se = [np.ascontiguousarray(m["se"], np.float64) for m in meshes]
+        ints = lambda v: (C.c_int * n)(*v)
+        ptrs = lambda arrs: (C.c_void_p * n)(*[a.ctypes.data for a in arrs])
+        L = lib()
+        L.sevc_create_batch.argtypes = [C.POINTER(Options), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]
+        h = C.c_void_p()
+        _check(L.sevc_create_batch(C.byref(opt), n, ints([len(a) for a in xy]), ptrs(xy), ints([len(a) for a in rd]),
+                                   ptrs(rd), ints([len(a) for a in ori]), ptrs(ori), ptrs(se), C.byref(h)))
+        eng = cls(h, opt)
+        eng._keep = (xy, rd, ori, se)
+        return eng
+
+    def instance_count(self):
+        n = C.c_int()
+        lib().sevc_instance_count.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        _check(lib().sevc_instance_count(self._h, C.byref(n)))
+        return n.value
+
+    def instance_ranges(self):
+        """(voff, boff, goff), each ninst+1 int32 offsets."""
+        n = self.instance_count()
+        out = [np.zeros(n + 1, np.int32) for _ in range(3)]
+        lib().sevc_instance_ranges.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _check(lib().sevc_instance_ranges(self._h, *[a.ctypes.data for a in out]))
+        return tuple(out)
+
+    def instance_info(self, inst):
+        info = StepInfo()
+        lib().sevc_instance_info.argtypes = [C.c_void_p, C.c_int, C.POINTER(StepInfo)]
+        _check(lib().sevc_instance_info(self._h, inst, C.byref(info)))
+        return info
+
+    def export_instance(self, inst, path, time):
+        lib().sevc_export_instance_text.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_double]
+        _check(lib().sevc_export_instance_text(self._h, inst, path.encode(), time))
+
+    def instance_state(self, state, inst):
+        """Instance `inst`'s part of a get_state() dict, in its own indices."""
+        vo, bo, go = self.instance_ranges()
+        v0, v1, b0, b1, g0, g1 = vo[inst], vo[inst + 1], bo[inst], bo[inst + 1], go[inst], go[inst + 1]
+        sl = {"v": slice(v0, v1), "v3": slice(3 * v0, 3 * v1), "b": slice(b0, b1), "g": slice(g0, g1),
+              "g100": slice(MAXV * g0, MAXV * g1)}
+        shift = {"vb": b0, "vg": g0, "bini": v0, "bend": v0, "glist": v0}
+        out = {}
+        for f, k, _ in _MESH_FIELDS:
+            a = state[f][sl[k]].copy()
+            if f in shift:
+                a = np.where(a >= 0, a - shift[f], a)
+            out[f] = a
+        return out
+
     def close(self):
         if self._h:
             lib().sevc_destroy(self._h)
@@ -223,6 +293,62 @@ class Engine:
         mh = MeshHost(self.nv, self.nb, self.ng, *[arrs[f].ctypes.data for f, _, _ in _MESH_FIELDS])
         _check(lib().sevc_get_state(self._h, C.byref(mh)))
         return arrs
+
+    # ---- checkpoint files, statistics ----
+    def checkpoint_save(self, path):
+        lib().sevc_checkpoint_save.argtypes = [C.c_void_p, C.c_char_p]
+        _check(lib().sevc_checkpoint_save(self._h, path.encode()))
+
+    def checkpoint_load(self, path):
+        lib().sevc_checkpoint_load.argtypes = [C.c_void_p, C.c_char_p]
+        _check(lib().sevc_checkpoint_load(self._h, path.encode()))
+
+    def grain_stats(self, inst=-1):
+        s = GrainStats()
+        lib().sevc_grain_stats.argtypes = [C.c_void_p, C.c_int, C.POINTER(GrainStats)]
+        _check(lib().sevc_grain_stats(self._h, inst, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in GrainStats._fields_}
+
+    # ---- parameters and the adjoint ----
+    def set_mobility(self, mu):
+        lib().sevc_set_mobility.argtypes = [C.c_void_p, C.c_double]
+        _check(lib().sevc_set_mobility(self._h, float(mu)))
+
+    def set_gb_scaling(self, s):
+        lib().sevc_set_gb_scaling.argtypes = [C.c_void_p, C.c_double]
+        _check(lib().sevc_set_gb_scaling(self._h, float(s)))
+
+    def set_stored_energy(self, se):
+        se = np.ascontiguousarray(se, np.float64)
+        assert se.shape == (self.ng,)
+        lib().sevc_set_stored_energy.argtypes = [C.c_void_p, C.c_void_p]
+        _check(lib().sevc_set_stored_energy(self._h, se.ctypes.data))
+
+    def tape_start(self, checkpoint_every):
+        lib().sevc_tape_start.argtypes = [C.c_void_p, C.c_int]
+        _check(lib().sevc_tape_start(self._h, int(checkpoint_every)))
+
+    def tape_stop(self):
+        lib().sevc_tape_stop.argtypes = [C.c_void_p]
+        _check(lib().sevc_tape_stop(self._h))
+
+    def area_histogram(self, nbins, amax):
+        out = np.zeros(nbins)
+        lib().sevc_area_histogram.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+        _check(lib().sevc_area_histogram(self._h, nbins, float(amax), out.ctypes.data))
+        return out
+
+    def adjoint_histogram(self, nbins, amax, dloss_dhist):
+        """(dloss/dSE per grain, dloss/dGB_scaling, dloss/dmu) for the taped steps."""
+        d = np.ascontiguousarray(dloss_dhist, np.float64)
+        assert d.shape == (nbins,)
+        gse = np.zeros(self.ng)
+        ggb, gmu = C.c_double(), C.c_double()
+        lib().sevc_adjoint_histogram.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p,
+                                                 C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _check(lib().sevc_adjoint_histogram(self._h, nbins, float(amax), d.ctypes.data, gse.ctypes.data,
+                                            C.byref(ggb), C.byref(gmu)))
+        return gse, ggb.value, gmu.value
 
     def set_exact_all(self, on):
         lib().sevc_set_exact_all.argtypes = [C.c_void_p, C.c_int]

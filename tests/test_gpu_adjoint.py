@@ -1,0 +1,159 @@
+"""Adjoint of the time step: gradients of the smoothed grain-area histogram
+loss with respect to per-grain stored energies, GB_scaling and mobility.
+
+Checked (1) against the FP64 torch restatement in oracle/adjoint_ref.py on
+a window without topological events, where both differentiate the same
+map (tolerance 1e-6 relative: both evaluate the finite-difference velocity,
+whose derivative has cancellation of order 1e-8), and (2) against central
+finite differences of the GPU forward itself through windows with flips
+and removals, with the event sequence checked identical in the perturbed
+runs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NB, AMAX = 20, 3.0
+
+
+def options(sevc, n, dt):
+    o = sevc.default_options(n_grains=n, dt=dt, dtau=1.0, domain_bound=1.0, GB_eps=0.0, GB_scaling=1.0, SE_eps=1.0,
+                             SE_min=999.0, SE_max=999.0, do_nucleation=0, nmax=10 ** 8, tmax=-1, snap_gap=10 ** 8,
+                             n_blocks=32, n_threads=256)
+    o.min_grains = -1
+    return o
+
+
+def make(sevc, mesh, dt):
+    return sevc.Engine.from_arrays(options(sevc, len(mesh["oris"]), dt), mesh["xy"], mesh["ridges"], mesh["oris"],
+                                   mesh["se"])
+
+
+def forward(sevc, mesh, dt, steps, se, gam, mu, every=None):
+    e = make(sevc, mesh, dt)
+    e.set_stored_energy(se)
+    e.set_gb_scaling(gam)
+    e.set_mobility(mu)
+    if every:
+        e.tape_start(every)
+    events = []
+    for _ in range(steps):
+        i = e.step()
+        events.append((i.n_flips, i.n_removals, i.n_two_three))
+    return e, e.area_histogram(NB, AMAX), events
+
+
+def loss_of(h, target):
+    return float(((h - target) ** 2).mean())
+
+
+def dloss(h, target):
+    return 2.0 * (h - target) / len(h)
+
+
+def test_histogram_matches_reference(gpu):
+    import meshgen
+    from oracle import adjoint_ref
+    import torch
+    mesh = meshgen.make_inputs(300, 3)
+    e = make(gpu, mesh, 1e-6)
+    st = e.get_state()
+    h = e.area_histogram(NB, AMAX)
+    topo = adjoint_ref.Topology(st)
+    x = torch.tensor(np.stack([st["px"], st["py"]], 1))
+    ref = adjoint_ref.histogram(x, topo, 1.0, NB, AMAX).numpy()
+    assert np.allclose(h, ref, rtol=1e-12, atol=1e-15)
+    assert abs(h.sum() - 1.0) < 0.05
+
+
+def test_adjoint_matches_fp64_reference_without_events(gpu):
+    import meshgen
+    from oracle import adjoint_ref
+    mesh = meshgen.make_inputs(80, 5)
+    se = np.random.default_rng(1).uniform(0.0, 0.5, 80)
+    dt, steps = 2e-6, 40
+    e, h, events = forward(gpu, mesh, dt, steps, se, 1.0, 1.0)
+    assert all(ev == (0, 0, 0) for ev in events), "window must have no topological event"
+    target = h * 0.9 + 0.1 / NB
+    e.close()
+    e0 = make(gpu, mesh, dt)
+    e0.set_stored_energy(se)
+    st0 = e0.get_state()
+    e0.close()
+    e, h, _ = forward(gpu, mesh, dt, steps, se, 1.0, 1.0, every=15)
+    gse, ggam, gmu = e.adjoint_histogram(NB, AMAX, dloss(h, target))
+    loss_r, gse_r, ggam_r, gmu_r, h_r = adjoint_ref.loss_and_grads(st0, se, 1.0, 1.0, dt, steps, 1.0, NB, AMAX,
+                                                                    target)
+    assert np.allclose(h, h_r, rtol=1e-9, atol=1e-14)
+    assert abs(loss_of(h, target) - loss_r) <= 1e-9 * abs(loss_r)
+    scale = np.abs(gse_r).max()
+    assert np.abs(gse - gse_r).max() <= 1e-6 * scale, (np.abs(gse - gse_r).max(), scale)
+    assert abs(ggam - ggam_r) <= 1e-6 * abs(ggam_r), (ggam, ggam_r)
+    assert abs(gmu - gmu_r) <= 1e-6 * abs(gmu_r), (gmu, gmu_r)
+    e.close()
+
+
+def central_fd(gpu, mesh, dt, steps, se, gam, mu, target, which, h, direction=None):
+    """(loss(+h) - loss(-h)) / 2h of one parameter, with the event
+    sequences of both runs returned for comparison."""
+    out = []
+    for sgn in (1.0, -1.0):
+        s, g, m = se.copy(), gam, mu
+        if which == "se":
+            s = se + sgn * h * direction
+        elif which == "gamma":
+            g = gam + sgn * h
+        else:
+            m = mu + sgn * h
+        e, hh, ev = forward(gpu, mesh, dt, steps, s, g, m)
+        e.close()
+        out.append((loss_of(hh, target), ev))
+    return (out[0][0] - out[1][0]) / (2 * h), out[0][1], out[1][1]
+
+
+def test_adjoint_matches_central_differences_through_events(gpu):
+    """h = 1e-4: the forward's finite-difference velocity carries rounding
+    noise of ~1e-8 relative, which a step of 1e-6 turns into differences of
+    1e-6..1e-4 relative; at 1e-4 the central difference's own error
+    (O(h^2)) stays below 1e-7."""
+    import meshgen
+    mesh = meshgen.make_inputs(400, 9)
+    rng = np.random.default_rng(2)
+    se = rng.uniform(0.0, 0.5, 400)
+    dt, steps = 1e-4, 300
+    e, h, events = forward(gpu, mesh, dt, steps, se, 1.0, 1.0, every=100)
+    n_ev = np.array(events).sum(0)
+    assert n_ev[0] > 0 and n_ev[1] > 0, "window should contain flips and removals: %s" % n_ev
+    e2, h2, _ = forward(gpu, mesh, dt, steps, se * 1.3, 1.1, 0.9)
+    e2.close()
+    target = h2
+    gse, ggam, gmu = e.adjoint_histogram(NB, AMAX, dloss(h, target))
+    e.close()
+    d = rng.standard_normal(400)
+    checks = [("mu", gmu, None), ("gamma", ggam, None), ("se", float(gse @ d), d)]
+    for which, adj, direction in checks:
+        fd, ev_p, ev_m = central_fd(gpu, mesh, dt, steps, se, 1.0, 1.0, target, which, 1e-4, direction)
+        assert ev_p == events and ev_m == events, "%s: perturbed runs changed the event sequence" % which
+        assert abs(adj - fd) <= 2e-5 * abs(fd), (which, adj, fd)
+
+
+def test_torch_function_gradients(gpu):
+    torch = pytest.importorskip("torch")
+    import meshgen
+    import sevc_torch
+    mesh = meshgen.make_inputs(200, 4)
+    se0 = np.random.default_rng(3).uniform(0.0, 0.5, 200)
+    dt, steps = 2e-5, 60
+    target = torch.full((NB,), 1.0 / NB, dtype=torch.float64)
+    se = torch.tensor(se0, requires_grad=True)
+    gam = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    mu = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    h = sevc_torch.GrainAreaHistogram.apply(se, gam, mu, lambda: make(gpu, mesh, dt), steps, NB, AMAX, 25)
+    loss = sevc_torch.histogram_loss(h, target)
+    loss.backward()
+    e, hh, _ = forward(gpu, mesh, dt, steps, se0, 1.0, 1.0, every=25)
+    assert np.array_equal(h.detach().numpy(), hh)
+    gse, ggam, gmu = e.adjoint_histogram(NB, AMAX, dloss(hh, target.numpy()))
+    e.close()
+    assert np.allclose(se.grad.numpy(), gse, rtol=1e-12, atol=0)
+    assert np.isclose(float(gam.grad), ggam, rtol=1e-12) and np.isclose(float(mu.grad), gmu, rtol=1e-12)
