@@ -135,8 +135,14 @@ sevc_status sevc_export_text(sevc_handle *h, const char *path, double time);
  * copy the mesh into caller-owned arrays sized like sevc_mesh_sizes. */
 sevc_status sevc_get_state(sevc_handle *h, sevc_mesh_host *out);
 sevc_status sevc_mesh_sizes(const sevc_handle *h, int *nv, int *nb, int *ng);
-/* check_data, src/utils.h:85-336: number of violated invariants (>= 0). */
+/* check_data, src/utils.h:85-336: number of violated invariants (>= 0),
+ * counted on the device (one thread per boundary, vertex and grain). */
 sevc_status sevc_check_data(sevc_handle *h, int *n_bad);
+/* The same count on the host after a download of the mesh. */
+sevc_status sevc_check_data_host(sevc_handle *h, int *n_bad);
+/* The device count for a mesh held in host arrays (uploaded to temporary
+ * device memory); indices outside their arrays count as violations. */
+sevc_status sevc_check_mesh(const sevc_mesh_host *mesh, int *n_bad);
 
 /* The whole program of src/main.cu:21-424 after option loading: create
  * DATA folder, load, loop with snapshots and the reference's log lines.
@@ -258,6 +264,12 @@ sevc_status sevc_set_exact_all(sevc_handle *h, int on);
 sevc_status sevc_set_profiling(sevc_handle *h, int on);
 sevc_status sevc_get_profile(sevc_handle *h, int max_entries, char (*names)[48], double *ms,
                              int64_t *launches, int *n_entries);
+
+/* The number formatting of the snapshots: writes x as printf("%.16f")
+ * does (correctly rounded, ties to even) into out (at least 48 bytes),
+ * returns the length.  Integer arithmetic only, several times faster
+ * than printf; used by sevc_export_text. */
+int sevc_format_fixed16(double x, char *out);
 
 /* Text of the last error on this thread. */
 const char *sevc_last_error(void);

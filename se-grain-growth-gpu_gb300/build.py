@@ -23,7 +23,8 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC
            "-I", os.path.join(ROOT, "include")]
 CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-I", os.path.join(ROOT, "include")]
 
-CU = ["sevc_geometry.cu", "sevc_topology.cu", "sevc_nucleation.cu", "sevc_adjoint.cu", "sevc_engine.cu"]
+CU = ["sevc_geometry.cu", "sevc_topology.cu", "sevc_nucleation.cu", "sevc_adjoint.cu", "sevc_check.cu",
+      "sevc_engine.cu"]
 C = ["sevc_host.c"]
 HDRS = ["sevc_device.cuh", "sevc_internal.h", "sevc_host.h"]
 

@@ -843,12 +843,59 @@ sevc_status sevc_export_instance_text(sevc_handle *h, int inst, const char *path
 sevc_status sevc_check_data(sevc_handle *h, int *n_bad)
 {
     if (!h || !n_bad) return SEVC_ERR_ARG;
+    launch_check(h->m, h->x.nrun, h->stream);   /* nrun is free between steps */
+    if (read_ints(h, h->x.nrun, 1, n_bad)) return SEVC_ERR_CUDA;
+    return SEVC_OK;
+}
+
+sevc_status sevc_check_data_host(sevc_handle *h, int *n_bad)
+{
+    if (!h || !n_bad) return SEVC_ERR_ARG;
     sevc_hmesh hm;
     if (sevc_hmesh_alloc(&hm, h->nv, h->nb, h->ng)) return SEVC_ERR_CAPACITY;
     sevc_status st = sevc_get_state(h, &hm.m);
     if (!st) *n_bad = sevc_host_check(&hm.m);
     sevc_hmesh_free(&hm);
     return st;
+}
+
+sevc_status sevc_check_mesh(const sevc_mesh_host *hm, int *n_bad)
+{
+    if (!hm || !n_bad || hm->nv < 0 || hm->nb < 0 || hm->ng < 0) return SEVC_ERR_ARG;
+    if (require_device()) return SEVC_ERR_CUDA;
+    size_t V = hm->nv, B = hm->nb, G = hm->ng;
+    std::vector<int4> vb(V), vg(V);
+    std::vector<int2> bv(B);
+    for (size_t i = 0; i < V; i++) {
+        vb[i] = make_int4(hm->vb[3 * i], hm->vb[3 * i + 1], hm->vb[3 * i + 2], -1);
+        vg[i] = make_int4(hm->vg[3 * i], hm->vg[3 * i + 1], hm->vg[3 * i + 2], -1);
+    }
+    for (size_t i = 0; i < B; i++) bv[i] = make_int2(hm->bini[i], hm->bend[i]);
+    DevMesh m{};
+    m.nv = (int)V; m.nb = (int)B; m.ng = (int)G;
+    size_t off[9], total = 0;
+    size_t sz[9] = { V * 16, V * 16, V, B * 8, B, G * SEVC_MAXV * 4, G * 4, G, 4 };
+    for (int i = 0; i < 9; i++) { off[i] = total; total += align256(sz[i]); }
+    char *d = nullptr;
+    if (!cuda_ok(cudaMalloc(&d, total), "cudaMalloc")) return SEVC_ERR_CUDA;
+    m.vb = (int4 *)(d + off[0]); m.vg = (int4 *)(d + off[1]); m.ven = (uint8_t *)(d + off[2]);
+    m.bv = (int2 *)(d + off[3]); m.ben = (uint8_t *)(d + off[4]); m.glist = (int *)(d + off[5]);
+    m.gvlen = (int *)(d + off[6]); m.gen = (uint8_t *)(d + off[7]);
+    int *cnt = (int *)(d + off[8]);
+    bool ok = cuda_ok(cudaMemcpy(m.vb, vb.data(), V * 16, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.vg, vg.data(), V * 16, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.ven, hm->ven, V, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.bv, bv.data(), B * 8, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.ben, hm->ben, B, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.glist, hm->glist, G * SEVC_MAXV * 4, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.gvlen, hm->gvlen, G * 4, cudaMemcpyHostToDevice), "upload") &&
+              cuda_ok(cudaMemcpy(m.gen, hm->gen, G, cudaMemcpyHostToDevice), "upload");
+    if (ok) {
+        launch_check(m, cnt, 0);
+        ok = cuda_ok(cudaMemcpy(n_bad, cnt, 4, cudaMemcpyDeviceToHost), "readback");
+    }
+    cudaFree(d);
+    return ok ? SEVC_OK : SEVC_ERR_CUDA;
 }
 
 sevc_status sevc_rng_record(int nstreams, int ndraws, double *out)

@@ -12,6 +12,7 @@
 
 #include <math.h>
 #include <stdarg.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -369,13 +370,109 @@ sevc_status sevc_load_mesh_host(const sevc_options *opt, sevc_mesh_host *out, in
 }
 
 /* ---------------------------------------------------------------- */
+/* exact "%.16f" and "%d" into a buffer                               */
+/* ---------------------------------------------------------------- */
+/* A finite double is m * 2^e with m < 2^53.  Its value times 10^16 is
+ * m * 10^16 * 2^e, and m * 10^16 < 2^107 fits an unsigned 128-bit integer,
+ * so the correctly rounded N = round(x * 10^16) (ties to even, as printf
+ * rounds in the default rounding mode) is an integer shift with an exact
+ * remainder; the text is N / 10^16, '.', and the 16 digits of N mod 10^16.
+ * Values of 2^73 or more, NaN and infinities go to snprintf. */
+typedef unsigned __int128 u128;
+
+static char *put_u128(char *p, u128 v)
+{
+    char tmp[48];
+    int n = 0;
+    do {
+        tmp[n++] = (char)('0' + (int)(v % 10));
+        v /= 10;
+    } while (v);
+    while (n) *p++ = tmp[--n];
+    return p;
+}
+
+static char *put_f16(char *p, double x)
+{
+    if (!isfinite(x) || fabs(x) >= 9.4e21) return p + sprintf(p, "%.16f", x);
+    if (signbit(x)) { *p++ = '-'; x = -x; }
+    u128 N = 0;
+    if (x != 0) {
+        int k;
+        double f = frexp(x, &k);                     /* x = f * 2^k, f in [0.5, 1) */
+        uint64_t mant = (uint64_t)ldexp(f, 53);      /* exact: 53 significant bits */
+        int e = k - 53;
+        u128 P = (u128)mant * (u128)10000000000000000ULL;
+        if (e >= 0) {
+            N = P << e;                              /* e <= 20 here: no overflow */
+        } else {
+            int s = -e;
+            if (s >= 108) {
+                N = 0;                               /* P < 2^107 <= half: rounds to 0 */
+            } else {
+                u128 q = P >> s, r = P - (q << s), half = (u128)1 << (s - 1);
+                if (r > half || (r == half && (q & 1))) q++;
+                N = q;
+            }
+        }
+    }
+    const u128 TEN16 = (u128)10000000000000000ULL;
+    p = put_u128(p, N / TEN16);
+    uint64_t frac = (uint64_t)(N % TEN16);
+    *p++ = '.';
+    for (int i = 15; i >= 0; i--) {
+        p[i] = (char)('0' + (int)(frac % 10));
+        frac /= 10;
+    }
+    return p + 16;
+}
+
+static char *put_int(char *p, int v)
+{
+    unsigned int u = (unsigned int)v;
+    if (v < 0) { *p++ = '-'; u = 0u - u; }
+    char tmp[12];
+    int n = 0;
+    do {
+        tmp[n++] = (char)('0' + u % 10);
+        u /= 10;
+    } while (u);
+    while (n) *p++ = tmp[--n];
+    return p;
+}
+
+int sevc_format_fixed16(double x, char *out)
+{
+    char *e = put_f16(out, x);
+    *e = 0;
+    return (int)(e - out);
+}
+
+/* ---------------------------------------------------------------- */
 /* snapshot text, src/io.h:280-377                                   */
 /* ---------------------------------------------------------------- */
+/* lines are formatted into a buffer with the exact formatter above and
+ * written in large blocks */
+typedef struct { FILE *f; char *buf, *p; size_t cap; int err; } outbuf;
+
+static void ob_flush(outbuf *b)
+{
+    size_t n = (size_t)(b->p - b->buf);
+    if (n && fwrite(b->buf, 1, n, b->f) != n) b->err = 1;
+    b->p = b->buf;
+}
+static void ob_room(outbuf *b, size_t need)
+{
+    if ((size_t)(b->p - b->buf) + need > b->cap) ob_flush(b);
+}
+
 int sevc_host_export(const sevc_mesh_host *m, const sevc_options *o, const char *path, double time)
 {
     FILE *f = fopen(path, "w");
     if (!f) { sevc_set_error("cannot write %s", path); return SEVC_ERR_IO; }
-    setvbuf(f, NULL, _IOFBF, 1 << 22);
+    outbuf ob = { f, NULL, NULL, (size_t)1 << 24, 0 };
+    ob.buf = ob.p = (char *)malloc(ob.cap);
+    if (!ob.buf) { fclose(f); sevc_set_error("out of host memory"); return SEVC_ERR_CAPACITY; }
     int cv = 0, cb = 0, cg = 0;
     for (int i = 0; i < m->nv; i++) cv += m->ven[i] != 0;
     for (int i = 0; i < m->nb; i++) cb += m->ben[i] != 0;
@@ -388,35 +485,67 @@ int sevc_host_export(const sevc_mesh_host *m, const sevc_options *o, const char 
             o->nucleation_scaling, SEVC_MAX_VRT_PER_GRN);
     fprintf(f, "VERTICES %d\nBOUNDARIES %d\nGRAINS %d\nCURR VERTICES %d\nCURR BOUNDARIES %d\nCURR GRAINS %d\n",
             m->nv, m->nb, m->ng, cv, cb, cg);
-    fputs("#VERTEX ENABLED ENERGY X Y VX VY VXbnd VXgrn VYbnd VYgrn VG1 G2 G3 N1 N2 N3\n", f);
+    fflush(f);
+#define SP (*ob.p++ = ' ')
+    const char *vh = "#VERTEX ENABLED ENERGY X Y VX VY VXbnd VXgrn VYbnd VYgrn VG1 G2 G3 N1 N2 N3\n";
+    ob_room(&ob, strlen(vh));
+    memcpy(ob.p, vh, strlen(vh)); ob.p += strlen(vh);
     for (int i = 0; i < m->nv; i++) {
         const int *s = &m->vb[3 * i];
         int nbr[3];
         for (int j = 0; j < 3; j++)
             nbr[j] = s[j] < 0 ? -1 : (m->bini[s[j]] == i ? m->bend[s[j]] : m->bini[s[j]]);
-        fprintf(f, "%d %d %.16f %.16f %.16f %.16f %.16f %.16f %.16f %.16f %.16f %d %d %d %d %d %d\n", i,
-                m->ven[i] ? 1 : 0, m->venergy[i], m->px[i], m->py[i], m->vx[i], m->vy[i], m->vel_bnd_x[i],
-                m->vel_grn_x[i], m->vel_bnd_y[i], m->vel_grn_y[i], m->vg[3 * i], m->vg[3 * i + 1],
-                m->vg[3 * i + 2], nbr[0], nbr[1], nbr[2]);
+        ob_room(&ob, 1024);
+        ob.p = put_int(ob.p, i); SP;
+        ob.p = put_int(ob.p, m->ven[i] ? 1 : 0);
+        const double vals[9] = { m->venergy[i], m->px[i], m->py[i], m->vx[i], m->vy[i], m->vel_bnd_x[i],
+                                 m->vel_grn_x[i], m->vel_bnd_y[i], m->vel_grn_y[i] };
+        for (int k = 0; k < 9; k++) { SP; ob.p = put_f16(ob.p, vals[k]); }
+        const int ints[6] = { m->vg[3 * i], m->vg[3 * i + 1], m->vg[3 * i + 2], nbr[0], nbr[1], nbr[2] };
+        for (int k = 0; k < 6; k++) { SP; ob.p = put_int(ob.p, ints[k]); }
+        *ob.p++ = '\n';
     }
-    fputs("#BOUNDARY ENABLED INI END ENERGY ARCLEN EXTTIME CANDIDATE\n", f);
-    for (int i = 0; i < m->nb; i++)
-        fprintf(f, "%d %d %d %d %.16f %.16f %.16f %d\n", i, m->ben[i] ? 1 : 0, m->bini[i], m->bend[i],
-                m->benergy[i], m->blen[i], m->btext[i], m->bcand[i] ? 1 : 0);
-    fputs("#GRAIN ID ENABLED NUCLEATED ORIENT SE AREA dAdt VLEN VERTICES\n", f);
+    const char *bh = "#BOUNDARY ENABLED INI END ENERGY ARCLEN EXTTIME CANDIDATE\n";
+    ob_room(&ob, strlen(bh));
+    memcpy(ob.p, bh, strlen(bh)); ob.p += strlen(bh);
+    for (int i = 0; i < m->nb; i++) {
+        ob_room(&ob, 512);
+        ob.p = put_int(ob.p, i); SP;
+        ob.p = put_int(ob.p, m->ben[i] ? 1 : 0); SP;
+        ob.p = put_int(ob.p, m->bini[i]); SP;
+        ob.p = put_int(ob.p, m->bend[i]); SP;
+        ob.p = put_f16(ob.p, m->benergy[i]); SP;
+        ob.p = put_f16(ob.p, m->blen[i]); SP;
+        ob.p = put_f16(ob.p, m->btext[i]); SP;
+        ob.p = put_int(ob.p, m->bcand[i] ? 1 : 0);
+        *ob.p++ = '\n';
+    }
+    const char *gh = "#GRAIN ID ENABLED NUCLEATED ORIENT SE AREA dAdt VLEN VERTICES\n";
+    ob_room(&ob, strlen(gh));
+    memcpy(ob.p, gh, strlen(gh)); ob.p += strlen(gh);
     for (int i = 0; i < m->ng; i++) {
         int n = m->gvlen[i];
-        fprintf(f, "%d %d %d %.16f %.16f %.16f %.16f %d ", i, m->gen[i] ? 1 : 0, (int)m->gtype[i], m->gori[i],
-                m->gse[i], m->garea[i], m->gdadt[i], n);
+        ob_room(&ob, 512 + 12 * SEVC_MAX_VRT_PER_GRN);
+        ob.p = put_int(ob.p, i); SP;
+        ob.p = put_int(ob.p, m->gen[i] ? 1 : 0); SP;
+        ob.p = put_int(ob.p, (int)m->gtype[i]); SP;
+        ob.p = put_f16(ob.p, m->gori[i]); SP;
+        ob.p = put_f16(ob.p, m->gse[i]); SP;
+        ob.p = put_f16(ob.p, m->garea[i]); SP;
+        ob.p = put_f16(ob.p, m->gdadt[i]); SP;
+        ob.p = put_int(ob.p, n); SP;
         const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * i];
         for (int j = 0; j < SEVC_MAX_VRT_PER_GRN; j++) {
-            if (j < n) fprintf(f, "%d ", L[j]);
-            else if (j == SEVC_MAX_VRT_PER_GRN - 1) fputs("-1", f);
-            else fputs("-1 ", f);
+            if (j < n) { ob.p = put_int(ob.p, L[j]); SP; }
+            else if (j == SEVC_MAX_VRT_PER_GRN - 1) { *ob.p++ = '-'; *ob.p++ = '1'; }
+            else { *ob.p++ = '-'; *ob.p++ = '1'; SP; }
         }
-        fputc('\n', f);
+        *ob.p++ = '\n';
     }
-    if (fclose(f)) { sevc_set_error("write error on %s", path); return SEVC_ERR_IO; }
+#undef SP
+    ob_flush(&ob);
+    free(ob.buf);
+    if (fclose(f) || ob.err) { sevc_set_error("write error on %s", path); return SEVC_ERR_IO; }
     return SEVC_OK;
 }
 
@@ -437,10 +566,17 @@ static int two_common(const sevc_mesh_host *m, int a, int b, int *g0, int *g1)
 static int in_list(const sevc_mesh_host *m, int g, int v)
 {
     const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * g];
-    for (int i = 0; i < m->gvlen[g]; i++)
+    int n = m->gvlen[g];
+    if (n > SEVC_MAX_VRT_PER_GRN) n = SEVC_MAX_VRT_PER_GRN;
+    for (int i = 0; i < n; i++)
         if (L[i] == v) return 1;
     return 0;
 }
+
+/* An index outside its array counts as one violation and is not followed
+ * (the reference would read out of bounds there); the device checker
+ * (sevc_check.cu) counts the same way. */
+static int inr(int x, int n) { return x >= 0 && x < n; }
 
 int sevc_host_check(const sevc_mesh_host *m)
 {
@@ -448,13 +584,19 @@ int sevc_host_check(const sevc_mesh_host *m)
     for (int b = 0; b < m->nb; b++) {
         if (!m->ben[b]) continue;
         int a = m->bini[b], c = m->bend[b];
+        if (!inr(a, m->nv) || !inr(c, m->nv)) { bad++; continue; }
         const int *sa = &m->vb[3 * a], *sc = &m->vb[3 * c];
         bad += a == c;
         bad += !m->ven[a] || !m->ven[c];
         bad += sa[0] != b && sa[1] != b && sa[2] != b;
         bad += sc[0] != b && sc[1] != b && sc[2] != b;
-        bad += !m->ben[sc[0]] || !m->ben[sc[1]] || !m->ben[sc[2]];
-        bad += !m->ben[sa[0]] || !m->ben[sa[1]] || !m->ben[sa[2]];
+        int ok_c = 1, ok_a = 1;
+        for (int j = 0; j < 3; j++) {
+            ok_c &= inr(sc[j], m->nb) && m->ben[sc[j]];
+            ok_a &= inr(sa[j], m->nb) && m->ben[sa[j]];
+        }
+        bad += !ok_c;
+        bad += !ok_a;
         int g0, g1;
         bad += two_common(m, a, c, &g0, &g1) < 2 || g0 == g1;
     }
@@ -463,28 +605,36 @@ int sevc_host_check(const sevc_mesh_host *m)
         const int *s = &m->vb[3 * v], *g = &m->vg[3 * v];
         bad += s[0] == s[1] || s[1] == s[2] || s[2] == s[0];
         bad += g[0] == g[1] || g[1] == g[2] || g[2] == g[0];
-        int nb[3];
+        int nb[3] = { -1, -2, -3 };
         for (int j = 0; j < 3; j++) {
+            int gok = inr(g[j], m->ng);
+            bad += !gok || !m->gen[g[j]];
+            bad += !gok || !in_list(m, g[j], v);
+            if (!inr(s[j], m->nb)) { bad++; continue; }
             bad += !m->ben[s[j]];
-            bad += g[j] < 0 || !m->gen[g[j]];
             bad += m->bini[s[j]] == m->bend[s[j]];
             nb[j] = m->bini[s[j]] == v ? m->bend[s[j]] : m->bini[s[j]];
             bad += m->bini[s[j]] != v && m->bend[s[j]] != v;
-            bad += g[j] < 0 || !in_list(m, g[j], v);
         }
         bad += nb[0] == nb[1] || nb[1] == nb[2] || nb[2] == nb[0];
     }
     for (int gi = 0; gi < m->ng; gi++) {
         if (!m->gen[gi]) continue;
         const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * gi];
-        for (int j = 0; j < m->gvlen[gi]; j++) bad += !m->ven[L[j]];
-        for (int j = 0; j < m->gvlen[gi]; j++) {
+        int n = m->gvlen[gi];
+        if (n < 0 || n > SEVC_MAX_VRT_PER_GRN) { bad++; continue; }
+        int listed = 1;
+        for (int j = 0; j < n; j++) {
+            if (!inr(L[j], m->nv)) { bad++; listed = 0; continue; }
+            bad += !m->ven[L[j]];
+        }
+        for (int j = 0; j < n && listed; j++) {
             const int *g = &m->vg[3 * L[j]];
             if (g[0] != gi && g[1] != gi && g[2] != gi) { bad++; break; }
         }
         int cnt = 0;
         for (int j = 0; j < SEVC_MAX_VRT_PER_GRN; j++) cnt += L[j] != -1;
-        bad += cnt != m->gvlen[gi];
+        bad += cnt != n;
     }
     return bad;
 }

@@ -89,6 +89,9 @@ void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncan
 void launch_fix_lists(const DevMesh &m, cudaStream_t s);
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s);
 
+/* check_data on the device (sevc_check.cu): violations counted into *out */
+void launch_check(const DevMesh &m, int *out, cudaStream_t s);
+
 /* nucleation (sevc_nucleation.cu) */
 void launch_rng_init(curandState *st, int n, cudaStream_t s);
 void launch_nucleation(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s);

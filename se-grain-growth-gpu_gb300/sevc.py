@@ -24,7 +24,8 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_create_batch", "sevc_instance_count", "sevc_instance_ranges", "sevc_instance_info",
            "sevc_export_instance_text", "sevc_set_mobility", "sevc_set_gb_scaling", "sevc_set_stored_energy",
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
-           "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats"]
+           "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
+           "sevc_check_data_host", "sevc_check_mesh"]
 
 
 class SevcError(RuntimeError):
@@ -150,6 +151,41 @@ def load_mesh_host(opt):
     mh = MeshHost(nv.value, nb.value, ng.value, *[arrs[f].ctypes.data for f, _, _ in _MESH_FIELDS])
     _check(L.sevc_load_mesh_host(C.byref(opt), C.byref(mh), None, None, None))
     return arrs
+
+
+def mesh_host_of(arrs):
+    """A MeshHost view of a dict of arrays (keys of get_state)."""
+    nv, nb, ng = len(arrs["px"]), len(arrs["bini"]), len(arrs["gvlen"])
+    return MeshHost(nv, nb, ng, *[np.ascontiguousarray(arrs[f]).ctypes.data for f, _, _ in _MESH_FIELDS])
+
+
+def check_mesh(arrs):
+    """check_data's violation count of a host mesh, counted on the device."""
+    arrs = {f: np.ascontiguousarray(arrs[f], dt) for f, _, dt in _MESH_FIELDS}
+    mh = mesh_host_of(arrs)
+    n = C.c_int()
+    L = lib()
+    L.sevc_check_mesh.argtypes = [C.POINTER(MeshHost), C.POINTER(C.c_int)]
+    _check(L.sevc_check_mesh(C.byref(mh), C.byref(n)))
+    return n.value
+
+
+def check_mesh_host(arrs):
+    """The same count by the host restatement (no GPU)."""
+    arrs = {f: np.ascontiguousarray(arrs[f], dt) for f, _, dt in _MESH_FIELDS}
+    mh = mesh_host_of(arrs)
+    L = lib()
+    L.sevc_host_check.argtypes = [C.POINTER(MeshHost)]
+    return int(L.sevc_host_check(C.byref(mh)))
+
+
+def format_fixed16(x):
+    """The snapshot writer's number text (printf "%.16f")."""
+    buf = C.create_string_buffer(64)
+    L = lib()
+    L.sevc_format_fixed16.argtypes = [C.c_double, C.c_char_p]
+    n = L.sevc_format_fixed16(float(x), buf)
+    return buf.raw[:n].decode()
 
 
 def rng_record(nstreams, ndraws):
@@ -284,6 +320,12 @@ class Engine:
     def check_data(self):
         n = C.c_int()
         _check(lib().sevc_check_data(self._h, C.byref(n)))
+        return n.value
+
+    def check_data_host(self):
+        n = C.c_int()
+        lib().sevc_check_data_host.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        _check(lib().sevc_check_data_host(self._h, C.byref(n)))
         return n.value
 
     def get_state(self):

@@ -148,3 +148,46 @@ def test_synthetic_stream_range():
     o.rng_synthetic(5)
     pos = o.field("rng_pos")
     assert pos.shape == (8192,) and pos.max() == 0
+
+
+def test_fixed16_formatter_matches_printf(engine_mod):
+    """The snapshot number writer equals printf("%.16f") (the C library's
+    and Python's, both correctly rounded) on random doubles of every scale,
+    exact decimal ties, signed zeros, subnormals and large values."""
+    import ctypes
+    import numpy as np
+    libc = ctypes.CDLL(None)
+    buf = ctypes.create_string_buffer(128)
+
+    def c_printf(x):
+        n = libc.snprintf(buf, 128, b"%.16f", ctypes.c_double(x))
+        return buf.raw[:n].decode()
+
+    rng = np.random.default_rng(0)
+    vals = list(rng.uniform(-1, 1, 20000) * 10.0 ** rng.integers(-20, 22, 20000))
+    vals += list(rng.uniform(0, 1000, 5000)) + list(rng.standard_normal(5000) * 1e-8)
+    vals += [0.0, -0.0, 5e-324, -5e-324, 2.0 ** -17, 3 * 2.0 ** -17, 2.0 ** -18, 0.5e-16, 1.5e-16, 2.5e-16,
+             100000.0, 99999.99999999999, 1e21, -1e21, 2.0 ** 72, 9.3e21, 1 / 3, 2 / 3, 0.1, 1e-17, 5e-17,
+             float(np.nextafter(5e-17, 1)), float(np.nextafter(5e-17, 0))]
+    vals += [k * 2.0 ** -20 for k in range(1, 4000, 7)]         # many exact decimal ties
+    for x in vals:
+        got = engine_mod.format_fixed16(x)
+        assert got == c_printf(x) == "%.16f" % x, (x, got, c_printf(x))
+
+
+def test_host_check_counts_planted_faults(engine_mod, tmp_path):
+    """check_data's host restatement: a freshly loaded mesh has no violation,
+    each planted fault is counted."""
+    import numpy as np
+    import meshgen
+    from test_gpu_check import plant
+    mesh = meshgen.make_inputs(200, 3)
+    p = meshgen.write_files(str(tmp_path), mesh)
+    o = engine_mod.default_options(n_grains=200, domain_bound=1.0, vertex_fname=p["vertices"],
+                                   boundary_fname=p["ridges"], orientation_fname=p["oris"], SE_fname=p["se"])
+    st = engine_mod.load_mesh_host(o)
+    assert engine_mod.check_mesh_host(st) == 0
+    rng = np.random.default_rng(0)
+    for kind in ["boundary_off", "dup_boundary_slot", "dup_grain_slot", "self_loop", "short_list", "grain_off",
+                 "vertex_off", "foreign_grain"]:
+        assert engine_mod.check_mesh_host(plant(st, kind, rng)) > 0, kind
