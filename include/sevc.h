@@ -259,6 +259,13 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
  * are always complete.  on = 1 computes them on every step. */
 sevc_status sevc_set_exact_all(sevc_handle *h, int on);
 
+/* The fixed launch sequences of a step (its first half, one polling
+ * iteration, the second half of a step without 2x3 pairs) are captured
+ * into CUDA graphs on first use and replayed (on = 1, the default); on = 0
+ * launches every kernel directly.  Results are identical either way.
+ * Profiling and adjoint replays always launch directly. */
+sevc_status sevc_set_graphs(sevc_handle *h, int on);
+
 /* Per-kernel device time accumulated while profiling is on (CUDA events
  * around each launch on the handle's stream). */
 sevc_status sevc_set_profiling(sevc_handle *h, int on);

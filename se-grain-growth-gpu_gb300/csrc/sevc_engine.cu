@@ -29,6 +29,11 @@ long long sevc_kernel_launches = 0;
 
 struct ProfEntry { double ms = 0; int64_t launches = 0; };
 
+struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;   /* kernels one replay launches */
+};
+
 /* host part of the run state (the device part is the handle's block) */
 struct RunState {
     int n = 0, curr_n_grains = 0;
@@ -78,8 +83,14 @@ struct sevc_handle {
     int *h_big = nullptr;
     size_t h_big_ints = 0;
     int *h_on = nullptr;   /* per instance: nucleation attempt this step */
+    int *h_flags = nullptr;/* host part of the step's output decision (x.flags) */
     size_t dbytes = 0;     /* size of the device block */
     Tape tape;
+    /* CUDA graphs of the step's fixed launch sequences: the first half
+     * without / with a nucleation attempt, one polling iteration, and the
+     * second half of a step without 2x3 pairs */
+    StepGraph g_pre[2], g_poll, g_post;
+    bool use_graphs = true;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool profiling = false;
     std::map<std::string, ProfEntry> prof;
@@ -153,7 +164,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.voff, (I + 1) * 4 }, { (void **)&m.boff, (I + 1) * 4 }, { (void **)&m.goff, (I + 1) * 4 },
         { (void **)&m.binst, B * 4 }, { (void **)&m.ginst, G * 4 }, { (void **)&m.pdone, I * 4 },
         { (void **)&x.pblock, I * h->p.n_blocks * 4 }, { (void **)&x.piters, I * 4 }, { (void **)&x.nrun, 4 },
-        { (void **)&x.segcnt, I * TWO_THREE_PASSES * 4 }, { (void **)&x.nucl_on, I * 4 },
+        { (void **)&x.segcnt, I * TWO_THREE_PASSES * 4 }, { (void **)&x.nucl_on, I * 4 }, { (void **)&x.flags, 16 },
         { (void **)&m.pos, V * 16 }, { (void **)&m.vel, V * 16 }, { (void **)&m.terms, V * 32 },
         { (void **)&m.contrib, V * 48 }, { (void **)&m.venergy, V * 8 }, { (void **)&m.ven, V },
         { (void **)&m.vb, V * 16 }, { (void **)&m.vg, V * 16 }, { (void **)&m.vmod, V * 64 },
@@ -303,7 +314,8 @@ sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handl
     if (!cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream") ||
         !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") ||
         !cuda_ok(cudaMallocHost(&h->h_big, h->h_big_ints * sizeof(int)), "pinned") ||
-        !cuda_ok(cudaMallocHost(&h->h_on, ninst * sizeof(int)), "pinned") || !alloc_device(h) ||
+        !cuda_ok(cudaMallocHost(&h->h_on, ninst * sizeof(int)), "pinned") ||
+        !cuda_ok(cudaMallocHost(&h->h_flags, 4 * sizeof(int)), "pinned") || !alloc_device(h) ||
         !upload(h, hm->m)) {
         sevc_destroy(h);
         return SEVC_ERR_CUDA;
@@ -375,6 +387,108 @@ void tape_free(sevc_handle *h)
     if (tp.rec) cudaFree(tp.rec);
     if (tp.adj) cudaFree(tp.adj);
     tp = Tape();
+}
+
+void drop_graphs(sevc_handle *h)
+{
+    StepGraph *gs[] = { &h->g_pre[0], &h->g_pre[1], &h->g_poll, &h->g_post };
+    for (StepGraph *g : gs) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        *g = StepGraph();
+    }
+}
+
+/* Graphs replay launches with their captured arguments: not while
+ * profiling (events between groups), nor while a tape records events
+ * (the log pointers are arguments). */
+bool graphs_on(const sevc_handle *h)
+{
+    return h->use_graphs && !h->profiling && !h->m.elog && !h->tape.replaying;
+}
+
+/* Run a fixed launch sequence: replay its graph (captured on first use) or
+ * enqueue it directly. */
+template <class F> bool run_seq(sevc_handle *h, StepGraph &g, F &&enqueue)
+{
+    if (!graphs_on(h)) { enqueue(); return true; }
+    if (!g.exec) {
+        long long k0 = sevc_kernel_launches;
+        cudaGraph_t graph = nullptr;
+        if (!cuda_ok(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "capture")) return false;
+        enqueue();
+        if (!cuda_ok(cudaStreamEndCapture(h->stream, &graph), "capture")) return false;
+        bool ok = cuda_ok(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+        cudaGraphDestroy(graph);
+        g.kernels = (int)(sevc_kernel_launches - k0);
+        sevc_kernel_launches = k0;
+        if (!ok) { g = StepGraph(); return false; }
+    }
+    sevc_kernel_launches += g.kernels;
+    return cuda_ok(cudaGraphLaunch(g.exec, h->stream), "graph launch");
+}
+
+/* first half of the step, up to the candidate list (src/main.cu:121-216) */
+void enqueue_pre(sevc_handle *h, bool nucleation)
+{
+    cudaStream_t s = h->stream;
+    const sevc_options &o = h->opt;
+    DevMesh &m = h->m;
+    DevScratch &x = h->x;
+    size_t I = h->ninst;
+    cudaMemsetAsync(m.err, 0, 16, s);
+    cudaMemsetAsync(m.evt, 0, I * EVT_COUNT * sizeof(int), s);
+    cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
+    launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
+    { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :124-130 */
+    if (nucleation) {
+        { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
+        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :171-181 */
+    }
+    { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, s); }                                         /* :127,:203 */
+    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, s); }                                 /* :133,:203 */
+    /* The first count of the 2x3 loop (:228) depends only on the topology,
+     * which nothing changes before that loop: count now, and decide on the
+     * device whether this step must compute every output-only value. */
+    { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
+    launch_full_flag(x, s);
+    { Prof pr(h, "text_label"); launch_mark_force(m, x, s); }
+    { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }                                     /* :206 */
+    { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, s); }                               /* :212-216 */
+    { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
+    cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
+    cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);
+}
+
+void enqueue_poll(sevc_handle *h)
+{
+    Prof pr(h, "polling");
+    launch_poll_iteration(h->m, h->x, h->x.list_a, h->x.n_a, h->p, h->stream);
+}
+
+/* from the 3-sided labels to the end of the step (src/main.cu:252-325) */
+void enqueue_tail(sevc_handle *h)
+{
+    cudaStream_t s = h->stream;
+    const sevc_options &o = h->opt;
+    DevMesh &m = h->m;
+    DevScratch &x = h->x;
+    { Prof pr(h, "label_3sided"); launch_label_3sided(m, o.dt, s); }                              /* :252-255 */
+    { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
+    { Prof pr(h, "remove_grains"); launch_remove_grains(m, x.list_c, x.n_c, s); }                 /* :259 */
+    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
+    { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
+    { Prof pr(h, "unlabel_st2"); launch_unlabel_st2(m, x.list_a, x.n_a, s); }                     /* :282 */
+    { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }                     /* :289 */
+    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :294 */
+    { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                                /* :314 */
+    { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }                                       /* :317-325 */
+}
+
+/* second half of a step without 2x3 pairs: conflicts, then the tail */
+void enqueue_post(sevc_handle *h)
+{
+    { Prof pr(h, "conflicts"); launch_conflicts(h->m, h->x.list_a, h->x.n_a, h->stream); }         /* :222-225 */
+    enqueue_tail(h);
 }
 
 sevc_status err_bits_to_status(int bits)
@@ -529,7 +643,9 @@ void sevc_destroy(sevc_handle *h)
     if (h->h_ctr) cudaFreeHost(h->h_ctr);
     if (h->h_big) cudaFreeHost(h->h_big);
     if (h->h_on) cudaFreeHost(h->h_on);
+    if (h->h_flags) cudaFreeHost(h->h_flags);
     tape_free(h);
+    drop_graphs(h);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (auto e : h->evpool) cudaEventDestroy(e);
@@ -562,12 +678,6 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     loc.t = h->t;
     long long launches0 = sevc_kernel_launches;
     cudaEventRecord(h->ev0, s);
-    cudaMemsetAsync(m.err, 0, 16, s);
-    cudaMemsetAsync(m.evt, 0, (size_t)I * EVT_COUNT * sizeof(int), s);
-    cudaMemsetAsync(x.segcnt, 0, (size_t)I * TWO_THREE_PASSES * sizeof(int), s);
-    launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
-
-    { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :124-130 */
     int n_on = 0;                                                                                  /* :137-141 */
     for (int i = 0; i < I; i++) {
         if (h->icurr[i] <= 5 * h->ng0[i] / 6) h->iallow[i] = 1;
@@ -578,82 +688,69 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         loc.nucleation_attempted = 1;
         if (!cuda_ok(cudaMemcpyAsync(x.nucl_on, h->h_on, I * sizeof(int), cudaMemcpyHostToDevice, s), "upload"))
             return SEVC_ERR_CUDA;
-        { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
-        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :171-181 */
     }
-    { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, s); }                                         /* :127,:203 */
-    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, s); }                                 /* :133,:203 */
-    /* The first count of the 2x3 loop (:228) depends only on the topology,
-     * which nothing changes before that loop: count now, and learn whether
-     * this step can disable boundaries other than 3-sided grains' or export.
-     * Otherwise only 3-sided grains' dA/dt and the extinction times that
-     * matter are computed (see k_text_label).  A batched handle computes
-     * every output on every step. */
-    int c23 = 0, n3 = 0;
-    { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
-    if (!cuda_ok(cudaMemcpyAsync(h->h_ctr, x.n_b, 4, cudaMemcpyDeviceToHost, s), "readback") ||
-        !cuda_ok(cudaMemcpyAsync(h->h_ctr + 1, x.vbucket + VB_COUNT(3), 4, cudaMemcpyDeviceToHost, s), "readback") ||
-        !cuda_ok(cudaStreamSynchronize(s), "sync"))
-        return SEVC_ERR_CUDA;
-    c23 = h->h_ctr[0];
-    n3 = h->h_ctr[1];
+    /* host part of the output decision (k_full_flag): steps that can export,
+     * long steps, exact_all, and every step of a batch */
     int mg = o.min_grains;
-    int full = batch || h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0) || c23 > 0 ||
-               (mg > 0 && h->curr_n_grains + 1 - n3 <= mg);
-    loc.outputs_complete = full;
-    if (!full) { Prof pr(h, "text_label"); launch_mark_force(m, x, n3, s); }
-    { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, full, n3, s); }                           /* :206 */
-    { Prof pr(h, "text_label"); launch_text_label(m, o.dt, full, s); }                            /* :212-216 */
-    { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
+    h->h_flags[1] = batch || h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0);
+    h->h_flags[2] = mg;
+    h->h_flags[3] = h->curr_n_grains;
+    if (!cuda_ok(cudaMemcpyAsync(x.flags + 1, h->h_flags + 1, 3 * sizeof(int), cudaMemcpyHostToDevice, s), "upload"))
+        return SEVC_ERR_CUDA;
+    if (!run_seq(h, h->g_pre[n_on ? 1 : 0], [&] { enqueue_pre(h, n_on > 0); })) return SEVC_ERR_CUDA;
 
-    cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
-    cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);
-    int running = 1, it = 0;
+    /* polling (:219); the first readback also brings the 2x3 count */
+    int running = 1, it = 0, c23 = 0;
     while (running) {
         if (it >= h->polling_cap) { sevc_set_error("polling did not converge"); return SEVC_ERR_NONCONVERGED; }
         it++;
-        { Prof pr(h, "polling"); launch_poll_iteration(m, x, x.list_a, x.n_a, h->p, s); }
-        if (read_ints(h, x.nrun, 1, &running)) return SEVC_ERR_CUDA;
+        if (!run_seq(h, h->g_poll, [&] { enqueue_poll(h); })) return SEVC_ERR_CUDA;
+        if (!cuda_ok(cudaMemcpyAsync(h->h_ctr, x.nrun, 4, cudaMemcpyDeviceToHost, s), "readback") ||
+            (it == 1 && !cuda_ok(cudaMemcpyAsync(h->h_ctr + 1, x.n_b, 4, cudaMemcpyDeviceToHost, s), "readback")) ||
+            !cuda_ok(cudaStreamSynchronize(s), "sync"))
+            return SEVC_ERR_CUDA;
+        running = h->h_ctr[0];
+        if (it == 1) c23 = h->h_ctr[1];
     }
     loc.polling_iters = it;
-    { Prof pr(h, "conflicts"); launch_conflicts(m, x.list_a, x.n_a, s); }                         /* :222-225 */
 
-    for (int k = 0; k < TWO_THREE_PASSES; k++) {                                                   /* :227-250 */
-        int c = c23;
-        if (k > 0) {
-            { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
-            if (read_ints(h, x.n_b, 1, &c)) return SEVC_ERR_CUDA;
+    if (c23 == 0) {                                  /* the usual step: no 2x3 pair */
+        loc.two_three_counts[0] = 0;
+        loc.n_two_three_iters = 1;
+        if (!run_seq(h, h->g_post, [&] { enqueue_post(h); })) return SEVC_ERR_CUDA;
+    } else {
+        { Prof pr(h, "conflicts"); launch_conflicts(m, x.list_a, x.n_a, s); }                     /* :222-225 */
+        for (int k = 0; k < TWO_THREE_PASSES; k++) {                                               /* :227-250 */
+            int c = c23;
+            if (k > 0) {
+                { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
+                if (read_ints(h, x.n_b, 1, &c)) return SEVC_ERR_CUDA;
+            }
+            loc.two_three_counts[k] = c;
+            loc.n_two_three_iters = k + 1;
+            if (c == 0) break;
+            { Prof pr(h, "two_three_remove"); launch_remove_two_three(m, x, x.list_b, x.n_b, k, s); }
+            { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }
         }
-        loc.two_three_counts[k] = c;
-        loc.n_two_three_iters = k + 1;
-        if (c == 0) break;
-        { Prof pr(h, "two_three_remove"); launch_remove_two_three(m, x, x.list_b, x.n_b, k, s); }
-        { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }
+        enqueue_tail(h);
     }
-    { Prof pr(h, "label_3sided"); launch_label_3sided(m, o.dt, s); }                              /* :252-255 */
-    { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
-    { Prof pr(h, "remove_grains"); launch_remove_grains(m, x.list_c, x.n_c, s); }                 /* :259 */
-    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
-    { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
-    { Prof pr(h, "unlabel_st2"); launch_unlabel_st2(m, x.list_a, x.n_a, s); }                     /* :282 */
-    { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }                     /* :289 */
-    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :294 */
-    { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                                /* :314 */
-    { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }                                       /* :317-325 */
     cudaEventRecord(h->ev1, s);
 
     /* one readback: counters, events, error bits, polling iterations and
      * 2x3 counts of every instance */
     int *hb = h->h_big;
     const size_t o_evt = (size_t)I * CTR_COUNT, o_err = o_evt + (size_t)I * EVT_COUNT, o_pit = o_err + 4,
-                 o_seg = o_pit + I;
+                 o_seg = o_pit + I, o_full = o_seg + (size_t)I * TWO_THREE_PASSES;
     auto get = [&](int *dst, const int *src, size_t n) {
         return cuda_ok(cudaMemcpyAsync(dst, src, n * sizeof(int), cudaMemcpyDeviceToHost, s), "readback");
     };
     if (!get(hb, x.counters, (size_t)I * CTR_COUNT) || !get(hb + o_evt, m.evt, (size_t)I * EVT_COUNT) ||
         !get(hb + o_err, m.err, 4) || !get(hb + o_pit, x.piters, I) ||
-        !get(hb + o_seg, x.segcnt, (size_t)I * TWO_THREE_PASSES) || !cuda_ok(cudaStreamSynchronize(s), "readback sync"))
+        !get(hb + o_seg, x.segcnt, (size_t)I * TWO_THREE_PASSES) || !get(hb + o_full, x.flags, 1) ||
+        !cuda_ok(cudaStreamSynchronize(s), "readback sync"))
         return SEVC_ERR_CUDA;
+    const int full = hb[o_full] != 0;
+    loc.outputs_complete = full;
     float ms = 0;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     if (h->profiling) prof_collect(h);
@@ -911,6 +1008,7 @@ sevc_status sevc_set_mobility(sevc_handle *h, double mu)
 {
     if (!h || !(mu > 0) || h->tape.every > 0) return SEVC_ERR_ARG;
     h->p.mu = mu;
+    drop_graphs(h);              /* mu is a captured kernel argument */
     return SEVC_OK;
 }
 
@@ -919,6 +1017,15 @@ sevc_status sevc_set_gb_scaling(sevc_handle *h, double s)
     if (!h || h->tape.every > 0) return SEVC_ERR_ARG;
     h->opt.GB_scaling = s;
     h->p.scaling = s;
+    drop_graphs(h);
+    return SEVC_OK;
+}
+
+sevc_status sevc_set_graphs(sevc_handle *h, int on)
+{
+    if (!h) return SEVC_ERR_ARG;
+    h->use_graphs = on != 0;
+    if (!on) drop_graphs(h);
     return SEVC_OK;
 }
 
@@ -1142,6 +1249,7 @@ sevc_status sevc_checkpoint_load(sevc_handle *h, const char *path)
         return SEVC_ERR_CUDA;
     h->n = hd.n; h->curr_n_grains = hd.curr_n_grains; h->t = hd.t; h->nucleated_area = hd.nucleated_area;
     h->p.mu = hd.mu; h->opt.GB_scaling = hd.gb_scaling; h->p.scaling = hd.gb_scaling;
+    drop_graphs(h);
     h->icurr = icurr; h->iallow = iallow; h->iarea = iarea;
     return SEVC_OK;
 }

@@ -287,22 +287,33 @@ __global__ void k_vlen_offsets(int *cnt, int *cursor, int *total)
     }
 }
 
-/* dA/dt of the 3-sided grains only (bucket 3 of the side-count order) */
-__global__ void k_grain_dadt_bucket(DevMesh m, const int *perm, const int *vbucket);
+/* The step computes every output-only value (extinction times of all
+ * boundaries, dA/dt of all grains) when it can export, has 2x3 pairs, is
+ * near the stop threshold, or is asked to (flags[1], set by the host);
+ * else only those a step can observe.  flags[0] = the decision, taken on
+ * the device from the 2x3 count and the 3-sided bucket so that no host
+ * round trip separates the step's first half from its second. */
+__global__ void k_full_flag(const int *n_two_three, const int *vbucket, int *flags)
+{
+    int mg = flags[2], curr = flags[3], n3 = vbucket[3 * NBUCKET + 3];
+    flags[0] = flags[1] || *n_two_three > 0 || (mg > 0 && curr + 1 - n3 <= mg);
+}
 
 /* boundaries of the vertices of 3-sided grains must get exact extinction
  * times: they are the only ones a step without 2x3 pairs can disable */
-__global__ void k_mark_force(DevMesh m, const int *perm, const int *vbucket)
+__global__ void k_mark_force(DevMesh m, const int *perm, const int *vbucket, const int *flags)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= vbucket[3 * NBUCKET + 3]) return;
-    int g = perm[vbucket[2 * NBUCKET + 3] + i];
-    const int *L = m.glist + (size_t)SEVC_MAXV * g;
-    for (int k = 0; k < 3; k++) {
-        int4 s = m.vb[L[k]];
-        m.bforce[s.x] = 1;
-        m.bforce[s.y] = 1;
-        m.bforce[s.z] = 1;
+    if (flags[0]) return;
+    int n3 = vbucket[3 * NBUCKET + 3], start = vbucket[2 * NBUCKET + 3];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        int g = perm[start + i];
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        for (int k = 0; k < 3; k++) {
+            int4 s = m.vb[L[k]];
+            m.bforce[s.x] = 1;
+            m.bforce[s.y] = 1;
+            m.bforce[s.z] = 1;
+        }
     }
 }
 __global__ void k_vlen_scatter(DevMesh m, int *cursor, int *perm)
@@ -396,18 +407,16 @@ __global__ void k_vertex_fd(DevMesh m, double mu)
  * src/geometry.h:779-787 streamed over the list */
 __device__ void dadt_of(const DevMesh &m, int g);
 
-__global__ void k_grain_dadt(DevMesh m)
-{
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= m.ng || !m.gen[g]) return;
-    dadt_of(m, g);
-}
-
-__global__ void k_grain_dadt_bucket(DevMesh m, const int *perm, const int *vbucket)
+/* every enabled grain when flags[0], else the 3-sided ones (bucket 3 of
+ * the side-count order) */
+__global__ void k_grain_dadt(DevMesh m, const int *perm, const int *vbucket, const int *flags)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= vbucket[3 * NBUCKET + 3]) return;
-    dadt_of(m, perm[vbucket[2 * NBUCKET + 3] + i]);
+    if (flags[0]) {
+        if (i < m.ng && m.gen[i]) dadt_of(m, i);
+    } else if (i < vbucket[3 * NBUCKET + 3]) {
+        dadt_of(m, perm[vbucket[2 * NBUCKET + 3] + i]);
+    }
 }
 
 __device__ void dadt_of(const DevMesh &m, int g)
@@ -449,13 +458,13 @@ __device__ void dadt_of(const DevMesh &m, int g)
  *   margin = 1e-12 |d|^2/dt + 1e-14 (|dx|+|dy|)(|Px|+|Py|) + 1e-15 (|dx Px| + |dy Py|)
  * (each term at least five times the error it covers) it is not one.
  */
-__global__ void k_text_label(DevMesh m, double dt, double inv_dt, int full)
+__global__ void k_text_label(DevMesh m, double dt, double inv_dt, const int *flags)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= m.nb) return;
     double text = m.btext[b];
     if (m.ben[b]) {
-        bool exact = full || m.bforce[b];
+        bool exact = flags[0] || m.bforce[b];
         if (m.bforce[b]) m.bforce[b] = 0;
         int2 e = m.bv[b];
         double2 pi = m.pos[e.x], pe = m.pos[e.y];
@@ -618,18 +627,22 @@ void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m, mu);
 }
-void launch_grain_dadt(const DevMesh &m, const DevScratch &x, int full, int n3, cudaStream_t s)
+void launch_full_flag(const DevScratch &x, cudaStream_t s)
 {
-    if (full) COUNT_LAUNCHES(1), k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m);
-    else if (n3 > 0) COUNT_LAUNCHES(1), k_grain_dadt_bucket<<<nblk(n3), TPB, 0, s>>>(m, x.perm, x.vbucket);
+    COUNT_LAUNCHES(1), k_full_flag<<<1, 1, 0, s>>>(x.n_b, x.vbucket, x.flags);
 }
-void launch_mark_force(const DevMesh &m, const DevScratch &x, int n3, cudaStream_t s)
+void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    if (n3 > 0) COUNT_LAUNCHES(1), k_mark_force<<<nblk(n3), TPB, 0, s>>>(m, x.perm, x.vbucket);
+    COUNT_LAUNCHES(1), k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m, x.perm, x.vbucket, x.flags);
 }
-void launch_text_label(const DevMesh &m, double dt, int full, cudaStream_t s)
+void launch_mark_force(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt, 1.0 / dt, full);
+    int g = nblk(m.ng);
+    COUNT_LAUNCHES(1), k_mark_force<<<g < 152 ? g : 152, TPB, 0, s>>>(m, x.perm, x.vbucket, x.flags);
+}
+void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt, 1.0 / dt, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)

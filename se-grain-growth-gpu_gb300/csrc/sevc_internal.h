@@ -28,6 +28,7 @@ struct DevScratch {
     int *nucl_buf;                   /* 64 ints per instance: per-block pick and alive count */
     int *nucl_on;                    /* per instance: attempt a nucleation this step */
     int *vbucket;                    /* 64 ints: side-count histogram + cursors */
+    int *flags;                      /* 4 ints: the step's output decision, see launch_full_flag */
     int *perm, *n_perm;              /* enabled grains ordered by side count */
 };
 constexpr int EXTRA_CAP = 1024;
@@ -62,9 +63,12 @@ void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s);
 /* side-count histogram layout in DevScratch::vbucket */
 #define VB_START(b) (32 + (b))
 #define VB_COUNT(b) (48 + (b))
-void launch_grain_dadt(const DevMesh &m, const DevScratch &x, int full, int n3, cudaStream_t s);
-void launch_mark_force(const DevMesh &m, const DevScratch &x, int n3, cudaStream_t s);
-void launch_text_label(const DevMesh &m, double dt, int full, cudaStream_t s);
+/* x.flags: [0] computed "full" decision, [1] host part of it, [2]
+ * min_grains, [3] current grain count (see k_full_flag) */
+void launch_full_flag(const DevScratch &x, cudaStream_t s);
+void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s);
+void launch_mark_force(const DevMesh &m, const DevScratch &x, cudaStream_t s);
+void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s);
 void launch_grain_area(const DevMesh &m, cudaStream_t s);
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s);

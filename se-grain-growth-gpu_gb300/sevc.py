@@ -25,7 +25,7 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_export_instance_text", "sevc_set_mobility", "sevc_set_gb_scaling", "sevc_set_stored_energy",
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
            "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
-           "sevc_check_data_host", "sevc_check_mesh"]
+           "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs"]
 
 
 class SevcError(RuntimeError):
@@ -395,6 +395,10 @@ class Engine:
     def set_exact_all(self, on):
         lib().sevc_set_exact_all.argtypes = [C.c_void_p, C.c_int]
         _check(lib().sevc_set_exact_all(self._h, 1 if on else 0))
+
+    def set_graphs(self, on):
+        lib().sevc_set_graphs.argtypes = [C.c_void_p, C.c_int]
+        _check(lib().sevc_set_graphs(self._h, 1 if on else 0))
 
     def set_profiling(self, on):
         _check(lib().sevc_set_profiling(self._h, 1 if on else 0))
