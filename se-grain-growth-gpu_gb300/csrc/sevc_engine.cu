@@ -165,6 +165,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.binst, B * 4 }, { (void **)&m.ginst, G * 4 }, { (void **)&m.pdone, I * 4 },
         { (void **)&x.pblock, I * h->p.n_blocks * 4 }, { (void **)&x.piters, I * 4 }, { (void **)&x.nrun, 4 },
         { (void **)&x.segcnt, I * TWO_THREE_PASSES * 4 }, { (void **)&x.nucl_on, I * 4 }, { (void **)&x.flags, 16 },
+        { (void **)&x.summary, h->h_big_ints * 4 },
         { (void **)&m.pos, V * 16 }, { (void **)&m.vel, V * 16 }, { (void **)&m.terms, V * 32 },
         { (void **)&m.contrib, V * 48 }, { (void **)&m.venergy, V * 8 }, { (void **)&m.ven, V },
         { (void **)&m.vb, V * 16 }, { (void **)&m.vg, V * 16 }, { (void **)&m.vmod, V * 64 },
@@ -482,6 +483,7 @@ void enqueue_tail(sevc_handle *h)
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :294 */
     { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                                /* :314 */
     { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }                                       /* :317-325 */
+    launch_pack_summary(m, x, h->ninst, x.summary, s);
 }
 
 /* second half of a step without 2x3 pairs: conflicts, then the tail */
@@ -741,12 +743,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     int *hb = h->h_big;
     const size_t o_evt = (size_t)I * CTR_COUNT, o_err = o_evt + (size_t)I * EVT_COUNT, o_pit = o_err + 4,
                  o_seg = o_pit + I, o_full = o_seg + (size_t)I * TWO_THREE_PASSES;
-    auto get = [&](int *dst, const int *src, size_t n) {
-        return cuda_ok(cudaMemcpyAsync(dst, src, n * sizeof(int), cudaMemcpyDeviceToHost, s), "readback");
-    };
-    if (!get(hb, x.counters, (size_t)I * CTR_COUNT) || !get(hb + o_evt, m.evt, (size_t)I * EVT_COUNT) ||
-        !get(hb + o_err, m.err, 4) || !get(hb + o_pit, x.piters, I) ||
-        !get(hb + o_seg, x.segcnt, (size_t)I * TWO_THREE_PASSES) || !get(hb + o_full, x.flags, 1) ||
+    if (!cuda_ok(cudaMemcpyAsync(hb, x.summary, (o_full + 1) * sizeof(int), cudaMemcpyDeviceToHost, s), "readback") ||
         !cuda_ok(cudaStreamSynchronize(s), "readback sync"))
         return SEVC_ERR_CUDA;
     const int full = hb[o_full] != 0;

@@ -528,6 +528,27 @@ __global__ void k_area_dirty(DevMesh m, int compute)
     }
 }
 __global__ void k_reset_count(int *c) { *c = 0; }
+
+/* the step's summary in one buffer, for one readback: counters, events,
+ * error bits, polling iterations, 2x3 pass counts (all per instance) and
+ * the output decision */
+__global__ void k_pack_summary(DevMesh m, DevScratch x, int ninst, int *out)
+{
+    size_t nc = (size_t)ninst * CTR_COUNT, ne = (size_t)ninst * EVT_COUNT, np = ninst,
+           ns = (size_t)ninst * TWO_THREE_PASSES;
+    size_t total = nc + ne + 4 + np + ns + 1;
+    for (size_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        size_t k = i;
+        int v;
+        if (k < nc) v = x.counters[k];
+        else if ((k -= nc) < ne) v = m.evt[k];
+        else if ((k -= ne) < 4) v = m.err[k];
+        else if ((k -= 4) < np) v = x.piters[k];
+        else if ((k -= np) < ns) v = x.segcnt[k];
+        else v = x.flags[0];
+        out[i] = v;
+    }
+}
 __global__ void k_reset_ngrains(int *counters, int ninst)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -651,6 +672,13 @@ void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
     COUNT_LAUNCHES(1), k_reset_count<<<1, 1, 0, s>>>(m.nadirty);
 }
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { COUNT_LAUNCHES(1), k_update<<<nblk(m.nv), TPB, 0, s>>>(m, dt); }
+
+void launch_pack_summary(const DevMesh &m, const DevScratch &x, int ninst, int *out, cudaStream_t s)
+{
+    size_t total = (size_t)ninst * (CTR_COUNT + EVT_COUNT + 1 + TWO_THREE_PASSES) + 5;
+    int g = (int)((total + TPB - 1) / TPB);
+    COUNT_LAUNCHES(1), k_pack_summary<<<g < 152 ? g : 152, TPB, 0, s>>>(m, x, ninst, out);
+}
 
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)
 {

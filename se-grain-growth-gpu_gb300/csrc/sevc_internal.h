@@ -29,6 +29,7 @@ struct DevScratch {
     int *nucl_on;                    /* per instance: attempt a nucleation this step */
     int *vbucket;                    /* 64 ints: side-count histogram + cursors */
     int *flags;                      /* 4 ints: the step's output decision, see launch_full_flag */
+    int *summary;                    /* the step's summary packed for one readback */
     int *perm, *n_perm;              /* enabled grains ordered by side count */
 };
 constexpr int EXTRA_CAP = 1024;
@@ -73,6 +74,8 @@ void launch_grain_area(const DevMesh &m, cudaStream_t s);
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s);
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s);
+/* counters | events | error bits | polling iterations | 2x3 counts | output decision, into out */
+void launch_pack_summary(const DevMesh &m, const DevScratch &x, int ninst, int *out, cudaStream_t s);
 
 /* topology (sevc_topology.cu) */
 enum CompactKind { CK_CAND = 0, CK_TWO_THREE = 1, CK_GRAIN_CAND = 2, CK_GVLEN3 = 3 };

@@ -653,31 +653,24 @@ __global__ void k_flips(DevMesh m, double eps, const int *list, const int *n)
 /* ------------------------------------------------------------------ */
 /* fix_grain_lists, src/topological.h:1035-1227                        */
 /* ------------------------------------------------------------------ */
-__global__ void k_fix_add(DevMesh m)
+/* perform_ADD_ops, perform_REMOVE_ops, perform_REPLACE_ops
+ * (src/topological.h:1035-1148) for one queued grain.  The reference runs
+ * each over all grains before the next; an edit only touches its own
+ * grain's list and only reads the mods, which nothing writes meanwhile, so
+ * running the three for one grain back to back gives the same lists. */
+__device__ void fix_grain(const DevMesh &m, int g)
 {
-    int nf = *m.nfix;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
-        int g = m.fixlist[w];
-        if (!(m.gen[g] && m.gfix[g])) continue;
-        const int *L = m.glist + (size_t)SEVC_MAXV * g;
-        for (int i = 0; i < m.gvlen[g]; i++) {
-            int v = L[i];
-            for (int j = 0; j < 4; j++) {
-                int4 md = m.vmod[4 * (size_t)v + j];
-                if (md.w == FIX_ADD && md.x == g) glist_add_after(m, g, md.y, md.z);
-            }
+    int *L = m.glist + (size_t)SEVC_MAXV * g;
+    for (int i = 0; i < m.gvlen[g]; i++) {               /* ADD */
+        int v = L[i];
+        for (int j = 0; j < 4; j++) {
+            int4 md = m.vmod[4 * (size_t)v + j];
+            if (md.w == FIX_ADD && md.x == g) glist_add_after(m, g, md.y, md.z);
         }
     }
-}
-__global__ void k_fix_remove(DevMesh m)
-{
-    int nf = *m.nfix;
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
-        int g = m.fixlist[w];
-        if (!(m.gen[g] && m.gfix[g])) continue;
+    {                                                    /* REMOVE */
         int snap[SEVC_MAXV];   /* the list as it was when the mod buffer was filled (:1088-1097) */
         int n0 = m.gvlen[g];
-        const int *L = m.glist + (size_t)SEVC_MAXV * g;
         for (int i = 0; i < n0; i++) snap[i] = L[i];
         for (int i = 0; i < n0; i++)
             for (int j = 0; j < 4; j++) {
@@ -685,21 +678,20 @@ __global__ void k_fix_remove(DevMesh m)
                 if (md.w == FIX_REMOVE && md.x == g) glist_remove(m, g, md.y);
             }
     }
+    for (int i = 0; i < m.gvlen[g]; i++) {               /* REPLACE */
+        int v = L[i];
+        for (int j = 0; j < 4; j++) {
+            int4 md = m.vmod[4 * (size_t)v + j];
+            if (md.w == FIX_REPLACE && md.x == g) glist_replace(m, g, md.z, md.y);
+        }
+    }
 }
-__global__ void k_fix_replace(DevMesh m)
+__global__ void k_fix_edit(DevMesh m)
 {
     int nf = *m.nfix;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
         int g = m.fixlist[w];
-        if (!(m.gen[g] && m.gfix[g])) continue;
-        const int *L = m.glist + (size_t)SEVC_MAXV * g;
-        for (int i = 0; i < m.gvlen[g]; i++) {
-            int v = L[i];
-            for (int j = 0; j < 4; j++) {
-                int4 md = m.vmod[4 * (size_t)v + j];
-                if (md.w == FIX_REPLACE && md.x == g) glist_replace(m, g, md.z, md.y);
-            }
-        }
+        if (m.gen[g] && m.gfix[g]) fix_grain(m, g);
     }
 }
 /* clear_grains_fix_state (:1150-1163): fix = false for enabled grains and
@@ -825,9 +817,7 @@ void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncan
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_fix_add<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    COUNT_LAUNCHES(1), k_fix_remove<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    COUNT_LAUNCHES(1), k_fix_replace<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    COUNT_LAUNCHES(1), k_fix_edit<<<WL_BLOCKS, TPB, 0, s>>>(m);
     COUNT_LAUNCHES(1), k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
     COUNT_LAUNCHES(1), k_fix_reset<<<1, 1, 0, s>>>(m);
 }
