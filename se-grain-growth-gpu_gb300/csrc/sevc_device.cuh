@@ -74,10 +74,10 @@ struct DevMesh {
     int *binst, *ginst;  /* instance of every boundary / grain */
     int *pdone;          /* per instance: polling has converged this step */
     /* position-moving events of the step in application order, recorded
-     * only while an adjoint tape replays a segment (elog == nullptr else) */
-    struct EventRec *elog;
-    int *nelog;
-    int elog_cap;
+     * only while an adjoint tape replays a segment (elog->buf == nullptr
+     * else); the control block lives in device memory so that captured
+     * launches stay valid whether or not events are recorded */
+    struct EventLog *elog;
     /* grains whose list changed since the step's grain pass (their area is
      * recomputed after removals, src/main.cu:266) */
     int *adirty, *nadirty;
@@ -85,8 +85,15 @@ struct DevMesh {
     /* slots that ever held a nucleated grain, ascending; instance i's
      * entries start at nlist[goff[i]], nnlist[i] of them */
     int *nlist, *nnlist;
-    /* boundaries whose extinction time must be exact this step */
-    uint8_t *bforce;
+    /* Output-only values (extinction time, dA/dt) are computed exactly for
+     * every entity only on steps that can export; on other steps the values
+     * of entities an event disables are computed at that moment from the
+     * positions, velocities and boundary ends the step started its events
+     * with (pos0, vel0, bv0, copied after the labels).  bexact / gexact say
+     * which values are already exact this step. */
+    double2 *pos0, *vel0;
+    int2 *bv0;
+    uint8_t *bexact, *gexact;
 };
 
 enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
@@ -100,15 +107,22 @@ struct EventRec {
     double2 pa, pb, pc;
 };
 
+struct EventLog {
+    EventRec *buf;   /* nullptr: not recording */
+    int *n;
+    int cap;
+};
+
 __device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int b, int c, double2 pa, double2 pb,
                                           double2 pc)
 {
-    if (!m.elog) return;
-    int i = atomicAdd(m.nelog, 1);
-    if (i >= m.elog_cap) { atomicOr(m.err, ERRB_WORKLIST); return; }
+    EventLog L = *m.elog;
+    if (!L.buf) return;
+    int i = atomicAdd(L.n, 1);
+    if (i >= L.cap) { atomicOr(m.err, ERRB_WORKLIST); return; }
     EventRec r;
     r.type = type; r.a = a; r.b = b; r.c = c; r.pa = pa; r.pb = pb; r.pc = pc;
-    m.elog[i] = r;
+    L.buf[i] = r;
 }
 
 /* ---- periodic geometry, src/geometry.h:133-331 ----
@@ -237,6 +251,67 @@ __device__ __forceinline__ void set_slot3(int4 &s, int i, int v)
 __device__ __forceinline__ int other_end(int2 e, int v) { return e.x == v ? e.y : e.x; }
 
 __device__ __forceinline__ void raise_err(const DevMesh &m, int bits) { atomicOr(m.err, bits); }
+
+/* compute_t_ext for one boundary (src/topological.h:303-334): ends at
+ * pi, pe with velocities vi, ve */
+__device__ __forceinline__ double text_exact(double2 pi, double2 pe, double2 vi, double2 ve, double D)
+{
+    double dx = 0.0 + wrapd(pe.x, pi.x, D);   /* adjust_origin_for_points on 2 points */
+    double dy = 0.0 + wrapd(pe.y, pi.y, D);
+    dx = dx - 0.0;
+    dy = dy - 0.0;
+    double norm = vmag(dx, dy);
+    double tx = 0, ty = 0;
+    if (norm != 0) {                          /* vector2_unitary, src/geometry.h:274 */
+        double ang = atan2(dy, dx);
+        tx = cos(ang);
+        ty = sin(ang);
+    }
+    double aux = tx * (ve.x - vi.x) + ty * (ve.y - vi.y);
+    return (aux == 0) ? 100 : -norm / aux;
+}
+
+/* compute_dAdt (src/geometry.h:779-787) of grain g over its list, with the
+ * given positions and velocities */
+__device__ __forceinline__ double dadt_from(const DevMesh &m, int g, const double2 *pos, const double2 *vel)
+{
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int n = m.gvlen[g];
+    double d = 0;
+    if (n > 0) {
+        double2 r0 = pos[L[0]], v0 = vel[L[0]];
+        double ax = 0, ay = 0, rx = r0.x, ry = r0.y, vxk = v0.x, vyk = v0.y;
+        for (int k = 1; k < n; k++) {
+            double2 r = pos[L[k]], w = vel[L[k]];
+            double nx = ax + wrapd(r.x, rx, m.D);
+            double ny = ay + wrapd(r.y, ry, m.D);
+            d += (vxk * ny + ax * w.y);
+            d -= (vyk * nx + ay * w.x);
+            ax = nx; ay = ny; rx = r.x; ry = r.y; vxk = w.x; vyk = w.y;
+        }
+        d += (vxk * 0.0 + ax * v0.y);
+        d -= (vyk * 0.0 + ay * v0.x);
+    }
+    return d;
+}
+
+/* an event is about to disable boundary b: make its extinction time the
+ * value the step's labels would have computed */
+__device__ __forceinline__ void finalize_boundary(const DevMesh &m, int b)
+{
+    if (m.bexact[b]) return;
+    int2 e = m.bv0[b];
+    m.btext[b] = text_exact(m.pos0[e.x], m.pos0[e.y], m.vel0[e.x], m.vel0[e.y], m.D);
+    m.bexact[b] = 1;
+}
+/* an event is about to edit grain g's list (or disable it): its dA/dt as
+ * the step computed it before any event */
+__device__ __forceinline__ void finalize_grain(const DevMesh &m, int g)
+{
+    if (m.gexact[g]) return;
+    m.gdadt[g] = dadt_from(m, g, m.pos0, m.vel0);
+    m.gexact[g] = 1;
+}
 
 /* first position of an ascending list whose value is >= x */
 __device__ __forceinline__ int lower_bound_i(const int *a, int n, int x)

@@ -165,7 +165,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.binst, B * 4 }, { (void **)&m.ginst, G * 4 }, { (void **)&m.pdone, I * 4 },
         { (void **)&x.pblock, I * h->p.n_blocks * 4 }, { (void **)&x.piters, I * 4 }, { (void **)&x.nrun, 4 },
         { (void **)&x.segcnt, I * TWO_THREE_PASSES * 4 }, { (void **)&x.nucl_on, I * 4 }, { (void **)&x.flags, 16 },
-        { (void **)&x.summary, h->h_big_ints * 4 },
+        { (void **)&x.summary, h->h_big_ints * 4 }, { (void **)&m.elog, sizeof(EventLog) },
         { (void **)&m.pos, V * 16 }, { (void **)&m.vel, V * 16 }, { (void **)&m.terms, V * 32 },
         { (void **)&m.contrib, V * 48 }, { (void **)&m.venergy, V * 8 }, { (void **)&m.ven, V },
         { (void **)&m.vb, V * 16 }, { (void **)&m.vg, V * 16 }, { (void **)&m.vmod, V * 64 },
@@ -185,7 +185,8 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.rng, nrng * sizeof(curandState) }, { (void **)&x.rng_saved, nrng * sizeof(curandState) },
         { (void **)&x.nucl_buf, I * 64 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
         { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
-        { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.bforce, B },
+        { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
+        { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -404,7 +405,7 @@ void drop_graphs(sevc_handle *h)
  * (the log pointers are arguments). */
 bool graphs_on(const sevc_handle *h)
 {
-    return h->use_graphs && !h->profiling && !h->m.elog && !h->tape.replaying;
+    return h->use_graphs && !h->profiling;
 }
 
 /* Run a fixed launch sequence: replay its graph (captured on first use) or
@@ -439,6 +440,7 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     cudaMemsetAsync(m.err, 0, 16, s);
     cudaMemsetAsync(m.evt, 0, I * EVT_COUNT * sizeof(int), s);
     cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
+    cudaMemsetAsync(m.gexact, 0, (size_t)h->ng, s);
     launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
     { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :124-130 */
     if (nucleation) {
@@ -452,9 +454,9 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
      * device whether this step must compute every output-only value. */
     { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
     launch_full_flag(x, s);
-    { Prof pr(h, "text_label"); launch_mark_force(m, x, s); }
     { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }                                     /* :206 */
     { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, s); }                               /* :212-216 */
+    { Prof pr(h, "snapshot"); launch_snapshot(m, x, s); }
     { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
     cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
     cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);
@@ -1141,13 +1143,14 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
                       d2d(rec(k, off_gen), m.gen, G) &&
                       cuda_ok(cudaMemsetAsync(rec(k, off_nlog), 0, 4, s), "memset");
             if (!ok) { st = SEVC_ERR_CUDA; break; }
-            m.elog = (EventRec *)rec(k, off_log);
-            m.nelog = (int *)rec(k, off_nlog);
-            m.elog_cap = tp.log_cap;
+            EventLog on = { (EventRec *)rec(k, off_log), (int *)rec(k, off_nlog), tp.log_cap }, off = { nullptr, nullptr, 0 };
+            if (!cuda_ok(cudaMemcpyAsync(m.elog, &on, sizeof on, cudaMemcpyHostToDevice, s), "upload")) {
+                st = SEVC_ERR_CUDA;
+                break;
+            }
             st = sevc_step(h, nullptr);
-            m.elog = nullptr;
-            m.nelog = nullptr;
-            m.elog_cap = 0;
+            if (!cuda_ok(cudaMemcpyAsync(m.elog, &off, sizeof off, cudaMemcpyHostToDevice, s), "upload"))
+                st = SEVC_ERR_CUDA;
             if (!st && !(d2d(rec(k, off_vel1), m.vel, V * 16) && d2d(rec(k, off_ven1), m.ven, V))) st = SEVC_ERR_CUDA;
         }
         for (int k = K - 1; k >= 0 && !st; k--) {

@@ -288,33 +288,18 @@ __global__ void k_vlen_offsets(int *cnt, int *cursor, int *total)
 }
 
 /* The step computes every output-only value (extinction times of all
- * boundaries, dA/dt of all grains) when it can export, has 2x3 pairs, is
- * near the stop threshold, or is asked to (flags[1], set by the host);
- * else only those a step can observe.  flags[0] = the decision, taken on
- * the device from the 2x3 count and the 3-sided bucket so that no host
- * round trip separates the step's first half from its second. */
+ * boundaries, dA/dt of all grains) when it can export or is asked to
+ * (flags[1], set by the host), or when it could end at the stop threshold
+ * (a final export): every removal takes a 3-sided grain, and a pass of the
+ * 2x3 loop can make at most two per pair; the bound is generous, as the
+ * threshold is crossed once per run.  Else only what the step can observe
+ * is computed.  flags[0] = the decision, taken on the device so that no
+ * host round trip separates the step's first half from its second. */
 __global__ void k_full_flag(const int *n_two_three, const int *vbucket, int *flags)
 {
     int mg = flags[2], curr = flags[3], n3 = vbucket[3 * NBUCKET + 3];
-    flags[0] = flags[1] || *n_two_three > 0 || (mg > 0 && curr + 1 - n3 <= mg);
-}
-
-/* boundaries of the vertices of 3-sided grains must get exact extinction
- * times: they are the only ones a step without 2x3 pairs can disable */
-__global__ void k_mark_force(DevMesh m, const int *perm, const int *vbucket, const int *flags)
-{
-    if (flags[0]) return;
-    int n3 = vbucket[3 * NBUCKET + 3], start = vbucket[2 * NBUCKET + 3];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
-        int g = perm[start + i];
-        const int *L = m.glist + (size_t)SEVC_MAXV * g;
-        for (int k = 0; k < 3; k++) {
-            int4 s = m.vb[L[k]];
-            m.bforce[s.x] = 1;
-            m.bforce[s.y] = 1;
-            m.bforce[s.z] = 1;
-        }
-    }
+    long long reach = (long long)curr - n3 - 40LL * *n_two_three - 64;
+    flags[0] = flags[1] || (mg > 0 && reach <= mg);
 }
 __global__ void k_vlen_scatter(DevMesh m, int *cursor, int *perm)
 {
@@ -411,43 +396,31 @@ __device__ void dadt_of(const DevMesh &m, int g);
  * the side-count order) */
 __global__ void k_grain_dadt(DevMesh m, const int *perm, const int *vbucket, const int *flags)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int stride = gridDim.x * blockDim.x;
     if (flags[0]) {
-        if (i < m.ng && m.gen[i]) dadt_of(m, i);
-    } else if (i < vbucket[3 * NBUCKET + 3]) {
-        dadt_of(m, perm[vbucket[2 * NBUCKET + 3] + i]);
+        for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.ng; g += stride)
+            if (m.gen[g]) dadt_of(m, g);
+    } else {
+        int n3 = vbucket[3 * NBUCKET + 3], start = vbucket[2 * NBUCKET + 3];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += stride) dadt_of(m, perm[start + i]);
     }
 }
 
 __device__ void dadt_of(const DevMesh &m, int g)
 {
-    const int *L = m.glist + (size_t)SEVC_MAXV * g;
-    int n = m.gvlen[g];
-    double d = 0;
-    if (n > 0) {
-        double2 r0 = m.pos[L[0]], v0 = m.vel[L[0]];
-        double ax = 0, ay = 0, rx = r0.x, ry = r0.y, vxk = v0.x, vyk = v0.y;
-        for (int k = 1; k < n; k++) {
-            double2 r = m.pos[L[k]], w = m.vel[L[k]];
-            double nx = ax + wrapd(r.x, rx, m.D);
-            double ny = ay + wrapd(r.y, ry, m.D);
-            d += (vxk * ny + ax * w.y);
-            d -= (vyk * nx + ay * w.x);
-            ax = nx; ay = ny; rx = r.x; ry = r.y; vxk = w.x; vyk = w.y;
-        }
-        d += (vxk * 0.0 + ax * v0.y);
-        d -= (vyk * 0.0 + ay * v0.x);
-    }
-    m.gdadt[g] = d;
+    m.gdadt[g] = dadt_from(m, g, m.pos, m.vel);
+    m.gexact[g] = 1;
 }
 
 /* compute_t_ext (src/topological.h:303-334) then label_boundaries
  * (:343-353), which runs on every slot including disabled ones */
 /*
- * When `full` is 0 a boundary that provably is not a candidate skips the
- * transcendental evaluation and keeps its previous t_ext (the value is not
- * observed: exports happen only on steps run with `full`, and every
- * boundary a step can disable gets an exact value through `bforce`).
+ * When flags[0] is 0 a boundary that provably is not a candidate skips
+ * the transcendental evaluation and gets a t_ext outside [0, dt], so the
+ * labels (this kernel's and label_3sided's) see what they would see; the
+ * value itself is not observed: exports happen only on steps that compute
+ * every value, and a boundary an event disables gets its exact value then
+ * (finalize_boundary).
  *
  * Certificate.  With d the unwrapped edge vector, P = v_end - v_ini and
  * s = d.P, the reference's denominator is aux = T.P with T = (cos, sin) of
@@ -464,16 +437,12 @@ __global__ void k_text_label(DevMesh m, double dt, double inv_dt, const int *fla
     if (b >= m.nb) return;
     double text = m.btext[b];
     if (m.ben[b]) {
-        bool exact = flags[0] || m.bforce[b];
-        if (m.bforce[b]) m.bforce[b] = 0;
         int2 e = m.bv[b];
         double2 pi = m.pos[e.x], pe = m.pos[e.y];
-        double dx = 0.0 + wrapd(pe.x, pi.x, m.D);  /* adjust_origin_for_points on 2 points */
-        double dy = 0.0 + wrapd(pe.y, pi.y, m.D);
-        dx = dx - 0.0;
-        dy = dy - 0.0;
         double2 vi = m.vel[e.x], ve = m.vel[e.y];
-        if (!exact) {
+        if (!flags[0]) {
+            double dx = 0.0 + wrapd(pe.x, pi.x, m.D);
+            double dy = 0.0 + wrapd(pe.y, pi.y, m.D);
             double px = ve.x - vi.x, py = ve.y - vi.y;
             double s = dx * px + dy * py;
             double n2 = dx * dx + dy * dy;
@@ -481,24 +450,35 @@ __global__ void k_text_label(DevMesh m, double dt, double inv_dt, const int *fla
             double margin = 1e-12 * (n2 * inv_dt) + 1e-14 * (dabs(dx) + dabs(dy)) * (dabs(px) + dabs(py)) +
                             1e-15 * (dabs(dx * px) + dabs(dy * py));
             if (n2 > 0 && s > thr + margin) {
+                /* not a candidate: its t_ext is outside [0, dt]; the value
+                 * itself is only observed if an event disables the
+                 * boundary, which then computes it (finalize_boundary) */
+                m.btext[b] = SEVC_MAX_T_EXT_D;
+                m.bexact[b] = 0;
                 m.bcand[b] = 0;
                 m.bconf[b] = -1;
                 return;
             }
         }
-        double norm = vmag(dx, dy);
-        double tx = 0, ty = 0;
-        if (norm != 0) {                            /* vector2_unitary, src/geometry.h:274 */
-            double ang = atan2(dy, dx);
-            tx = cos(ang);
-            ty = sin(ang);
-        }
-        double aux = tx * (ve.x - vi.x) + ty * (ve.y - vi.y);
-        text = (aux == 0) ? 100 : -norm / aux;
+        text = text_exact(pi, pe, vi, ve, m.D);
         m.btext[b] = text;
+        m.bexact[b] = 1;
     }
     m.bcand[b] = (text >= 0 && text <= dt) ? 1 : 0;
     m.bconf[b] = -1;
+}
+
+/* the positions, velocities and boundary ends the step's events start from
+ * (only needed when not every output value was computed exactly) */
+__global__ void k_snapshot(DevMesh m, const int *flags)
+{
+    if (flags[0]) return;
+    int stride = gridDim.x * blockDim.x;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m.nv; v += stride) {
+        m.pos0[v] = m.pos[v];
+        m.vel0[v] = m.vel[v];
+    }
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < m.nb; b += stride) m.bv0[b] = m.bv[b];
 }
 
 /* compute_grain_areas, src/calculus.h:224 */
@@ -654,12 +634,12 @@ void launch_full_flag(const DevScratch &x, cudaStream_t s)
 }
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_grain_dadt<<<nblk(m.ng), TPB, 0, s>>>(m, x.perm, x.vbucket, x.flags);
+    int g = nblk(m.ng);   /* grid-stride: every grain, or only the 3-sided ones, decided on the device */
+    COUNT_LAUNCHES(1), k_grain_dadt<<<g < 8 * 152 ? g : 8 * 152, TPB, 0, s>>>(m, x.perm, x.vbucket, x.flags);
 }
-void launch_mark_force(const DevMesh &m, const DevScratch &x, cudaStream_t s)
+void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    int g = nblk(m.ng);
-    COUNT_LAUNCHES(1), k_mark_force<<<g < 152 ? g : 152, TPB, 0, s>>>(m, x.perm, x.vbucket, x.flags);
+    COUNT_LAUNCHES(1), k_snapshot<<<4 * 152, TPB, 0, s>>>(m, x.flags);
 }
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s)
 {

@@ -68,7 +68,8 @@ void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s);
  * min_grains, [3] current grain count (see k_full_flag) */
 void launch_full_flag(const DevScratch &x, cudaStream_t s);
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s);
-void launch_mark_force(const DevMesh &m, const DevScratch &x, cudaStream_t s);
+/* copies pos, vel, bv to pos0, vel0, bv0 unless the step computes every output */
+void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s);
 void launch_grain_area(const DevMesh &m, cudaStream_t s);
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);

@@ -73,9 +73,11 @@ __device__ void glist_replace(const DevMesh &m, int g, int oldv, int newv) /* :6
         if (L[i] == oldv) { L[i] = newv; return; }
 }
 
-/* queue a grain for the fix-up pass (grain.fix = true) */
+/* queue a grain for the fix-up pass (grain.fix = true); its list is
+ * about to change, so its dA/dt for this step is settled first */
 __device__ void mark_fix(const DevMesh &m, int g)
 {
+    finalize_grain(m, g);
     if (m.gfix[g]) return;
     m.gfix[g] = 1;
     int i = atomicAdd(m.nfix, 1);
@@ -365,7 +367,14 @@ __device__ int remove_two_grains_dev(const DevMesh &m, int bnd, const int *gnic)
     set_mod(m, B, 1, FIX_REMOVE, G4, C, -2);
     set_mod(m, B, 2, FIX_REMOVE, G4, D, -2);
     sa = m.vb[A]; sbv = m.vb[B];
-    for (int i = 0; i < 3; i++) { m.ben[slot3(sa, i)] = 0; m.ben[slot3(sbv, i)] = 0; }
+    for (int i = 0; i < 3; i++) {
+        finalize_boundary(m, slot3(sa, i));
+        finalize_boundary(m, slot3(sbv, i));
+        m.ben[slot3(sa, i)] = 0;
+        m.ben[slot3(sbv, i)] = 0;
+    }
+    finalize_boundary(m, DF);
+    finalize_boundary(m, bnd);
     m.ben[DF] = 0;
     m.ben[bnd] = 0;
     m.ven[A] = 0; m.ven[D] = 0; m.ven[C] = 0; m.ven[B] = 0;
@@ -501,7 +510,7 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
     for (int i = 0; i < 3; i++) {
         int x = slot3(sc, i);
         int2 e = m.bv[x];
-        if ((e.x == B && e.y == C) || (e.y == B && e.x == C)) { m.ben[x] = 0; break; }
+        if ((e.x == B && e.y == C) || (e.y == B && e.x == C)) { finalize_boundary(m, x); m.ben[x] = 0; break; }
     }
     int BE = -1, CF = -1;
     for (int i = 0; i < 3; i++) {
@@ -522,12 +531,12 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
     for (int i = 0; i < 3; i++) {
         int x = slot3(sa, i);
         int2 f = m.bv[x];
-        if (f.x == B || f.y == B) { m.ben[x] = 0; set_slot3(sa, i, BE); break; }
+        if (f.x == B || f.y == B) { finalize_boundary(m, x); m.ben[x] = 0; set_slot3(sa, i, BE); break; }
     }
     for (int i = 0; i < 3; i++) {
         int x = slot3(sa, i);
         int2 f = m.bv[x];
-        if (f.x == C || f.y == C) { m.ben[x] = 0; set_slot3(sa, i, CF); break; }
+        if (f.x == C || f.y == C) { finalize_boundary(m, x); m.ben[x] = 0; set_slot3(sa, i, CF); break; }
     }
     m.vb[A] = sa;
     m.ven[B] = 0;
