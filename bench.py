@@ -137,7 +137,7 @@ def ensemble_options(mod, n):
 
 def run_ensemble(n_inst, lo, hi, steps, warmup, seed=7, cache=None):
     """Batched handle against the same instances run one after another as
-    plain handles (each computing every output, like the batch).  Times are
+    plain handles (same output rule as the batch).  Times are
     wall clock around the steps (the host round trips of every step are
     part of what batching removes)."""
     import sevc
@@ -163,7 +163,6 @@ def run_ensemble(n_inst, lo, hi, steps, warmup, seed=7, cache=None):
     for m in meshes:
         o = ensemble_options(sevc, len(m["oris"]))
         e = sevc.Engine.from_arrays(o, m["xy"], m["ridges"], m["oris"], m["se"])
-        e.set_exact_all(True)
         gi = len(m["oris"])
         for _ in range(warmup):
             gi = e.step().curr_n_grains

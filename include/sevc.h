@@ -129,7 +129,9 @@ sevc_status sevc_run_steps(sevc_handle *h, int nsteps, int *done, sevc_step_info
 int sevc_should_continue(const sevc_handle *h);
 
 /* export_data, src/io.h:280-377: write one snapshot with the reference's
- * exact text format; `time` is printed as TIME. */
+ * exact text format; `time` is printed as TIME.  Allowed before the first
+ * step and after steps whose outputs are complete (export_due steps, or
+ * every step with sevc_set_exact_all); SEVC_ERR_ARG otherwise. */
 sevc_status sevc_export_text(sevc_handle *h, const char *path, double time);
 /* device_to_host, src/translation.h:184-199 (without freeing anything):
  * copy the mesh into caller-owned arrays sized like sevc_mesh_sizes. */
@@ -178,13 +180,13 @@ sevc_status sevc_rng_record_noalloc(int nstreams, int ndraws, double *d_out, voi
  * kernel launch of a step covers all of them, so hundreds of small runs
  * cost one run's launches and host round trips.  Every instance follows
  * exactly the plain method: instance i, stepped in a batch, produces bit
- * for bit what a plain handle created from the same arrays produces with
- * sevc_set_exact_all(1) (its own polling convergence, 2x3 loop, event
- * order and its own copy of the 8192 random streams).  Options are shared
- * except n_grains, which is each instance's grain count.  The batch runs
- * until the shared tmax / nmax; min_grains is reported per instance
- * (keep_going of sevc_instance_info) but stops nothing.  Outputs are
- * complete on every step.
+ * for bit what a plain handle created from the same arrays produces (its
+ * own polling convergence, 2x3 loop, event order and its own copy of the
+ * 8192 random streams).  Options are shared except n_grains, which is
+ * each instance's grain count.  The batch runs until the shared tmax /
+ * nmax; min_grains is reported per instance (keep_going of
+ * sevc_instance_info) but stops nothing.  Output-only values follow the
+ * plain rule (complete on snapshot steps, see sevc_set_exact_all).
  *
  * Arrays of instance i: nv[i] positions xy[i] (interleaved), nb[i] ridges
  * ridges[i] (pairs), ng[i] orientations oris[i] and stored energies se[i],
@@ -254,9 +256,12 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
                                    double *grad_se, double *grad_gb_scaling, double *grad_mu);
 
 /* Output-only fields (extinction times of boundaries that cannot flip,
- * dA/dt of grains that cannot vanish) are computed only on steps that can
- * export a snapshot (sevc_step_info.outputs_complete); exported snapshots
- * are always complete.  on = 1 computes them on every step. */
+ * dA/dt of grains that cannot vanish) are computed for every entity only
+ * on steps that can export a snapshot (sevc_step_info.outputs_complete);
+ * on other steps only the values that can ever be exported are (those of
+ * entities the step disables).  sevc_export_text after a step that was
+ * not complete is refused (SEVC_ERR_ARG).  on = 1 computes every value on
+ * every step. */
 sevc_status sevc_set_exact_all(sevc_handle *h, int on);
 
 /* The fixed launch sequences of a step (its first half, one polling

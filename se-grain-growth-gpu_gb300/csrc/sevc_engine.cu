@@ -71,6 +71,7 @@ struct sevc_handle {
     double t = 0, nucleated_area = 0;
     int polling_cap = 100000;
     int exact_all = 0;
+    int outputs_complete = 1;   /* the last step computed every output-only value */
     /* instances (one for a plain handle): entity offsets, initial grain
      * count (the n_grains of src/main.cu:137), per-instance run state and
      * the per-instance summary of the last step */
@@ -696,8 +697,8 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     /* host part of the output decision (k_full_flag): steps that can export,
      * long steps, exact_all, and every step of a batch */
     int mg = o.min_grains;
-    h->h_flags[1] = batch || h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0);
-    h->h_flags[2] = mg;
+    h->h_flags[1] = h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && h->n % o.snap_gap == 0);
+    h->h_flags[2] = batch ? 0 : mg;   /* a batch does not stop at min_grains */
     h->h_flags[3] = h->curr_n_grains;
     if (!cuda_ok(cudaMemcpyAsync(x.flags + 1, h->h_flags + 1, 3 * sizeof(int), cudaMemcpyHostToDevice, s), "upload"))
         return SEVC_ERR_CUDA;
@@ -750,6 +751,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         return SEVC_ERR_CUDA;
     const int full = hb[o_full] != 0;
     loc.outputs_complete = full;
+    h->outputs_complete = full;
     float ms = 0;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     if (h->profiling) prof_collect(h);
@@ -881,9 +883,20 @@ sevc_status sevc_get_state(sevc_handle *h, sevc_mesh_host *o)
     return ok ? SEVC_OK : SEVC_ERR_CUDA;
 }
 
+/* a snapshot after a step that skipped output-only values would not be
+ * the reference's: refuse it */
+static bool export_allowed(const sevc_handle *h)
+{
+    if (h->outputs_complete) return true;
+    sevc_set_error("the last step computed only the output values it could observe: export after steps with "
+                   "export_due (snap_gap) or enable sevc_set_exact_all");
+    return false;
+}
+
 sevc_status sevc_export_text(sevc_handle *h, const char *path, double time)
 {
     if (!h || !path) return SEVC_ERR_ARG;
+    if (!export_allowed(h)) return SEVC_ERR_ARG;
     sevc_hmesh hm;
     if (sevc_hmesh_alloc(&hm, h->nv, h->nb, h->ng)) return SEVC_ERR_CAPACITY;
     sevc_status st = sevc_get_state(h, &hm.m);
@@ -895,6 +908,7 @@ sevc_status sevc_export_text(sevc_handle *h, const char *path, double time)
 sevc_status sevc_export_instance_text(sevc_handle *h, int inst, const char *path, double time)
 {
     if (!h || !path || inst < 0 || inst >= h->ninst) return SEVC_ERR_ARG;
+    if (!export_allowed(h)) return SEVC_ERR_ARG;
     sevc_hmesh all, one;
     if (sevc_hmesh_alloc(&all, h->nv, h->nb, h->ng)) return SEVC_ERR_CAPACITY;
     sevc_status st = sevc_get_state(h, &all.m);
@@ -1195,6 +1209,7 @@ struct CkptHeader {
     uint64_t dbytes;
     int32_t n, curr_n_grains;
     double t, nucleated_area, mu, gb_scaling;
+    int32_t outputs_complete, reserved;
 };
 } // namespace
 
@@ -1211,6 +1226,7 @@ sevc_status sevc_checkpoint_save(sevc_handle *h, const char *path)
     hd.dbytes = h->dbytes;
     hd.n = h->n; hd.curr_n_grains = h->curr_n_grains;
     hd.t = h->t; hd.nucleated_area = h->nucleated_area; hd.mu = h->p.mu; hd.gb_scaling = h->opt.GB_scaling;
+    hd.outputs_complete = h->outputs_complete;
     FILE *f = fopen(path, "wb");
     if (!f) { sevc_set_error("cannot write %s", path); return SEVC_ERR_IO; }
     size_t I = h->ninst;
@@ -1249,6 +1265,7 @@ sevc_status sevc_checkpoint_load(sevc_handle *h, const char *path)
         return SEVC_ERR_CUDA;
     h->n = hd.n; h->curr_n_grains = hd.curr_n_grains; h->t = hd.t; h->nucleated_area = hd.nucleated_area;
     h->p.mu = hd.mu; h->opt.GB_scaling = hd.gb_scaling; h->p.scaling = hd.gb_scaling;
+    h->outputs_complete = hd.outputs_complete;
     drop_graphs(h);
     h->icurr = icurr; h->iallow = iallow; h->iarea = iarea;
     return SEVC_OK;

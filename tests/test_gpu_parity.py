@@ -202,6 +202,8 @@ def test_skipped_outputs_change_nothing_else(gpu, name, tmp_path):
             skipped += 1
             c = (sa["bcand"] > 0) | (sa["ben"] == 0)
             assert np.array_equal(sa["btext"][c], sb["btext"][c])
+            g = sa["gen"] == 0                       # dA/dt of every grain ever disabled
+            assert np.array_equal(sa["gdadt"][g], sb["gdadt"][g]), (name, ia.n)
         if not ia.keep_going:
             break
     assert skipped > 0
