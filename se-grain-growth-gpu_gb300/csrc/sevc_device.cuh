@@ -94,6 +94,7 @@ struct DevMesh {
     double2 *pos0, *vel0;
     int2 *bv0;
     uint8_t *bexact, *gexact;
+    uint8_t *bmark;      /* boundaries marked by a sparse pass, compacted next */
 };
 
 enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };

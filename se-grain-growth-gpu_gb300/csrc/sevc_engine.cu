@@ -188,6 +188,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
         { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
         { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
+        { (void **)&m.bmark, B },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -453,7 +454,7 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     /* The first count of the 2x3 loop (:228) depends only on the topology,
      * which nothing changes before that loop: count now, and decide on the
      * device whether this step must compute every output-only value. */
-    { Prof pr(h, "two_three_count"); launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, s); }
+    { Prof pr(h, "two_three_count"); launch_two_three_first(m, x, x.list_b, x.n_b, s); }
     launch_full_flag(x, s);
     { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }                                     /* :206 */
     { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, s); }                               /* :212-216 */

@@ -79,8 +79,10 @@ void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, c
 void launch_pack_summary(const DevMesh &m, const DevScratch &x, int ninst, int *out, cudaStream_t s);
 
 /* topology (sevc_topology.cu) */
-enum CompactKind { CK_CAND = 0, CK_TWO_THREE = 1, CK_GRAIN_CAND = 2, CK_GVLEN3 = 3 };
+enum CompactKind { CK_CAND = 0, CK_TWO_THREE = 1, CK_GRAIN_CAND = 2, CK_GVLEN3 = 3, CK_MARKED = 4 };
 void launch_compact(const DevMesh &m, const DevScratch &x, CompactKind kind, int *out, int *n_out, cudaStream_t s);
+/* the CK_TWO_THREE list from the 3-sided bucket of this step's grain pass */
+void launch_two_three_first(const DevMesh &m, const DevScratch &x, int *out, int *n_out, cudaStream_t s);
 /* one polling iteration for every instance not yet converged; leaves the
  * number still running in x.nrun */
 void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *cand, const int *ncand,

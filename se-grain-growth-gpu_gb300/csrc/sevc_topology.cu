@@ -108,6 +108,7 @@ __device__ __forceinline__ bool pred(const DevMesh &m, int i)
     if (KIND == CK_CAND) return m.ben[i] && m.bcand[i];
     if (KIND == CK_GRAIN_CAND) return m.gen[i] && m.gcand[i];
     if (KIND == CK_GVLEN3) return m.gvlen[i] == 3;
+    if (KIND == CK_MARKED) return m.bmark[i] != 0;
     /* CK_TWO_THREE: enabled boundary whose two common grains both have
      * three vertices (src/topological.h:31-35, :970-974) */
     if (!m.ben[i]) return false;
@@ -389,6 +390,26 @@ __device__ bool two_three_qualifies(const DevMesh &m, int b, int *gic)
     return m.gvlen[gic[0]] == 3 && m.gvlen[gic[1]] == 3;
 }
 
+/* The step's first 2x3 count: a qualifying boundary lies on two 3-sided
+ * grains, so only the boundaries at the vertices of the 3-sided grains
+ * (bucket 3 of this step's side-count order) are tested; the ordered
+ * compaction of the marks then gives the same ascending list as testing
+ * every boundary. */
+__global__ void k_mark_two_three(DevMesh m, const int *perm, const int *vbucket)
+{
+    int n3 = vbucket[VB_COUNT(3)], start = vbucket[VB_START(3)];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        const int *L = m.glist + (size_t)SEVC_MAXV * perm[start + i];
+        for (int k = 0; k < 3; k++) {
+            int4 s = m.vb[L[k]];
+            for (int j = 0; j < 3; j++) {
+                int b = slot3(s, j), gic[2];
+                if (two_three_qualifies(m, b, gic)) m.bmark[b] = 1;
+            }
+        }
+    }
+}
+
 __device__ bool sorted_contains(const int *a, int lo, int hi, int x)
 {
     int end = hi;
@@ -553,18 +574,27 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
 
 /* remove_grains (:994), launched <<<1,1>>> by the reference: grains in
  * ascending index order */
+/* one warp per instance: a removal disables only its own grain, so the
+ * listed grains that will be removed are known up front; lane 0 applies
+ * them in list order */
 __global__ void k_remove_grains(DevMesh m, const int *list, const int *n)
 {
-    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (inst >= m.ninst) return;
     int lo = lower_bound_i(list, *n, m.goff[inst]);
     int hi = lower_bound_i(list, *n, m.goff[inst + 1]);
-    for (int i = lo; i < hi; i++) {
-        int g = list[i];
-        if (m.gen[g] && m.gcand[g]) {
-            remove_grain_dev(m, g);
-            m.evt[EVT_COUNT * inst + EVT_REMOVALS]++;
-        }
+    for (int base = lo; base < hi; base += 32) {
+        int i = base + lane;
+        bool f = i < hi && m.gen[list[i]] && m.gcand[list[i]];
+        unsigned hits = __ballot_sync(0xffffffffu, f);
+        if (lane == 0)
+            while (hits) {
+                int j = __ffs(hits) - 1;
+                hits &= hits - 1;
+                remove_grain_dev(m, list[base + j]);
+                m.evt[EVT_COUNT * inst + EVT_REMOVALS]++;
+            }
+        __syncwarp();
     }
 }
 
@@ -644,18 +674,27 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
 
 /* apply_flippings (:1016-1026); flips that share no vertex commute, the
  * rest are applied in ascending boundary order */
+/* One warp per instance.  A flip changes no boundary's enabled or
+ * candidate flag, so which listed boundaries flip is known up front: the
+ * warp tests 32 at a time and lane 0 applies the hits in list order. */
 __global__ void k_flips(DevMesh m, double eps, const int *list, const int *n)
 {
-    int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (inst >= m.ninst) return;
     int lo = lower_bound_i(list, *n, m.boff[inst]);
     int hi = lower_bound_i(list, *n, m.boff[inst + 1]);
-    for (int i = lo; i < hi; i++) {
-        int b = list[i];
-        if (m.ben[b] && m.bcand[b]) {
-            flip_dev(m, b, eps);
-            m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
-        }
+    for (int base = lo; base < hi; base += 32) {
+        int i = base + lane;
+        bool f = i < hi && m.ben[list[i]] && m.bcand[list[i]];
+        unsigned hits = __ballot_sync(0xffffffffu, f);
+        if (lane == 0)
+            while (hits) {
+                int j = __ffs(hits) - 1;
+                hits &= hits - 1;
+                flip_dev(m, list[base + j], eps);
+                m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
+            }
+        __syncwarp();
     }
 }
 
@@ -769,7 +808,16 @@ void launch_compact(const DevMesh &m, const DevScratch &x, CompactKind kind, int
     case CK_TWO_THREE: compact_impl<CK_TWO_THREE>(m, x, m.nb, out, n_out, s); break;
     case CK_GRAIN_CAND: compact_impl<CK_GRAIN_CAND>(m, x, m.ng, out, n_out, s); break;
     case CK_GVLEN3: compact_impl<CK_GVLEN3>(m, x, m.ng, out, n_out, s); break;
+    case CK_MARKED: compact_impl<CK_MARKED>(m, x, m.nb, out, n_out, s); break;
     }
+}
+
+void launch_two_three_first(const DevMesh &m, const DevScratch &x, int *out, int *n_out, cudaStream_t s)
+{
+    cudaMemsetAsync(m.bmark, 0, (size_t)m.nb, s);
+    int g = (m.ng + TPB - 1) / TPB;
+    COUNT_LAUNCHES(1), k_mark_two_three<<<g < 4 * WL_BLOCKS ? g : 4 * WL_BLOCKS, TPB, 0, s>>>(m, x.perm, x.vbucket);
+    compact_impl<CK_MARKED>(m, x, m.nb, out, n_out, s);
 }
 
 void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *cand, const int *ncand,
@@ -809,7 +857,7 @@ void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s)
 
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_remove_grains<<<instgrid(m), 32, 0, s>>>(m, list, n);
+    COUNT_LAUNCHES(1), k_remove_grains<<<m.ninst, 32, 0, s>>>(m, list, n);
 }
 
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
@@ -821,7 +869,7 @@ void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncan
                   cudaStream_t s)
 {
     (void)x;
-    COUNT_LAUNCHES(1), k_flips<<<instgrid(m), 32, 0, s>>>(m, eps, cand, ncand);
+    COUNT_LAUNCHES(1), k_flips<<<m.ninst, 32, 0, s>>>(m, eps, cand, ncand);
 }
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)
