@@ -21,7 +21,8 @@ NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I", os.path.join(ROOT, "include")]
-CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-I", os.path.join(ROOT, "include")]
+CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-Wall", "-I",
+          os.path.join(ROOT, "include")]
 
 CU = ["sevc_geometry.cu", "sevc_topology.cu", "sevc_nucleation.cu", "sevc_adjoint.cu", "sevc_check.cu",
       "sevc_engine.cu"]
@@ -64,7 +65,7 @@ def build(force=False, verbose=False, ptxas_info=False):
             logs.append(out)
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lgomp"])
         os.replace(tmp, LIB)
     cli_src = os.path.join(PKG, "cli", "sevc_main.c")
     if force or _stale(CLI, [cli_src, LIB]):

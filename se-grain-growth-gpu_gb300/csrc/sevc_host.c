@@ -225,28 +225,37 @@ int sevc_host_build(const sevc_options *opt, int nv, const double *xy, int nb, c
             sevc_set_error("vertex %d has fewer than three boundaries", v);
             goto bad;
         }
+#pragma omp parallel for schedule(static)
     for (int v = 0; v < nv; v++) order_boundaries(m, v, D);
 
-    {   /* face traversal, src/io.h:137-186 */
+    {   /* face traversal, src/io.h:137-186.  The successor of every
+         * (vertex, side) half-edge is found in parallel first; the walk in
+         * the reference's order then only follows it. */
         unsigned char *seen = (unsigned char *)calloc(3 * (size_t)nv, 1);
+        int *next = (int *)malloc(3 * (size_t)nv * sizeof(int));
+        if (!seen || !next) { free(seen); free(next); sevc_set_error("out of host memory"); goto bad; }
+#pragma omp parallel for schedule(static)
+        for (int h = 0; h < 3 * nv; h++) {
+            int cur = h / 3, b = m->vb[h];
+            int nx = (m->bini[b] == cur) ? m->bend[b] : m->bini[b];
+            int i = 0;
+            while (i < 3 && m->vb[3 * nx + i] != b) i++;
+            next[h] = i == 3 ? -1 : 3 * nx + (i + 1) % 3;
+        }
         int ngr = 0;
         for (int j = 0; j < nv && ngr >= 0; j++)
             for (int side0 = 0; side0 < 3; side0++) {
                 if (seen[3 * j + side0]) continue;
                 if (ngr >= ng) { ngr = -1; break; }
                 int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * ngr];
-                int n = 0, cur = j, side = side0;
+                int n = 0, h = 3 * j + side0;
                 do {
-                    if (seen[3 * cur + side] || n >= SEVC_MAX_VRT_PER_GRN) { ngr = -2; break; }
-                    seen[3 * cur + side] = 1;
-                    L[n++] = cur;
-                    int b = m->vb[3 * cur + side];
-                    cur = (m->bini[b] == cur) ? m->bend[b] : m->bini[b];
-                    int i = 0;
-                    while (i < 3 && m->vb[3 * cur + i] != b) i++;
-                    if (i == 3) { ngr = -2; break; }
-                    side = (i + 1) % 3;
-                } while (cur != j);
+                    if (seen[h] || n >= SEVC_MAX_VRT_PER_GRN) { ngr = -2; break; }
+                    seen[h] = 1;
+                    L[n++] = h / 3;
+                    h = next[h];
+                    if (h < 0) { ngr = -2; break; }
+                } while (h / 3 != j);
                 if (ngr < 0) break;
                 for (int k = n; k < SEVC_MAX_VRT_PER_GRN; k++) L[k] = -1;
                 m->gvlen[ngr] = n;
@@ -254,13 +263,17 @@ int sevc_host_build(const sevc_options *opt, int nv, const double *xy, int nb, c
                 ngr++;
             }
         free(seen);
+        free(next);
         if (ngr != ng) {
             sevc_set_error("face traversal found %d grains, expected %d", ngr, ng);
             goto bad;
         }
     }
-    for (int v = 0; v < nv; v++) {               /* src/io.h:189-192 */
-        order_boundaries(m, v, D);
+    /* src/io.h:189-192 sorts each vertex's boundaries again, then swaps the
+     * first two.  Nothing moved since the first sort and the three
+     * compare-swaps leave a sorted triple unchanged, so only the swap
+     * remains. */
+    for (int v = 0; v < nv; v++) {
         int t = m->vb[3 * v + 1]; m->vb[3 * v + 1] = m->vb[3 * v]; m->vb[3 * v] = t;
     }
     for (int g = 0; g < ng; g++)                  /* src/io.h:196-200 */
