@@ -216,6 +216,18 @@ def run_adjoint(n=10000, steps=2000, every=100, dt=1e-6, seed=17, nbins=20, amax
             "timing": "wall clock; forward = the taped steps, backward = sevc_adjoint_histogram"}
 
 
+def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=5e-5, seed=5):
+    """Batched calibration of (gamma, mu, stored-energy scale) by Adam steps
+    through the adjoint, against the histogram of the same batch run with
+    the generating values (1, 1, 1)."""
+    import numpy as np
+    import meshgen
+    import calibrate
+    rng = np.random.default_rng(seed)
+    meshes = [meshgen.make_inputs(int(n), 100 + i) for i, n in enumerate(rng.integers(lo, hi + 1, n_inst))]
+    return calibrate.run(meshes, dt=dt, steps=steps, iters=iters, checkpoint_every=50)
+
+
 def algorithmic_bytes_per_step(nv):
     """Compulsory traffic of one step per vertex (131.5 B per vertex-step:
     72*V + 25*B + 20*G + 4*sum(vlen) with B = 1.5V, G = V/2, sum(vlen) = 3V)."""
@@ -344,6 +356,7 @@ def run_engine(args):
                                         10, 3, cache=args.ensemble_cache)
     if args.adjoint_sample:
         line["adjoint"] = run_adjoint()
+        line["calibration"] = run_calibration()
     print(json.dumps(line))
 
 
@@ -413,8 +426,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble"],
-                    help="ensemble: batched ensemble against sequential plain runs, its own JSON line")
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate"],
+                    help="ensemble: batched ensemble against sequential plain runs; calibrate: 64 x 20,000-grain "
+                         "batched calibration, 50 iterations; each prints its own JSON line")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--ensemble-grains", type=int, nargs=2, default=[500, 20000])
     ap.add_argument("--ensemble-sample", type=int, default=64,
@@ -438,6 +452,14 @@ def main():
                           "ms_per_step": r["batch_ms_per_step"], "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded periodic Voronoi)",
                           "config": {"workload": "batched ensemble", **r}}))
+        return
+    if args.workload == "calibrate":
+        r = run_calibration(n_inst=64, lo=20000, hi=20000, steps=args.steps, iters=50, dt=2e-5)
+        print(json.dumps({"metric": "backward/forward time ratio of batched calibration",
+                          "value": r["backward_forward_ratio"], "unit": "x", "n_gpus": 1, "steps": args.steps,
+                          "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic (seeded periodic Voronoi)",
+                          "config": {"workload": "batched stored-energy calibration", **r}}))
         return
     run_engine(args)
 
