@@ -216,16 +216,70 @@ def run_adjoint(n=10000, steps=2000, every=100, dt=1e-6, seed=17, nbins=20, amax
             "timing": "wall clock; forward = the taped steps, backward = sevc_adjoint_histogram"}
 
 
-def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=5e-5, seed=5):
+def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=2e-3, seed=5):
     """Batched calibration of (gamma, mu, stored-energy scale) by Adam steps
     through the adjoint, against the histogram of the same batch run with
-    the generating values (1, 1, 1)."""
+    the generating values (1, 1, 1); grains about one unit across (domain
+    sqrt of the mean grain count), SE U[0,1)."""
     import numpy as np
     import meshgen
     import calibrate
     rng = np.random.default_rng(seed)
-    meshes = [meshgen.make_inputs(int(n), 100 + i) for i, n in enumerate(rng.integers(lo, hi + 1, n_inst))]
-    return calibrate.run(meshes, dt=dt, steps=steps, iters=iters, checkpoint_every=50)
+    sizes = rng.integers(lo, hi + 1, n_inst)
+    meshes = [meshgen.make_inputs(int(n), 100 + i) for i, n in enumerate(sizes)]
+    return calibrate.run(meshes, dt=dt, steps=steps, iters=iters, checkpoint_every=50,
+                         domain=float(np.sqrt(sizes.mean())))
+
+
+def run_small(steps, seed=1, n=2000):
+    """The small plain configuration: 2,000 grains on the unit square, SE
+    U[0, 0.5], dt = 1e-6, no nucleation.  The engine and the oracle (serial
+    and with every host core) run the same steps; the per-step event counts
+    and grain counts are compared."""
+    import numpy as np
+    import sevc
+    import meshgen
+    from oracle import oracle as O
+    O.build()
+    mesh = meshgen.make_inputs(n, seed)
+    kw = dict(n_grains=n, dt=1e-6, dtau=1.0, domain_bound=1.0, GB_eps=0.0, GB_scaling=1.0, SE_eps=1.0,
+              SE_min=0.0, SE_max=0.5, do_nucleation=0, nmax=10 ** 8, tmax=-1, snap_gap=10 ** 8,
+              n_blocks=32, n_threads=256)
+    o = sevc.default_options(**kw)
+    o.min_grains = -1
+    e = sevc.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    ev_gpu, vs = [], 0
+    g = n
+    t0 = time.time()
+    for _ in range(steps):
+        vs += 2 * g
+        i = e.step()
+        g = i.curr_n_grains
+        ev_gpu.append((i.curr_n_grains, i.n_flips, i.n_removals, i.n_two_three))
+    gpu_s = time.time() - t0
+    e.close()
+    out = {"grains": n, "steps": steps, "grains_left": g, "gpu_vertex_steps_per_s": vs / gpu_s,
+           "gpu_ms_per_step": 1e3 * gpu_s / steps}
+    for threads in (1, os.cpu_count() or 1):
+        opt = O.default_options(**kw)
+        O.finish_options(opt)
+        opt.min_grains = -1
+        orc = O.Oracle.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+        orc.set_threads(threads)
+        ev, vs_c, g = [], 0, n
+        t0 = time.time()
+        for _ in range(steps):
+            vs_c += 2 * g
+            orc.step()
+            orc.finish_step()
+            s = orc.s
+            g = s.curr_n_grains
+            ev.append((s.curr_n_grains, s.ev_flips, s.ev_removals, s.ev_two_three))
+        cpu_s = time.time() - t0
+        out["cpu_%d_threads_vertex_steps_per_s" % threads] = vs_c / cpu_s
+        out["events_identical_%d" % threads] = ev == ev_gpu
+    out["events"] = [int(x) for x in np.array(ev_gpu)[:, 1:].sum(0)]
+    return out
 
 
 def algorithmic_bytes_per_step(nv):
@@ -426,7 +480,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate"],
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate", "small"],
                     help="ensemble: batched ensemble against sequential plain runs; calibrate: 64 x 20,000-grain "
                          "batched calibration, 50 iterations; each prints its own JSON line")
     ap.add_argument("--instances", type=int, default=512)
@@ -453,8 +507,16 @@ def main():
                           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded periodic Voronoi)",
                           "config": {"workload": "batched ensemble", **r}}))
         return
+    if args.workload == "small":
+        r = run_small(args.steps)
+        print(json.dumps({"metric": "vertex-steps/s at 2K grains", "value": r["gpu_vertex_steps_per_s"],
+                          "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 0,
+                          "ms_per_step": r["gpu_ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded periodic Voronoi)",
+                          "config": {"workload": "2,000-grain plain run, SE U[0,0.5], dt 1e-6", **r}}))
+        return
     if args.workload == "calibrate":
-        r = run_calibration(n_inst=64, lo=20000, hi=20000, steps=args.steps, iters=50, dt=2e-5)
+        r = run_calibration(n_inst=64, lo=20000, hi=20000, steps=args.steps, iters=50, dt=2e-3)
         print(json.dumps({"metric": "backward/forward time ratio of batched calibration",
                           "value": r["backward_forward_ratio"], "unit": "x", "n_gpus": 1, "steps": args.steps,
                           "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,

@@ -24,8 +24,8 @@ import sevc
 NB, AMAX = 20, 3.0
 
 
-def batch_options(n_grains, dt):
-    o = sevc.default_options(n_grains=n_grains, dt=dt, dtau=1.0, domain_bound=1.0, GB_eps=0.0, GB_scaling=1.0,
+def batch_options(n_grains, dt, domain=1.0):
+    o = sevc.default_options(n_grains=n_grains, dt=dt, dtau=1.0, domain_bound=domain, GB_eps=0.0, GB_scaling=1.0,
                              SE_eps=1.0, SE_min=999.0, SE_max=999.0, do_nucleation=0, nmax=10 ** 8, tmax=-1,
                              snap_gap=10 ** 8, n_blocks=32, n_threads=256)
     o.min_grains = -1
@@ -33,9 +33,9 @@ def batch_options(n_grains, dt):
 
 
 class Calibration:
-    def __init__(self, meshes, dt, steps, checkpoint_every=50):
+    def __init__(self, meshes, dt, steps, checkpoint_every=50, domain=1.0):
         self.meshes, self.dt, self.steps, self.every = meshes, dt, steps, checkpoint_every
-        self.eng = sevc.Engine.from_batch(batch_options(len(meshes[0]["oris"]), dt), meshes)
+        self.eng = sevc.Engine.from_batch(batch_options(len(meshes[0]["oris"]), dt, domain), meshes)
         self.se0 = self.eng.get_state()["gse"].copy()
         self.dir = tempfile.mkdtemp(prefix="sevc_cal_")
         self.ckpt = os.path.join(self.dir, "initial.ckpt")
@@ -79,10 +79,14 @@ class Calibration:
             pass
 
 
-def run(meshes, dt, steps, iters, truth=(1.0, 1.0, 1.0), start=(1.3, 0.8, 0.6), lr=0.08, checkpoint_every=50):
+def run(meshes, dt, steps, iters, truth=(1.0, 1.0, 1.0), start=(1.3, 0.8, 0.6), lr=0.08, checkpoint_every=50,
+        domain=1.0):
     """Calibrate (gamma, mu, c) from `start` against the histogram the
-    batch produces with `truth`.  Returns a summary dict."""
-    cal = Calibration(meshes, dt, steps, checkpoint_every)
+    batch produces with `truth`.  Returns a summary dict.  The stored-energy
+    term weighs against line tension in proportion to the grain size, so a
+    domain of about sqrt(grains per instance) (grains one unit across, as
+    in the reference's example) keeps c observable."""
+    cal = Calibration(meshes, dt, steps, checkpoint_every, domain)
     target = cal.histogram(*truth)
     cal.t_fwd = 0.0
     theta = np.log(np.array(start, float))
@@ -106,7 +110,7 @@ def run(meshes, dt, steps, iters, truth=(1.0, 1.0, 1.0), start=(1.3, 0.8, 0.6), 
     start = np.array(start, float)
     ident = lambda q: np.array([q[1] * q[0], q[1] * q[2]])
     return {"instances": len(meshes), "grains": int(sum(len(mm["oris"]) for mm in meshes)), "steps": steps,
-            "iterations": iters, "dt": dt, "params": ["gamma", "mu", "se_scale"],
+            "iterations": iters, "dt": dt, "domain_bound": domain, "params": ["gamma", "mu", "se_scale"],
             "truth": truth.tolist(), "start": start.tolist(), "final": p.tolist(),
             "rel_err_start": (np.abs(start - truth) / truth).tolist(),
             "rel_err_final": (np.abs(p - truth) / truth).tolist(),
