@@ -241,6 +241,31 @@ __global__ void k_adj_grains(DevMesh m, double mu, const double2 *lv, double *sg
     gse[g] += -mu * s * acc;
 }
 
+/* For the edge vector d (length L) and its end moved by eps along axis c,
+ * d' = d + eps e_c, L' = |d'|: *g = (d'/L' - d/L) / eps, the gradient with
+ * respect to the moved end of (L' - L) / eps, and *s = (L' - L) / eps, both
+ * in forms without cancellation:
+ *   (L' - L) / eps = (2 d_c + eps) / (L + L')
+ *   (d'/L' - d/L) / eps = e_c / L' - d (2 d_c + eps) / (L L' (L + L'))
+ * (the same values as the difference quotients, which lose about eight
+ * digits to cancellation).  L = 0, an edge whose ends coincide after a
+ * flip, takes the zero subgradient for d/L. */
+__device__ __forceinline__ void edge_fd_grad(double dx, double dy, double L, double E, int c, double2 *g, double *s)
+{
+    double ax = dx + (c == 0 ? E : 0.0), ay = dy + (c == 1 ? E : 0.0);
+    double L1 = sqrt(ax * ax + ay * ay);
+    double dc = c == 0 ? dx : dy;
+    double num = 2.0 * dc + E, S = L + L1;
+    *s = num / S;
+    double gx = (c == 0 ? 1.0 : 0.0) / L1, gy = (c == 1 ? 1.0 : 0.0) / L1;
+    if (L > 0) {
+        double t = num / (L * L1 * S);
+        gx -= dx * t;
+        gy -= dy * t;
+    }
+    *g = make_double2(gx, gy);
+}
+
 /* per vertex k (gather): lambda_n[k] = lambda_x[k] + (J_v^T lambda_v)[k];
  * d/ds of k's own velocity into ggam[k] */
 __global__ void k_adj_vertices(DevMesh m, double mu, double eps, double s_gb, const double2 *lx, const double2 *lv,
@@ -263,25 +288,24 @@ __global__ void k_adj_vertices(DevMesh m, double mu, double eps, double s_gb, co
         double2 pq = m.pos[q];
         double dx = wrapd(p.x, pq.x, m.D), dy = wrapd(p.y, pq.y, m.D);
         double L = sqrt(dx * dx + dy * dy);
-        /* a just-flipped boundary has both ends at one point: |d| has the
-         * zero subgradient there */
-        double nx = L > 0 ? dx / L : 0.0, ny = L > 0 ? dy / L : 0.0;
-        /* k moved along x / y: n' = (d + eps e_c) / |d + eps e_c| */
-        double Lx = sqrt((dx + E) * (dx + E) + dy * dy), Ly = sqrt(dx * dx + (dy + E) * (dy + E));
-        double n1x = (dx + E) / Lx, n1y = dy / Lx;      /* c = x */
-        double n2x = dx / Ly, n2y = (dy + E) / Ly;      /* c = y */
-        double cg = -mu * gam / E;
-        out.x += lk.x * cg * (n1x - nx) + lk.y * cg * (n2x - nx);
-        out.y += lk.x * cg * (n1y - ny) + lk.y * cg * (n2y - ny);
-        dgam += -mu * f * (lk.x * (Lx - L) + lk.y * (Ly - L)) / E;
-        /* q moved along x / y: seen from q the edge is -d */
+        /* k moved along x / y (d -> d + eps e_c) and q moved (-d -> -d + eps e_c) */
+        double2 gkx, gky, gqx, gqy;
+        double skx, sky;
+        edge_fd_grad(dx, dy, L, E, 0, &gkx, &skx);
+        edge_fd_grad(dx, dy, L, E, 1, &gky, &sky);
+        double sqx, sqy;
+        edge_fd_grad(-dx, -dy, L, E, 0, &gqx, &sqx);
+        edge_fd_grad(-dx, -dy, L, E, 1, &gqy, &sqy);
+        double cg = -mu * gam;
+        out.x += cg * (lk.x * gkx.x + lk.y * gky.x);
+        out.y += cg * (lk.x * gkx.y + lk.y * gky.y);
+        dgam += -mu * f * (lk.x * skx + lk.y * sky);
+        /* q's velocity: d/dx_k of -(gam/eps) (L(x_q + eps e_c) - L(x)) is
+         * minus the gradient with respect to the moved end */
         double2 lq = lv[q];
-        double qx = -dx, qy = -dy;
-        double Mx = sqrt((qx + E) * (qx + E) + qy * qy), My = sqrt(qx * qx + (qy + E) * (qy + E));
-        double m1x = (qx + E) / Mx, m1y = qy / Mx, m2x = qx / My, m2y = (qy + E) / My;
-        double cq = mu * gam / E;                        /* d/dx_k of -(gam/eps) L(x_q + eps e_c) */
-        out.x += lq.x * cq * (m1x + nx) + lq.y * cq * (m2x + nx);
-        out.y += lq.x * cq * (m1y + ny) + lq.y * cq * (m2y + ny);
+        double cq = mu * gam;
+        out.x += cq * (lq.x * gqx.x + lq.y * gqy.x);
+        out.y += cq * (lq.x * gqx.y + lq.y * gqy.y);
     }
     int4 sg = m.vg[k];
     for (int j = 0; j < 3; j++) {
