@@ -228,42 +228,79 @@ int sevc_host_build(const sevc_options *opt, int nv, const double *xy, int nb, c
 #pragma omp parallel for schedule(static)
     for (int v = 0; v < nv; v++) order_boundaries(m, v, D);
 
-    {   /* face traversal, src/io.h:137-186.  The successor of every
-         * (vertex, side) half-edge is found in parallel first; the walk in
-         * the reference's order then only follows it. */
-        unsigned char *seen = (unsigned char *)calloc(3 * (size_t)nv, 1);
-        int *next = (int *)malloc(3 * (size_t)nv * sizeof(int));
-        if (!seen || !next) { free(seen); free(next); sevc_set_error("out of host memory"); goto bad; }
-#pragma omp parallel for schedule(static)
-        for (int h = 0; h < 3 * nv; h++) {
-            int cur = h / 3, b = m->vb[h];
+    {   /* face traversal, src/io.h:137-186.  The reference walks a face from
+         * the first of its (vertex, side) half-edges met in index order and
+         * numbers faces in that order; that half-edge is the smallest index
+         * on the face's cycle of successors.  So: every successor in
+         * parallel, every half-edge's cycle minimum by pointer doubling
+         * (7 rounds cover 128 >= the 100 vertices a grain may have), faces
+         * numbered by ascending minimum, and each face walked from its
+         * minimum, in parallel. */
+        size_t H = 3 * (size_t)nv;
+        int *next = (int *)malloc(H * sizeof(int)), *fid = (int *)malloc(H * sizeof(int));
+        int *j0 = (int *)malloc(H * sizeof(int)), *j1 = (int *)malloc(H * sizeof(int));
+        int *c0 = (int *)malloc(H * sizeof(int)), *c1 = (int *)malloc(H * sizeof(int));
+        int bad_next = 0, bad_walk = 0;
+        if (!next || !fid || !j0 || !j1 || !c0 || !c1) {
+            free(next); free(fid); free(j0); free(j1); free(c0); free(c1);
+            sevc_set_error("out of host memory");
+            goto bad;
+        }
+#pragma omp parallel for schedule(static) reduction(| : bad_next)
+        for (long long h = 0; h < (long long)H; h++) {
+            int cur = (int)(h / 3), b = m->vb[h];
             int nx = (m->bini[b] == cur) ? m->bend[b] : m->bini[b];
             int i = 0;
             while (i < 3 && m->vb[3 * nx + i] != b) i++;
             next[h] = i == 3 ? -1 : 3 * nx + (i + 1) % 3;
+            bad_next |= i == 3;
+            j0[h] = i == 3 ? (int)h : next[h];
+            c0[h] = (int)h;
+            fid[h] = -1;
         }
-        int ngr = 0;
-        for (int j = 0; j < nv && ngr >= 0; j++)
-            for (int side0 = 0; side0 < 3; side0++) {
-                if (seen[3 * j + side0]) continue;
-                if (ngr >= ng) { ngr = -1; break; }
-                int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * ngr];
-                int n = 0, h = 3 * j + side0;
+        for (int r = 0; r < 7; r++) {
+#pragma omp parallel for schedule(static)
+            for (long long h = 0; h < (long long)H; h++) {
+                int s = j0[h], a = c0[s];
+                c1[h] = a < c0[h] ? a : c0[h];
+                j1[h] = j0[s];
+            }
+            int *t = j0; j0 = j1; j1 = t;
+            t = c0; c0 = c1; c1 = t;
+        }
+        int ngr = 0;                                 /* faces in the reference's order */
+        for (size_t h = 0; h < H; h++)
+            if (c0[h] == (int)h) j1[h] = ngr++;
+        if (!bad_next && ngr == ng) {
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : bad_walk)
+            for (long long h0 = 0; h0 < (long long)H; h0++) {
+                if (c0[h0] != (int)h0) continue;
+                int g = j1[h0], n = 0, h = (int)h0, start = (int)(h0 / 3);
+                int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * g];
                 do {
-                    if (seen[h] || n >= SEVC_MAX_VRT_PER_GRN) { ngr = -2; break; }
-                    seen[h] = 1;
+                    if (n >= SEVC_MAX_VRT_PER_GRN || fid[h] >= 0) { bad_walk = 1; break; }
+                    fid[h] = g;
                     L[n++] = h / 3;
                     h = next[h];
-                    if (h < 0) { ngr = -2; break; }
-                } while (h / 3 != j);
-                if (ngr < 0) break;
+                } while (h / 3 != start);
                 for (int k = n; k < SEVC_MAX_VRT_PER_GRN; k++) L[k] = -1;
-                m->gvlen[ngr] = n;
-                m->gen[ngr] = 1;
-                ngr++;
+                m->gvlen[g] = n;
+                m->gen[g] = 1;
             }
-        free(seen);
-        free(next);
+            for (size_t h = 0; h < H && !bad_walk; h++) bad_walk |= fid[h] < 0;
+        }
+        if (!bad_next && !bad_walk && ngr == ng) {
+#pragma omp parallel for schedule(static)
+            for (int v = 0; v < nv; v++) {          /* src/io.h:196-200: slots in ascending grain order */
+                int a = fid[3 * v], b = fid[3 * v + 1], c = fid[3 * v + 2], t;
+                if (a > b) { t = a; a = b; b = t; }
+                if (b > c) { t = b; b = c; c = t; }
+                if (a > b) { t = a; a = b; b = t; }
+                m->vg[3 * v] = a; m->vg[3 * v + 1] = b; m->vg[3 * v + 2] = c;
+            }
+        }
+        free(next); free(fid); free(j0); free(j1); free(c0); free(c1);
+        if (bad_next || bad_walk) { sevc_set_error("inconsistent ridges: the faces do not close"); goto bad; }
         if (ngr != ng) {
             sevc_set_error("face traversal found %d grains, expected %d", ngr, ng);
             goto bad;
@@ -276,11 +313,6 @@ int sevc_host_build(const sevc_options *opt, int nv, const double *xy, int nb, c
     for (int v = 0; v < nv; v++) {
         int t = m->vb[3 * v + 1]; m->vb[3 * v + 1] = m->vb[3 * v]; m->vb[3 * v] = t;
     }
-    for (int g = 0; g < ng; g++)                  /* src/io.h:196-200 */
-        for (int k = 0; k < m->gvlen[g]; k++) {
-            int *s = &m->vg[3 * m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * g + k]];
-            if (s[0] < 0) s[0] = g; else if (s[1] < 0) s[1] = g; else if (s[2] < 0) s[2] = g;
-        }
     for (int g = 0; g < ng; g++) m->gori[g] = (g < n_ori ? oris[g] : 0.0) * 2 * M_PI; /* :214-218 */
     for (int g = 0; g < ng; g++) m->gse[g] = g < n_se ? se[g] : 0.0;                   /* :223 */
     if (opt->SE_min == 999 && opt->SE_max == 999) {                                    /* :228-248 */
