@@ -19,11 +19,12 @@ metric = sum over timed steps of the enabled vertices / time.
            K steps with the per-step summary read back, download of the
            final state - all inside the timed region;
   roofline per-kernel CUDA-event times from a profiling pass of the same
-           workload; algorithmic bytes per launch are stated in the design doc.
+           workload; algorithmic bytes per launch are KERNEL_BYTES below.
 
 --impl reference times the reference's algorithm on the host cores: the
-oracle restatement (the reference's CUDA program cannot run on the GPU machine:
-its sources are not there and binaries built elsewhere are x86).
+oracle restatement (the reference's CUDA program cannot run where the
+benchmark runs: its sources are not there and binaries built elsewhere are
+x86).
 """
 import argparse
 import json
@@ -288,7 +289,7 @@ def algorithmic_bytes_per_step(nv):
     return 131.5 * nv
 
 
-# algorithmic bytes per unit for each kernel (kernel table)
+# algorithmic bytes per unit for each kernel phase (compulsory traffic, each datum once)
 KERNEL_BYTES = {
     # per grain: list 4*vlen + vlen/SE/area/gq/enabled 29 + positions 16*V/G + grain
     # slots of the listed vertices 16*V/G + stored-energy terms 48*V/G
@@ -301,9 +302,9 @@ KERNEL_BYTES = {
 }
 
 # DRAM bytes (read + write) per unit measured by ncu for each kernel phase on
-# the 200K-grain mesh (profiles/k_grain_fd_sorted_200k_grains.md,
-# profiles/k_vertex_fd_200k_grains.md); traffic grows with the units
-# processed, so a full launch is scaled by its units.
+# the 200K-grain mesh (the ncu summaries of k_grain_fd_sorted and
+# k_vertex_fd under profiles/); traffic grows with the units processed, so
+# a full launch is scaled by its units.
 NCU_TRAFFIC_PER_UNIT = {
     "grain_fd": (52.14e6 + 8.06e6) / 200000,
     "vertex_fd": (54.86e6 + 1.71e6) / 400000,

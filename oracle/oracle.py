@@ -1,8 +1,9 @@
 """ctypes binding of the C oracle (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module, as the checker.  The product (the CUDA
-library and its C ABI) never loads the oracle.
+``bench.py`` import this module, to compare results against and to time
+the host baseline.  The product (the CUDA library and its C ABI) never
+loads the oracle.
 """
 import ctypes as C
 import os

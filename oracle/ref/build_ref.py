@@ -12,7 +12,8 @@ stand-in), and link the runtime ``harness_rt.cpp``.  Only the executable
 
 The executable is ``sevc_ref -c file.ini``: the reference program itself,
 running its main loop on one CPU core.  The reference has no tests or golden
-vectors; its outputs from this build pin the oracle (tests/golden).
+vectors; the outputs of this compiled reference pin the oracle
+(tests/golden).
 """
 import os
 import re
