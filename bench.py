@@ -311,6 +311,9 @@ NCU_TRAFFIC_PER_UNIT = {
 }
 # FP64 pipe activity of the same captures (of elapsed cycles)
 NCU_FP64_ACTIVE = {"grain_fd": 0.726, "vertex_fd": 0.783}
+# DADD + DMUL + DFMA thread instructions per unit in the same captures
+# (thread instructions per elapsed cycle x elapsed cycles / units)
+NCU_FP64_INST_PER_UNIT = {"grain_fd": 206.1 * 397143 / 200000, "vertex_fd": 233.8 * 388213 / 400000}
 
 
 def run_engine(args):
@@ -359,6 +362,13 @@ def run_engine(args):
     except OSError:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
+    fp64_peak = sevc.measure_fp64_rate()
+    fp64 = {}
+    for k in ("grain_fd", "vertex_fd"):
+        if k in prof and prof[k][1]:
+            u = {"grains": g, "vertices": 2 * g, "boundaries": 3 * g}[KERNEL_BYTES[k][0]]
+            ach = NCU_FP64_INST_PER_UNIT[k] * u / (prof[k][0] / prof[k][1] / 1e3)
+            fp64[k] = {"achieved": ach, "frac": ach / fp64_peak}
 
     # ---------------- end-to-end leg through the C ABI ----------------
     e0 = time.time()
@@ -398,6 +408,11 @@ def run_engine(args):
                      "fp64_pipe_active_ncu": NCU_FP64_ACTIVE.get(dom),
                      "note": "FP64-issue bound on GB300 (DRAM idle); fp64_pipe_active_ncu is the fraction "
                              "of elapsed cycles the FP64 pipe was busy in the ncu capture"},
+        "roofline_fp64": {"bound": "fp64", "unit": "FP64 thread-instructions/s", "peak": fp64_peak,
+                          "peak_source": "sevc_measure_fp64_rate (independent DFMA chains, this GPU, now)",
+                          "kernels": fp64,
+                          "inst_per_unit_source": "ncu DADD+DMUL+DFMA thread instructions per grain / vertex "
+                                                  "on the 200K-grain mesh"},
         "kernel_ms_share": {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "step_bytes_rate_gbs": algorithmic_bytes_per_step(2 * n) * args.steps / (ms / 1e3) / 1e9,
         "gpu_launches": sum(i.kernel_launches for i in infos),

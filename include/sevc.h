@@ -283,6 +283,12 @@ sevc_status sevc_get_profile(sevc_handle *h, int max_entries, char (*names)[48],
  * than printf; used by sevc_export_text. */
 int sevc_format_fixed16(double x, char *out);
 
+/* The FP64 multiply-add issue rate of the current device, in thread
+ * operations per second (independent chains, CUDA events); the roofline
+ * that binds the finite-difference kernels.  No counterpart in the
+ * reference. */
+sevc_status sevc_measure_fp64_rate(double *ops_per_s);
+
 /* Text of the last error on this thread. */
 const char *sevc_last_error(void);
 

@@ -7,6 +7,7 @@
  * is not followed, so a damaged mesh is reported, never read out of bounds.
  */
 #include "sevc_internal.h"
+#include "sevc_host.h"
 
 namespace {
 
@@ -115,7 +116,49 @@ __global__ void k_check_grains(DevMesh m, int *out)
     add_count(out, bad);
 }
 
+/* FP64 issue-rate probe: 8 independent fused multiply-add chains per
+ * thread, so the pipe, not latency, limits the rate */
+__global__ void k_fp64_rate(int iters, double a, double b, double *sink)
+{
+    double x[8];
+    for (int k = 0; k < 8; k++) x[k] = threadIdx.x * 1e-3 + k;
+    for (int i = 0; i < iters; i++)
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, b);
+    double s = 0;
+    for (int k = 0; k < 8; k++) s += x[k];
+    if (s == 12345.678) *sink = s;   /* keeps the chains live */
+}
+
 } // namespace
+
+/* FP64 multiply-add instructions (thread operations) per second on the
+ * current device, measured with CUDA events */
+extern "C" sevc_status sevc_measure_fp64_rate(double *ops_per_s)
+{
+    if (!ops_per_s) return SEVC_ERR_ARG;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return SEVC_ERR_CUDA;
+    double *sink = nullptr;
+    cudaEvent_t e0, e1;
+    if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess) return SEVC_ERR_CUDA;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int blocks = nsm * 8, threads = 256, iters = 4096;
+    COUNT_LAUNCHES(1), k_fp64_rate<<<blocks, threads>>>(64, 1.0000001, 1e-9, sink);   /* warm-up */
+    cudaEventRecord(e0);
+    COUNT_LAUNCHES(1), k_fp64_rate<<<blocks, threads>>>(iters, 1.0000001, 1e-9, sink);
+    cudaEventRecord(e1);
+    float ms = 0;
+    bool ok = cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (!ok) return SEVC_ERR_CUDA;
+    *ops_per_s = (double)blocks * threads * iters * 8 / (ms * 1e-3);
+    return SEVC_OK;
+}
 
 void launch_check(const DevMesh &m, int *out, cudaStream_t s)
 {

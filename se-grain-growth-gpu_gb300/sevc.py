@@ -25,7 +25,7 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_export_instance_text", "sevc_set_mobility", "sevc_set_gb_scaling", "sevc_set_stored_energy",
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
            "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
-           "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs"]
+           "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs", "sevc_measure_fp64_rate"]
 
 
 class SevcError(RuntimeError):
@@ -177,6 +177,15 @@ def check_mesh_host(arrs):
     L = lib()
     L.sevc_host_check.argtypes = [C.POINTER(MeshHost)]
     return int(L.sevc_host_check(C.byref(mh)))
+
+
+def measure_fp64_rate():
+    """FP64 multiply-add thread operations per second of the current GPU."""
+    r = C.c_double()
+    L = lib()
+    L.sevc_measure_fp64_rate.argtypes = [C.POINTER(C.c_double)]
+    _check(L.sevc_measure_fp64_rate(C.byref(r)))
+    return r.value
 
 
 def format_fixed16(x):
