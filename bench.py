@@ -151,6 +151,7 @@ def run_ensemble(n_inst, lo, hi, steps, warmup, seed=7, cache=None):
     g = sum(grains)
     for _ in range(warmup):
         g = batch.step().curr_n_grains
+    shapes = batch.autotune(2)
     vs, ms = 0, 0.0
     w0 = time.time()
     for _ in range(steps):
@@ -178,6 +179,7 @@ def run_ensemble(n_inst, lo, hi, steps, warmup, seed=7, cache=None):
             "batch_device_ms_per_step": ms / steps, "sequential_ms_per_step": 1e3 * seq_wall / steps,
             "batch_vertex_steps_per_s": vs / batch_wall, "sequential_vertex_steps_per_s": seq_vs / seq_wall,
             "speedup": seq_wall / batch_wall, "mesh_generation_s": round(gen_s, 1),
+            "batch_launch_shapes": list(shapes),
             "timing": "wall clock around the steps, inputs resident on the device"}
 
 
@@ -330,6 +332,7 @@ def run_engine(args):
     g = n
     for _ in range(args.warmup):
         g = eng.step().curr_n_grains
+    shapes = eng.autotune(3)          # launch shapes for this mesh; the state is left as it was
     clocks = Clocks()
     clocks.start()
     ms, vsteps, infos = 0.0, 0, []
@@ -396,7 +399,10 @@ def run_engine(args):
                    "removals_per_step": sum(i.n_removals for i in infos) / len(infos),
                    "flips_per_step": sum(i.n_flips for i in infos) / len(infos),
                    "nucleation_attempts": sum(i.nucleation_attempted for i in infos),
-                   "mesh_generation_s": round(gen_s, 1), "wall_s": round(wall, 3)},
+                   "mesh_generation_s": round(gen_s, 1), "wall_s": round(wall, 3),
+                   "launch_shapes": {"tpb_vertex": shapes[0], "tpb_boundary": shapes[1], "wide_sides": shapes[2],
+                                     "picked_by": "sevc_autotune, 3 steps per candidate"},
+                   "launch_mode": "CUDA graphs"},
         "e2e": {"value": e_vsteps / e_wall, "unit": UNIT, "h2d_bytes_per_step": host_bytes / args.steps,
                 "d2h_bytes_per_step": step_info_bytes + state_bytes / args.steps},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -271,6 +271,14 @@ sevc_status sevc_set_exact_all(sevc_handle *h, int on);
  * Profiling and adjoint replays always launch directly. */
 sevc_status sevc_set_graphs(sevc_handle *h, int on);
 
+/* Launch-shape autotuner (no counterpart in the reference): times `steps`
+ * steps from the current state for each candidate block size of the
+ * vertex pass (128/256/512) and of the per-boundary passes, and each side
+ * count from which grains get a warp each (9..12), one parameter at a
+ * time, keeps the fastest and restores the state.  chosen (3 ints, may be
+ * NULL) receives them.  Results never depend on these shapes. */
+sevc_status sevc_autotune(sevc_handle *h, int steps, int *chosen);
+
 /* Per-kernel device time accumulated while profiling is on (CUDA events
  * around each launch on the handle's stream). */
 sevc_status sevc_set_profiling(sevc_handle *h, int on);

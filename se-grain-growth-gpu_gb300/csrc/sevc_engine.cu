@@ -444,20 +444,20 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
     cudaMemsetAsync(m.gexact, 0, (size_t)h->ng, s);
     launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
-    { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :124-130 */
+    { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :124-130 */
     if (nucleation) {
         { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
-        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, s); } /* :171-181 */
+        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :171-181 */
     }
-    { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, s); }                                         /* :127,:203 */
-    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, s); }                                 /* :133,:203 */
+    { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, h->p.shape, s); }                                         /* :127,:203 */
+    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, h->p.shape, s); }                                 /* :133,:203 */
     /* The first count of the 2x3 loop (:228) depends only on the topology,
      * which nothing changes before that loop: count now, and decide on the
      * device whether this step must compute every output-only value. */
     { Prof pr(h, "two_three_count"); launch_two_three_first(m, x, x.list_b, x.n_b, s); }
     launch_full_flag(x, s);
     { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }                                     /* :206 */
-    { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, s); }                               /* :212-216 */
+    { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, h->p.shape, s); }                               /* :212-216 */
     { Prof pr(h, "snapshot"); launch_snapshot(m, x, s); }
     { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
     cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
@@ -1032,6 +1032,62 @@ sevc_status sevc_set_gb_scaling(sevc_handle *h, double s)
     h->opt.GB_scaling = s;
     h->p.scaling = s;
     drop_graphs(h);
+    return SEVC_OK;
+}
+
+/* Launch-shape autotuner: coordinate search over the vertex-pass block
+ * size, the per-boundary block size and the side count from which grains
+ * get a warp each, timing `steps` steps (device time) per candidate from
+ * the same saved state; the state is restored afterwards, and results do
+ * not depend on the shapes. */
+sevc_status sevc_autotune(sevc_handle *h, int steps, int *chosen)
+{
+    if (!h || steps < 1 || h->tape.every > 0) return SEVC_ERR_ARG;
+    void *saved = nullptr;
+    if (!cuda_ok(cudaMalloc(&saved, h->dbytes), "cudaMalloc") ||
+        !cuda_ok(cudaMemcpyAsync(saved, h->dblock, h->dbytes, cudaMemcpyDeviceToDevice, h->stream), "copy"))
+        return SEVC_ERR_CUDA;
+    RunState r0 = save_run(h);
+    int oc = h->outputs_complete;
+    auto trial = [&](double *ms) -> sevc_status {
+        drop_graphs(h);
+        if (!cuda_ok(cudaMemcpyAsync(h->dblock, saved, h->dbytes, cudaMemcpyDeviceToDevice, h->stream), "copy"))
+            return SEVC_ERR_CUDA;
+        load_run(h, r0);
+        sevc_step_info inf;
+        sevc_status st = sevc_step(h, &inf);          /* captures the graphs */
+        *ms = 0;
+        for (int k = 0; k < steps && !st; k++) {
+            st = sevc_step(h, &inf);
+            *ms += inf.gpu_ms;
+        }
+        return st;
+    };
+    LaunchShape &sh = h->p.shape;
+    int *fields[3] = { &sh.tpb_vertex, &sh.tpb_boundary, &sh.wide_sides };
+    const std::vector<int> cands[3] = { { 128, 256, 512 }, { 128, 256, 512 }, { 9, 10, 11, 12 } };
+    sevc_status st = SEVC_OK;
+    for (int f = 0; f < 3 && !st; f++) {
+        int best = *fields[f];
+        double best_ms = 1e300;
+        for (int v : cands[f]) {
+            *fields[f] = v;
+            double ms = 0;
+            st = trial(&ms);
+            if (st) break;
+            if (ms < best_ms) { best_ms = ms; best = v; }
+        }
+        *fields[f] = best;
+    }
+    drop_graphs(h);
+    bool ok = cuda_ok(cudaMemcpyAsync(h->dblock, saved, h->dbytes, cudaMemcpyDeviceToDevice, h->stream), "copy") &&
+              cuda_ok(cudaStreamSynchronize(h->stream), "sync");
+    cudaFree(saved);
+    load_run(h, r0);
+    h->outputs_complete = oc;
+    if (st) return st;
+    if (!ok) return SEVC_ERR_CUDA;
+    if (chosen) { chosen[0] = sh.tpb_vertex; chosen[1] = sh.tpb_boundary; chosen[2] = sh.wide_sides; }
     return SEVC_OK;
 }
 

@@ -159,17 +159,16 @@ __device__ __noinline__ void grain_fd_generic(const DevMesh &m, int g, const int
     }
 }
 
-/* grain pass over the grains of fewer than WIDE_SIDES sides, ordered by
+/* grain pass over the grains of fewer than `wide` sides (11 by default), ordered by
  * side count (warps see one N), most sides first so that the longest
  * blocks start in the first wave.  The pass is FP64-latency bound:
  * capping registers at 128 (4 blocks of 128 per SM) measured 9% faster on
  * the 1M-grain mesh than the compiler's 218-register choice, despite a few
  * spills; an 80-register cap gained nothing more. */
-constexpr int WIDE_SIDES = 11;
-__global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int *perm, const int *vbucket)
+__global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int *perm, const int *vbucket, int wide)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int total = vbucket[VB_START(WIDE_SIDES)];
+    int total = vbucket[VB_START(wide)];
     if (i >= total) return;
     int g = perm[total - 1 - i];
     const int *L = m.glist + (size_t)SEVC_MAXV * g;
@@ -207,7 +206,7 @@ __device__ __forceinline__ double area_shared(const double2 *P, int n, int ps, d
     return area * 0.5;
 }
 
-/* grain pass over the grains of WIDE_SIDES or more sides (the tail of the
+/* grain pass over the grains of `wide` or more sides (the tail of the
  * side-count order): one warp per grain, polygon staged in shared memory.
  * The 2n+1 areas of a grain (vertex p moved along x: task 2p, along y:
  * task 2p+1, unmoved: task 2n) are spread over the lanes, so a grain of
@@ -216,14 +215,14 @@ __device__ __forceinline__ double area_shared(const double2 *P, int n, int ps, d
  * whole pass. */
 constexpr int WIDE_WARPS = 4;
 __global__ void __launch_bounds__(32 * WIDE_WARPS) k_grain_fd_wide(DevMesh m, const int *perm, const int *vbucket,
-                                                                  const int *total)
+                                                                  const int *total, int wide)
 {
     __shared__ double2 poly[WIDE_WARPS][SEVC_MAXV];
     __shared__ double area[WIDE_WARPS][2 * SEVC_MAXV + 1];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     double2 *P = poly[w];
     double *R = area[w];
-    int first = vbucket[VB_START(WIDE_SIDES)], end = *total;
+    int first = vbucket[VB_START(wide)], end = *total;
     int nwarps = gridDim.x * WIDE_WARPS;
     const double D = m.D;
     for (int i = first + blockIdx.x * WIDE_WARPS + w; i < end; i += nwarps) {
@@ -609,24 +608,26 @@ __global__ void k_nucl_area_final(const double *block_out, int nblocks, int nins
 
 } // namespace
 
-void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s)
+void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, const LaunchShape &sh, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_boundary_geometry<<<nblk(m.nb), TPB, 0, s>>>(m, eps, scaling);
+    int t = sh.tpb_boundary;
+    COUNT_LAUNCHES(1), k_boundary_geometry<<<(m.nb + t - 1) / t, t, 0, s>>>(m, eps, scaling);
 }
-void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s)
+void launch_grain_fd(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
     COUNT_LAUNCHES(1), k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
     COUNT_LAUNCHES(1), k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
-    COUNT_LAUNCHES(1), k_grain_fd_wide<<<2 * 152, 32 * WIDE_WARPS, 0, s>>>(m, x.perm, x.vbucket, x.n_perm);
-    COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.vbucket);
+    COUNT_LAUNCHES(1), k_grain_fd_wide<<<2 * 152, 32 * WIDE_WARPS, 0, s>>>(m, x.perm, x.vbucket, x.n_perm, sh.wide_sides);
+    COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
 }
 
 /* the unsorted per-grain pass, kept for A/B timing */
 void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s)
+void launch_vertex_fd(const DevMesh &m, double mu, const LaunchShape &sh, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_vertex_fd<<<nblk(m.nv), TPB, 0, s>>>(m, mu);
+    int t = sh.tpb_vertex;
+    COUNT_LAUNCHES(1), k_vertex_fd<<<(m.nv + t - 1) / t, t, 0, s>>>(m, mu);
 }
 void launch_full_flag(const DevScratch &x, cudaStream_t s)
 {
@@ -641,9 +642,10 @@ void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_snapshot<<<4 * 152, TPB, 0, s>>>(m, x.flags);
 }
-void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s)
+void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_text_label<<<nblk(m.nb), TPB, 0, s>>>(m, dt, 1.0 / dt, x.flags);
+    int t = sh.tpb_boundary;
+    COUNT_LAUNCHES(1), k_text_label<<<(m.nb + t - 1) / t, t, 0, s>>>(m, dt, 1.0 / dt, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)

@@ -9,7 +9,6 @@
 #include "sevc_device.cuh"
 #include <curand_kernel.h>
 
-/* scratch shared by launches of one handle */
 /* Scratch shared by launches of one handle.  Arrays marked "per instance"
  * hold one block for each instance of a batched handle. */
 struct DevScratch {
@@ -49,18 +48,26 @@ enum {
 };
 #define CTR_NUCL_AREA_SLOT 8 /* double stored at counters + 8 (two ints) */
 
+/* launch shapes the autotuner may change (results do not depend on them) */
+struct LaunchShape {
+    int tpb_vertex = 256;    /* threads per block of the vertex pass */
+    int tpb_boundary = 256;  /* of the per-boundary passes (geometry, t_ext) */
+    int wide_sides = 11;     /* grains of this many sides or more get a warp each */
+};
+
 struct StepParams {
     double dt, eps, scaling, MC_k;
     int n_blocks, n_threads; /* reference launch grid, drives observable partitions */
     int ninst;               /* instances in the handle */
     int max_inst_ng;         /* grains of the largest instance */
     double mu;               /* mobility (velocity factor); 1 in the reference */
+    LaunchShape shape;
 };
 
 /* geometry (sevc_geometry.cu) */
-void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cudaStream_t s);
-void launch_grain_fd(const DevMesh &m, const DevScratch &x, cudaStream_t s);
-void launch_vertex_fd(const DevMesh &m, double mu, cudaStream_t s);
+void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, const LaunchShape &sh, cudaStream_t s);
+void launch_grain_fd(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s);
+void launch_vertex_fd(const DevMesh &m, double mu, const LaunchShape &sh, cudaStream_t s);
 /* side-count histogram layout in DevScratch::vbucket */
 #define VB_START(b) (32 + (b))
 #define VB_COUNT(b) (48 + (b))
@@ -70,7 +77,7 @@ void launch_full_flag(const DevScratch &x, cudaStream_t s);
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 /* copies pos, vel, bv to pos0, vel0, bv0 unless the step computes every output */
 void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s);
-void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s);
+void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s);
 void launch_grain_area(const DevMesh &m, cudaStream_t s);
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s);

@@ -25,7 +25,8 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_export_instance_text", "sevc_set_mobility", "sevc_set_gb_scaling", "sevc_set_stored_energy",
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
            "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
-           "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs", "sevc_measure_fp64_rate"]
+           "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs", "sevc_measure_fp64_rate",
+           "sevc_autotune"]
 
 
 class SevcError(RuntimeError):
@@ -404,6 +405,13 @@ class Engine:
     def set_exact_all(self, on):
         lib().sevc_set_exact_all.argtypes = [C.c_void_p, C.c_int]
         _check(lib().sevc_set_exact_all(self._h, 1 if on else 0))
+
+    def autotune(self, steps=5):
+        """Pick launch shapes by timing; returns (tpb_vertex, tpb_boundary, wide_sides)."""
+        out = (C.c_int * 3)()
+        lib().sevc_autotune.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _check(lib().sevc_autotune(self._h, steps, out))
+        return tuple(out)
 
     def set_graphs(self, on):
         lib().sevc_set_graphs.argtypes = [C.c_void_p, C.c_int]

@@ -109,3 +109,30 @@ def test_graph_replay_matches_direct_launches(gpu, tmp_path):
     assert nucl > 0
     for e in engines:
         e.close()
+
+
+def test_autotune_keeps_state_and_results(gpu):
+    """The autotuner leaves the run where it was, and steps with the shapes
+    it picks equal steps with the default shapes, bit for bit."""
+    import meshgen
+    mesh = meshgen.make_inputs(3000, 77, se="triangular")
+    o = nucl_options(gpu, 3000)
+    o.do_nucleation = 0
+    o.domain_bound = 55.0
+    a = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    b = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    for _ in range(20):
+        a.step()
+        b.step()
+    chosen = a.autotune(steps=3)
+    assert chosen[0] in (128, 256, 512) and chosen[1] in (128, 256, 512) and 9 <= chosen[2] <= 12
+    assert same_state(a.get_state(), b.get_state()) is None
+    events = 0
+    for k in range(60):
+        ia, ib = a.step(), b.step()
+        assert (ia.n, ia.curr_n_grains, ia.n_flips, ia.n_removals) == (ib.n, ib.curr_n_grains, ib.n_flips, ib.n_removals)
+        events += ia.n_flips + ia.n_removals
+    assert same_state(a.get_state(), b.get_state()) is None
+    assert events > 0
+    a.close()
+    b.close()
