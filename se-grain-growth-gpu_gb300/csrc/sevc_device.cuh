@@ -272,6 +272,66 @@ __device__ __forceinline__ double text_exact(double2 pi, double2 pe, double2 vi,
     return (aux == 0) ? 100 : -norm / aux;
 }
 
+/* binary64 -> binary32 by cutting the significand, on the integer pipe:
+ * for 2^-126 <= |x| < 2^128 the result has x's sign and
+ * (1 - 2^-23)|x| < |r| <= |x|; smaller |x| give +-0 (error < 2^-126);
+ * larger or non-finite x give NaN, which fails every comparison. */
+__device__ __forceinline__ float f32_cut(double x)
+{
+    unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    unsigned e = (hi >> 20) & 0x7ffu;
+    unsigned mag = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    mag = e <= 896u ? 0u : mag;
+    mag = e >= 1151u ? 0x7fc00000u : mag;
+    return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
+/* True when compute_t_ext (src/topological.h:303-334) of the boundary
+ * from pi to pe, ends moving at vi, ve, is certainly outside [0, dt]
+ * (dt < 100), decided in binary32 so that the FP64 pipe stays free.
+ *
+ * With d = wrapped pe - pi and p = ve - vi, the reference's t_ext is
+ * -|d|^2 / (d.p) up to relative rounding of order 1e-15 (the unit
+ * tangent comes from atan2/cos/sin), and 100 when d.p rounds to 0; it is
+ * a candidate only if s + |d|^2/dt <= 0 for s = d.p, within that
+ * rounding.  Every input is cut to binary32 (f32_cut, relative error
+ * below 2^-23, plus 2^-126 absolute for tiny values), and each binary32
+ * quantity carries a bound on its distance from the exact value:
+ *   |X - dx| <= ex = 2.5e-7 (|pe.x| + |pi.x| + D) + 1e-37 (two cuts,
+ *     the rounded difference and, after a wrap, the cut D and one more
+ *     rounding: at most 1.5 * 2^-23 of the same sum), same for y;
+ *   |P - px| <= 2.5e-7 (|ve.x| + |vi.x|) + 1e-37, same for y;
+ *   |S - s| <= A Ep + B Ex and |N - |d|^2| <= 2 A Ex, with Ex, Ep the
+ *     summed bounds, A = |X| + |Y| + Ex >= |dx| + |dy| and
+ *     B = |P| + |Q| + Ep >= |px| + |py|.
+ * The rounding of the binary32 evaluation itself (a few 2^-24 of
+ * A B + N/dt) and the reference's own rounding fit in the further
+ * 1e-6 (A B + (N + 2 A Ex)/dt), and 1.001 covers the rounding of the bound.
+ * The wrap (wrap_dist, |d| > D/2) is decided the reference's way only
+ * outside a band of relative width 1e-5 plus ex around D/2; inside it,
+ * for |d|^2 below 1e-30 and for NaN or overflow the answer is false, and
+ * the caller computes t_ext exactly. */
+__device__ __forceinline__ bool text_outside_dt(double2 pi, double2 pe, double2 vi, double2 ve, float Df, float hDf,
+                                                float inv_dt)
+{
+    float ax = f32_cut(pe.x), bx = f32_cut(pi.x), ay = f32_cut(pe.y), by = f32_cut(pi.y);
+    float X = ax - bx, Y = ay - by;
+    float ex = 2.5e-7f * (fabsf(ax) + fabsf(bx) + Df) + 1e-37f;
+    float ey = 2.5e-7f * (fabsf(ay) + fabsf(by) + Df) + 1e-37f;
+    float lo = 0.99999f * hDf, hi = 1.00001f * hDf, aX = fabsf(X), aY = fabsf(Y);
+    if ((aX > lo - ex && aX < hi + ex) || (aY > lo - ey && aY < hi + ey)) return false;
+    if (X > hDf) X = X - Df; else if (X < -hDf) X = X + Df;
+    if (Y > hDf) Y = Y - Df; else if (Y < -hDf) Y = Y + Df;
+    float vex = f32_cut(ve.x), vix = f32_cut(vi.x), vey = f32_cut(ve.y), viy = f32_cut(vi.y);
+    float P = vex - vix, Q = vey - viy;
+    float Ex = ex + ey, Ep = 2.5e-7f * (fabsf(vex) + fabsf(vix) + fabsf(vey) + fabsf(viy)) + 2e-37f;
+    float A = fabsf(X) + fabsf(Y) + Ex, B = fabsf(P) + fabsf(Q) + Ep;
+    float S = X * P + Y * Q, N = X * X + Y * Y;
+    float ni = N * inv_dt, ai = 2.0f * A * Ex * inv_dt;
+    float E = A * Ep + B * Ex + ai + 1e-6f * (A * B + ni + ai);
+    return N > 1e-30f && S + ni > 1.001f * E;
+}
+
 /* compute_dAdt (src/geometry.h:779-787) of grain g over its list, with the
  * given positions and velocities */
 __device__ __forceinline__ double dadt_from(const DevMesh &m, int g, const double2 *pos, const double2 *vel)

@@ -430,38 +430,30 @@ __device__ void dadt_of(const DevMesh &m, int g)
  *   margin = 1e-12 |d|^2/dt + 1e-14 (|dx|+|dy|)(|Px|+|Py|) + 1e-15 (|dx Px| + |dy Py|)
  * (each term at least five times the error it covers) it is not one.
  */
-__global__ void k_text_label(DevMesh m, double dt, double inv_dt, const int *flags)
+__global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, const int *flags)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= m.nb) return;
-    double text = m.btext[b];
+    double text;
     if (m.ben[b]) {
         int2 e = m.bv[b];
         double2 pi = m.pos[e.x], pe = m.pos[e.y];
         double2 vi = m.vel[e.x], ve = m.vel[e.y];
-        if (!flags[0]) {
-            double dx = 0.0 + wrapd(pe.x, pi.x, m.D);
-            double dy = 0.0 + wrapd(pe.y, pi.y, m.D);
-            double px = ve.x - vi.x, py = ve.y - vi.y;
-            double s = dx * px + dy * py;
-            double n2 = dx * dx + dy * dy;
-            double thr = -(n2 * inv_dt);
-            double margin = 1e-12 * (n2 * inv_dt) + 1e-14 * (dabs(dx) + dabs(dy)) * (dabs(px) + dabs(py)) +
-                            1e-15 * (dabs(dx * px) + dabs(dy * py));
-            if (n2 > 0 && s > thr + margin) {
-                /* not a candidate: its t_ext is outside [0, dt]; the value
-                 * itself is only observed if an event disables the
-                 * boundary, which then computes it (finalize_boundary) */
-                m.btext[b] = SEVC_MAX_T_EXT_D;
-                m.bexact[b] = 0;
-                m.bcand[b] = 0;
-                m.bconf[b] = -1;
-                return;
-            }
+        if (!flags[0] && text_outside_dt(pi, pe, vi, ve, Df, hDf, inv_dt)) {
+            /* not a candidate: its t_ext is outside [0, dt]; the value
+             * itself is only observed if an event disables the boundary,
+             * which then computes it (finalize_boundary) */
+            m.btext[b] = SEVC_MAX_T_EXT_D;
+            m.bexact[b] = 0;
+            m.bcand[b] = 0;
+            m.bconf[b] = -1;
+            return;
         }
         text = text_exact(pi, pe, vi, ve, m.D);
         m.btext[b] = text;
         m.bexact[b] = 1;
+    } else {
+        text = m.btext[b];
     }
     m.bcand[b] = (text >= 0 && text <= dt) ? 1 : 0;
     m.bconf[b] = -1;
@@ -645,7 +637,10 @@ void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s)
 {
     int t = sh.tpb_boundary;
-    COUNT_LAUNCHES(1), k_text_label<<<(m.nb + t - 1) / t, t, 0, s>>>(m, dt, 1.0 / dt, x.flags);
+    /* binary32 copies for the certificate (text_outside_dt): rounded to
+     * nearest, within 2^-24 of the binary64 values */
+    float Df = (float)m.D, hDf = (float)(m.D / 2.0), inv_dt = (float)(1.0 / dt);
+    COUNT_LAUNCHES(1), k_text_label<<<(m.nb + t - 1) / t, t, 0, s>>>(m, dt, Df, hDf, inv_dt, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
