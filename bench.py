@@ -313,9 +313,9 @@ NCU_TRAFFIC_PER_UNIT = {
 }
 # FP64 pipe activity of the same captures (of elapsed cycles)
 NCU_FP64_ACTIVE = {"grain_fd": 0.726, "vertex_fd": 0.783}
-# DADD + DMUL + DFMA thread instructions per unit in the same captures
-# (thread instructions per elapsed cycle x elapsed cycles / units)
-NCU_FP64_INST_PER_UNIT = {"grain_fd": 206.1 * 397143 / 200000, "vertex_fd": 233.8 * 388213 / 400000}
+# DADD + DMUL + DFMA thread instructions per unit, ncu counters on the
+# 200K-grain mesh (the FP64 instruction summary kept with the profiles)
+NCU_FP64_INST_PER_UNIT = {"grain_fd": (78.278649e6 + 1.070703e6) / 200000, "vertex_fd": 85.99771e6 / 400000}
 
 
 def run_engine(args):

@@ -89,10 +89,15 @@ struct DevMesh {
      * every entity only on steps that can export; on other steps the values
      * of entities an event disables are computed at that moment from the
      * positions, velocities and boundary ends the step started its events
-     * with (pos0, vel0, bv0, copied after the labels).  bexact / gexact say
-     * which values are already exact this step. */
+     * with.  Events save those before they first overwrite them in a step
+     * (save_vertex, save_ends): pos0 / vel0 / bv0 hold the saved values
+     * and vstamp / bstamp the step stamp (*stamp, advanced once per step)
+     * under which they were saved; an entry with an older stamp is stale
+     * and the live value is still the step's starting one.  bexact /
+     * gexact say which values are already exact this step. */
     double2 *pos0, *vel0;
     int2 *bv0;
+    unsigned *vstamp, *bstamp, *stamp;
     uint8_t *bexact, *gexact;
     uint8_t *bmark;      /* boundaries marked by a sparse pass, compacted next */
 };
@@ -144,10 +149,59 @@ __device__ __forceinline__ double dmod(double a, double D)        /* dom_mod :13
     else if (b >= dbits(D)) return a - D;                         /* a >= D (D > 0) */
     return a;
 }
+/* Exact scalings and divisions kept off the FP64 pipe (on GB300 one FP64
+ * operation costs as much issue time as dozens of integer ones).  The
+ * slow paths are calls, so that the compiler cannot turn the branch into
+ * predicated FP64 instructions that would occupy the pipe anyway. */
+static __device__ __noinline__ double dmul_slow(double x, double s) { return x * s; }
+static __device__ __noinline__ double ddiv_slow(double x, double y) { return x / y; }
+
+/* x * 2^-K (K = 1..3), exactly: an exponent decrement on the integer pipe
+ * when x and the result are normal, else the multiplication */
+template <int K> __device__ __forceinline__ double dscale_down(double x)
+{
+    long long b = dbits(x);
+    unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
+    if (ex > (unsigned)K && ex < 0x7ffu) return __longlong_as_double(b - ((long long)K << 52));
+    return dmul_slow(x, K == 1 ? 0.5 : (K == 2 ? 0.25 : 0.125));
+}
+
+/* x / N for a small integer N, correctly rounded, with one multiplication
+ * and one fma (Brisebarre, Muller and Raina, "Accelerating correctly
+ * rounded floating-point division when the divisor is known in advance",
+ * IEEE Trans. Computers 53(8), 2004): zh = RN(1/N), zl = RN(1/N - zh).
+ * The fma's exact argument x zh + RN(x zl) is within 2^-105.8 of x/N
+ * (relative, worst N = 7), while x/N, a 53-bit integer over N <= 10
+ * scaled by a power of two, is never within 2^-59 (relative) of a
+ * rounding midpoint: the fma returns RN(x/N).  Valid while x zl is normal
+ * and x/N finite, 2^-900 <= |x| < 2^900; other x divide.  N = 4 and 8 are
+ * exact scalings. */
+template <int N> struct InvSplit;
+template <> struct InvSplit<3> { static constexpr double hi = 0x1.5555555555555p-2, lo = 0x1.5555555555555p-56; };
+template <> struct InvSplit<5> { static constexpr double hi = 0x1.999999999999ap-3, lo = -0x1.999999999999ap-57; };
+template <> struct InvSplit<6> { static constexpr double hi = 0x1.5555555555555p-3, lo = 0x1.5555555555555p-57; };
+template <> struct InvSplit<7> { static constexpr double hi = 0x1.2492492492492p-3, lo = 0x1.2492492492492p-57; };
+template <> struct InvSplit<9> { static constexpr double hi = 0x1.c71c71c71c71cp-4, lo = 0x1.c71c71c71c71cp-58; };
+template <> struct InvSplit<10> { static constexpr double hi = 0x1.999999999999ap-4, lo = -0x1.999999999999ap-58; };
+template <int N> __device__ __forceinline__ double div_small(double x)
+{
+    if constexpr (N == 4) {
+        return dscale_down<2>(x);
+    } else if constexpr (N == 8) {
+        return dscale_down<3>(x);
+    } else {
+        long long b = dbits(x) & 0x7FFFFFFFFFFFFFFFLL;
+        if (b >= 0x07B0000000000000LL && b < 0x7830000000000000LL)
+            return __fma_rn(x, InvSplit<N>::hi, __dmul_rn(x, InvSplit<N>::lo));
+        return ddiv_slow(x, (double)N);
+    }
+}
+
 __device__ __forceinline__ double wrapd(double dest, double orig, double D) /* wrap_dist :147 */
 {
     double d = dest - orig;
-    long long b = dbits(d), h = dbits(D / 2.0);
+    /* D/2 by an exponent decrement (D is a positive normal domain bound) */
+    long long b = dbits(d), h = dbits(D) - (1LL << 52);
     if (b > h) return (d - D);                                    /* d > +D/2 */
     if (b < 0 && (b & SEVC_ABSMASK) > h) return (D + d);          /* d < -D/2 */
     return d;
@@ -161,6 +215,27 @@ __device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :
     double r = q / p;
     return p * sqrt(1.0 + r * r);
 }
+/* x / SEVC_GRAD_EPS_D, correctly rounded, with one multiplication and one
+ * fma instead of a division: the divisor y is known in advance
+ * (Brisebarre, Muller and Raina, "Accelerating correctly rounded
+ * floating-point division when the divisor is known in advance", IEEE
+ * Trans. Computers 53(8), 2004).  With zh = RN(1/y) (exactly 1e8) and
+ * zl = RN(1/y - zh), the fma's exact argument x zh + RN(x zl) is within
+ * 2^-107.4 of x/y (relative), while the quotient of two 53-bit
+ * significands is never within 2^-107 (relative) of a rounding midpoint,
+ * so the fma returns RN(x/y).  That holds while x zl stays normal and
+ * x/y finite: 2^-990 <= |x| < 2^990; other x (zero, tiny, huge,
+ * non-finite) take the division. */
+#define SEVC_INV_EPS_HI 0x1.7d784p+26
+#define SEVC_INV_EPS_LO (-0x1.1f8eb76e8p-29)
+__device__ __forceinline__ double div_grad_eps(double x)
+{
+    long long b = dbits(x) & SEVC_ABSMASK;
+    if (b >= 0x0210000000000000LL && b < 0x7DD0000000000000LL)
+        return __fma_rn(x, SEVC_INV_EPS_HI, __dmul_rn(x, SEVC_INV_EPS_LO));
+    return ddiv_slow(x, SEVC_GRAD_EPS_D);
+}
+
 /* compute_arclength(a, b) = |delta_to(a, b)|, :328 */
 __device__ __forceinline__ double arclen(double2 a, double2 b, double D)
 {
@@ -208,8 +283,7 @@ __device__ __forceinline__ double area_stream(const int *__restrict__ L, int n, 
         }
         area = add_closing_term(area, ax, ay);
     }
-    area *= 0.5;
-    return area;
+    return dscale_down<1>(area);
 }
 
 /* grains_intersect, src/geometry.h:837-848; returns count found */
@@ -332,18 +406,20 @@ __device__ __forceinline__ bool text_outside_dt(double2 pi, double2 pe, double2 
     return N > 1e-30f && S + ni > 1.001f * E;
 }
 
-/* compute_dAdt (src/geometry.h:779-787) of grain g over its list, with the
- * given positions and velocities */
-__device__ __forceinline__ double dadt_from(const DevMesh &m, int g, const double2 *pos, const double2 *vel)
+/* compute_dAdt (src/geometry.h:779-787) of grain g over its list; get(v,
+ * r, w) gives vertex v's position and velocity */
+template <class Get> __device__ __forceinline__ double dadt_over(const DevMesh &m, int g, Get get)
 {
     const int *L = m.glist + (size_t)SEVC_MAXV * g;
     int n = m.gvlen[g];
     double d = 0;
     if (n > 0) {
-        double2 r0 = pos[L[0]], v0 = vel[L[0]];
+        double2 r0, v0;
+        get(L[0], r0, v0);
         double ax = 0, ay = 0, rx = r0.x, ry = r0.y, vxk = v0.x, vyk = v0.y;
         for (int k = 1; k < n; k++) {
-            double2 r = pos[L[k]], w = vel[L[k]];
+            double2 r, w;
+            get(L[k], r, w);
             double nx = ax + wrapd(r.x, rx, m.D);
             double ny = ay + wrapd(r.y, ry, m.D);
             d += (vxk * ny + ax * w.y);
@@ -355,22 +431,59 @@ __device__ __forceinline__ double dadt_from(const DevMesh &m, int g, const doubl
     }
     return d;
 }
+__device__ __forceinline__ double dadt_from(const DevMesh &m, int g, const double2 *pos, const double2 *vel)
+{
+    return dadt_over(m, g, [&](int v, double2 &r, double2 &w) { r = pos[v]; w = vel[v]; });
+}
+
+/* an event is about to overwrite vertex v's position or velocity: keep
+ * the step's starting values (once per step) */
+__device__ __forceinline__ void save_vertex(const DevMesh &m, int v)
+{
+    unsigned st = *m.stamp;
+    if (m.vstamp[v] == st) return;
+    m.pos0[v] = m.pos[v];
+    m.vel0[v] = m.vel[v];
+    m.vstamp[v] = st;
+}
+/* an event is about to change boundary b's ends */
+__device__ __forceinline__ void save_ends(const DevMesh &m, int b)
+{
+    unsigned st = *m.stamp;
+    if (m.bstamp[b] == st) return;
+    m.bv0[b] = m.bv[b];
+    m.bstamp[b] = st;
+}
+/* position and velocity of vertex v when the step's events began */
+__device__ __forceinline__ void start_state(const DevMesh &m, int v, unsigned st, double2 &p, double2 &w)
+{
+    bool saved = m.vstamp[v] == st;
+    p = saved ? m.pos0[v] : m.pos[v];
+    w = saved ? m.vel0[v] : m.vel[v];
+}
 
 /* an event is about to disable boundary b: make its extinction time the
  * value the step's labels would have computed */
 __device__ __forceinline__ void finalize_boundary(const DevMesh &m, int b)
 {
     if (m.bexact[b]) return;
-    int2 e = m.bv0[b];
-    m.btext[b] = text_exact(m.pos0[e.x], m.pos0[e.y], m.vel0[e.x], m.vel0[e.y], m.D);
+    unsigned st = *m.stamp;
+    int2 e = m.bstamp[b] == st ? m.bv0[b] : m.bv[b];
+    double2 pi, pe, vi, ve;
+    start_state(m, e.x, st, pi, vi);
+    start_state(m, e.y, st, pe, ve);
+    m.btext[b] = text_exact(pi, pe, vi, ve, m.D);
     m.bexact[b] = 1;
 }
 /* an event is about to edit grain g's list (or disable it): its dA/dt as
- * the step computed it before any event */
+ * the step computed it before any event.  The list itself is still the
+ * step's: lists change only in the fix-up pass, after mark_fix has
+ * settled every grain it edits. */
 __device__ __forceinline__ void finalize_grain(const DevMesh &m, int g)
 {
     if (m.gexact[g]) return;
-    m.gdadt[g] = dadt_from(m, g, m.pos0, m.vel0);
+    unsigned st = *m.stamp;
+    m.gdadt[g] = dadt_over(m, g, [&](int v, double2 &r, double2 &w) { start_state(m, v, st, r, w); });
     m.gexact[g] = 1;
 }
 

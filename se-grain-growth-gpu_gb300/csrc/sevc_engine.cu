@@ -187,7 +187,8 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.nucl_buf, I * 64 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
         { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
         { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
-        { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
+        { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.vstamp, V * 4 },
+        { (void **)&m.bstamp, B * 4 }, { (void **)&m.stamp, 4 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
         { (void **)&m.bmark, B },
     };
     size_t total = 0;
@@ -455,10 +456,9 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
      * which nothing changes before that loop: count now, and decide on the
      * device whether this step must compute every output-only value. */
     { Prof pr(h, "two_three_count"); launch_two_three_first(m, x, x.list_b, x.n_b, s); }
-    launch_full_flag(x, s);
+    launch_full_flag(m, x, s);
     { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }                                     /* :206 */
     { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, h->p.shape, s); }                               /* :212-216 */
-    { Prof pr(h, "snapshot"); launch_snapshot(m, x, s); }
     { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
     cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
     cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);

@@ -93,7 +93,7 @@ __device__ __forceinline__ double moved_area(const DevMesh &m, const int *__rest
         else a += B0[k] * Pm[k + 1] - Pm[k] * B0[k + 1];
     }
     a = C == 0 ? add_closing_term(a, Pm[N - 1], B0[N - 1]) : add_closing_term(a, B0[N - 1], Pm[N - 1]);
-    return a * 0.5;
+    return dscale_down<1>(a);
 }
 
 template <int N>
@@ -126,10 +126,10 @@ __device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const in
     }
     acc = add_closing_term(acc, AX[N - 1], AY[N - 1]);
     S[N - 1] = acc;
-    double A = acc * 0.5;
+    double A = dscale_down<1>(acc);
     m.garea[g] = A;
     double se = m.gse[g];
-    m.gq[g] = se * A / N;
+    m.gq[g] = div_small<N>(se * A);
     double absA = dabs(A);
 #pragma unroll
     for (int p = 0; p < N; p++) {
@@ -203,7 +203,7 @@ __device__ __forceinline__ double area_shared(const double2 *P, int n, int ps, d
         }
         area = add_closing_term(area, ax, ay);
     }
-    return area * 0.5;
+    return dscale_down<1>(area);
 }
 
 /* grain pass over the grains of `wide` or more sides (the tail of the
@@ -294,11 +294,12 @@ __global__ void k_vlen_offsets(int *cnt, int *cursor, int *total)
  * threshold is crossed once per run.  Else only what the step can observe
  * is computed.  flags[0] = the decision, taken on the device so that no
  * host round trip separates the step's first half from its second. */
-__global__ void k_full_flag(const int *n_two_three, const int *vbucket, int *flags)
+__global__ void k_full_flag(const int *n_two_three, const int *vbucket, int *flags, unsigned *stamp)
 {
     int mg = flags[2], curr = flags[3], n3 = vbucket[3 * NBUCKET + 3];
     long long reach = (long long)curr - n3 - 40LL * *n_two_three - 64;
     flags[0] = flags[1] || (mg > 0 && reach <= mg);
+    *stamp += 1;   /* a new step: every value saved by the last step's events is stale */
 }
 __global__ void k_vlen_scatter(DevMesh m, int *cursor, int *perm)
 {
@@ -374,14 +375,15 @@ __global__ void k_vertex_fd(DevMesh m, double mu)
             gt += (c == 0 ? cg[j].x : cg[j].y);
         }
         if (c == 0) { t.bx = bt; t.gx = gt; } else { t.by = bt; t.gy = gt; }
-        vel[c] = mu * (-(bt + gt) / SEVC_GRAD_EPS_D);   /* mobility; mu = 1 multiplies exactly */
+        vel[c] = div_grad_eps(-(bt + gt));
+        if (mu != 1.0) vel[c] = mu * vel[c];   /* mobility; 1 * v is v exactly */
     }
     m.terms[v] = t;
     m.vel[v] = make_double2(vel[0], vel[1]);
     double e = 0.0;
     for (int j = 0; j < 3; j++) {
         int g = slot3(sg, j);
-        e += (len[j] * gam[j] * 0.5);
+        e += dscale_down<1>(len[j] * gam[j]);
         e += g >= 0 ? m.gq[g] : 0.0;
     }
     m.venergy[v] = e;
@@ -457,19 +459,6 @@ __global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float in
     }
     m.bcand[b] = (text >= 0 && text <= dt) ? 1 : 0;
     m.bconf[b] = -1;
-}
-
-/* the positions, velocities and boundary ends the step's events start from
- * (only needed when not every output value was computed exactly) */
-__global__ void k_snapshot(DevMesh m, const int *flags)
-{
-    if (flags[0]) return;
-    int stride = gridDim.x * blockDim.x;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m.nv; v += stride) {
-        m.pos0[v] = m.pos[v];
-        m.vel0[v] = m.vel[v];
-    }
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < m.nb; b += stride) m.bv0[b] = m.bv[b];
 }
 
 /* compute_grain_areas, src/calculus.h:224 */
@@ -621,18 +610,14 @@ void launch_vertex_fd(const DevMesh &m, double mu, const LaunchShape &sh, cudaSt
     int t = sh.tpb_vertex;
     COUNT_LAUNCHES(1), k_vertex_fd<<<(m.nv + t - 1) / t, t, 0, s>>>(m, mu);
 }
-void launch_full_flag(const DevScratch &x, cudaStream_t s)
+void launch_full_flag(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_full_flag<<<1, 1, 0, s>>>(x.n_b, x.vbucket, x.flags);
+    COUNT_LAUNCHES(1), k_full_flag<<<1, 1, 0, s>>>(x.n_b, x.vbucket, x.flags, m.stamp);
 }
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
     int g = nblk(m.ng);   /* grid-stride: every grain, or only the 3-sided ones, decided on the device */
     COUNT_LAUNCHES(1), k_grain_dadt<<<g < 8 * 152 ? g : 8 * 152, TPB, 0, s>>>(m, x.perm, x.vbucket, x.flags);
-}
-void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s)
-{
-    COUNT_LAUNCHES(1), k_snapshot<<<4 * 152, TPB, 0, s>>>(m, x.flags);
 }
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s)
 {

@@ -72,11 +72,10 @@ void launch_vertex_fd(const DevMesh &m, double mu, const LaunchShape &sh, cudaSt
 #define VB_START(b) (32 + (b))
 #define VB_COUNT(b) (48 + (b))
 /* x.flags: [0] computed "full" decision, [1] host part of it, [2]
- * min_grains, [3] current grain count (see k_full_flag) */
-void launch_full_flag(const DevScratch &x, cudaStream_t s);
+ * min_grains, [3] current grain count (see k_full_flag); also advances
+ * the step stamp of the events' save-on-write (m.stamp) */
+void launch_full_flag(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s);
-/* copies pos, vel, bv to pos0, vel0, bv0 unless the step computes every output */
-void launch_snapshot(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s);
 void launch_grain_area(const DevMesh &m, cudaStream_t s);
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);

@@ -354,6 +354,7 @@ __device__ int remove_two_grains_dev(const DevMesh &m, int bnd, const int *gnic)
     int F = other_end(m.bv[DF], D);
     int2 ce = m.bv[CE];
     if (ce.x == C) ce.x = F; else ce.y = F;
+    save_ends(m, CE);
     m.bv[CE] = ce;
     int4 sf = m.vb[F];
     for (int p = 0; p < 3; p++) if (slot3(sf, p) == DF) { set_slot3(sf, p, CE); break; }
@@ -517,6 +518,7 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
     pa.y += (nBC * y0 + nCA * y1 + nAB * y2) / denom;
     pa.x = dmod(pa.x, D);
     pa.y = dmod(pa.y, D);
+    save_vertex(m, A);
     m.pos[A] = pa;
     int gbc[2], gab[2], gac[2];
     gintersect(m.vg[B], m.vg[C], gbc);
@@ -546,6 +548,8 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
     }
     if (BE < 0 || CF < 0) { raise_err(m, ERRB_TOPOLOGY); return; }
     int2 e;
+    save_ends(m, BE);
+    save_ends(m, CF);
     e = m.bv[BE]; if (e.x == B) e.x = A; else e.y = A; m.bv[BE] = e;
     e = m.bv[CF]; if (e.x == C) e.x = A; else e.y = A; m.bv[CF] = e;
     int4 sa = m.vb[A];
@@ -630,6 +634,8 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
     set_slot3(sb, j, AC);
     m.vb[A] = sa;
     m.vb[B] = sb;
+    save_ends(m, AC);
+    save_ends(m, BE);
     int2 e = m.bv[AC]; if (e.x == A) e.x = B; else e.y = B; m.bv[AC] = e;
     e = m.bv[BE]; if (e.x == B) e.x = A; else e.y = A; m.bv[BE] = e;
     int g1, g2, g3, g4;
@@ -656,6 +662,8 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
     c.y += wrapd(pb.y, pa.y, m.D) / 2;
     c.x = dmod(c.x, m.D);
     c.y = dmod(c.y, m.D);
+    save_vertex(m, A);
+    save_vertex(m, B);
     m.pos[A] = c;
     m.pos[B] = c;
     sa = m.vb[A]; { int t = sa.y; sa.y = sa.x; sa.x = t; } m.vb[A] = sa; /* vertex_invert_boundary_order */
