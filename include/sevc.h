@@ -297,6 +297,18 @@ int sevc_format_fixed16(double x, char *out);
  * reference. */
 sevc_status sevc_measure_fp64_rate(double *ops_per_s);
 
+/* Self-test of the device arithmetic behind every arclength: the
+ * certified fast division and square root that replace the binary64
+ * operations in vector2_mag (src/geometry.h:217).  Runs n random cases
+ * (general operands, operands whose exact result lies next to a rounding
+ * midpoint, special operands) on the current device and compares each
+ * certified result, and each whole vector2_mag, bit for bit with the
+ * native operation.  counts[8]: divisions, division mismatches, divisions
+ * not certified (these fall back to the native division), square roots,
+ * square-root mismatches, square roots not certified, vector2_mag
+ * evaluations, vector2_mag mismatches.  No counterpart in the reference. */
+sevc_status sevc_selftest_arith(long long n, unsigned long long seed, long long *counts);
+
 /* Text of the last error on this thread. */
 const char *sevc_last_error(void);
 

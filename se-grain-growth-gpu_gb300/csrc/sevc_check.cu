@@ -160,6 +160,94 @@ extern "C" sevc_status sevc_measure_fp64_rate(double *ops_per_s)
     return SEVC_OK;
 }
 
+/* ---- self-test of the certified division / square root (vmag) ---- */
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z)   /* splitmix64 finaliser */
+{
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+/* a double in [1, 2) from 52 random bits, times 2^k */
+__device__ __forceinline__ double unit_pow2(unsigned long long u, int k)
+{
+    return __longlong_as_double((long long)((u & 0x000FFFFFFFFFFFFFULL) | ((unsigned long long)(1023 + k) << 52)));
+}
+
+/* counts: 0 divisions, 1 division mismatches, 2 divisions not certified,
+ * 3 square roots, 4 square-root mismatches, 5 not certified, 6 vmag
+ * evaluations, 7 vmag mismatches (a mismatch is a certified result whose
+ * bits differ from the native operation's) */
+__global__ void k_selftest_arith(long long n, unsigned long long seed, unsigned long long *counts)
+{
+    unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long a = mix64(seed ^ (2 * i)), b = mix64(seed ^ (2 * i + 1)), kind = (a >> 60) & 7;
+        /* division q / p with 0 <= q <= p */
+        int kp = (int)((b >> 56) % 121) - 60;
+        double p = unit_pow2(b, kp), q;
+        if (kind < 4) {
+            q = p * unit_pow2(a, -1 - (int)((a >> 52) & 7));          /* a general ratio */
+        } else if (kind < 7) {
+            /* q = RN(p m) for a rounding midpoint m = k 2^-53 + 2^-54 of (1/2, 1) */
+            double kd = __longlong_as_double((long long)((a & 0x000FFFFFFFFFFFFFULL) | (1022ULL << 52)));
+            q = __fma_rn(p, kd, p * 0x1p-54);
+            if (kind == 6) q = __longlong_as_double(dbits(q) + (((a >> 59) & 1) ? 1 : -1));
+            if (dbits(q) > dbits(p)) q = p;
+        } else {
+            int w = (int)((a >> 40) & 3);
+            q = w == 0 ? p : (w == 1 ? 0.0 : p * 0x1p-1040);            /* r = 1, 0, subnormal q */
+        }
+        double r;
+        c[0]++;
+        if (div_fast(q, p, r)) { if (dbits(r) != dbits(q / p)) c[1]++; }
+        else c[2]++;
+        /* square root of t in [1, 2) */
+        double t;
+        if (kind < 4) {
+            t = unit_pow2(a, 0);
+        } else {
+            /* t = RN(m^2) next to the square of a midpoint m = s + 2^-53 */
+            double s = unit_pow2(a, 0);
+            if (s > 1.4142135623730950) s = s - 0.4142135623730950;
+            t = __fma_rn(s, s, s * 0x1p-52);
+            if (kind == 6) t = __longlong_as_double(dbits(t) + (((a >> 59) & 1) ? 1 : -1));
+            if ((dbits(t) >> 52) != 1023) t = 1.5;
+        }
+        c[3]++;
+        if (sqrt_fast(t, r)) { if (dbits(r) != dbits(sqrt(t))) c[4]++; }
+        else c[5]++;
+        /* whole vector2_mag on coordinates of random sign and scale */
+        double x = unit_pow2(mix64(a), (int)(b & 63) - 32), y = unit_pow2(mix64(b), (int)((a >> 8) & 63) - 32);
+        if (kind == 7) y = ((a >> 44) & 1) ? x : 0.0;
+        if ((a >> 48) & 1) x = -x;
+        if ((b >> 48) & 1) y = -y;
+        c[6]++;
+        if (dbits(vmag(x, y)) != dbits(vmag_native(x, y))) c[7]++;
+    }
+    for (int k = 0; k < 8; k++) {
+        unsigned long long v = c[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(counts + k, v);
+    }
+}
+
+extern "C" sevc_status sevc_selftest_arith(long long n, unsigned long long seed, long long *counts)
+{
+    if (!counts || n < 0) return SEVC_ERR_ARG;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 8 * sizeof(unsigned long long)) != cudaSuccess) return SEVC_ERR_CUDA;
+    bool ok = cudaMemset(d, 0, 8 * sizeof(unsigned long long)) == cudaSuccess;
+    if (ok) {
+        COUNT_LAUNCHES(1), k_selftest_arith<<<152 * 8, 256>>>(n, seed, d);
+        unsigned long long h[8];
+        ok = cudaGetLastError() == cudaSuccess && cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost) == cudaSuccess;
+        for (int k = 0; ok && k < 8; k++) counts[k] = (long long)h[k];
+    }
+    cudaFree(d);
+    return ok ? SEVC_OK : SEVC_ERR_CUDA;
+}
+
 void launch_check(const DevMesh &m, int *out, cudaStream_t s)
 {
     cudaMemsetAsync(out, 0, sizeof(int), s);

@@ -206,7 +206,116 @@ __device__ __forceinline__ double wrapd(double dest, double orig, double D) /* w
     if (b < 0 && (b & SEVC_ABSMASK) > h) return (D + d);          /* d < -D/2 */
     return d;
 }
-__device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :217 */
+/* ---- correctly rounded division and square root for vector2_mag ----
+ * On GB300 a binary64 division or square root costs ~10-12 FP64
+ * instructions (ncu: 22 for the pair).  These versions take a binary32
+ * seed from the special-function unit, refine it on the FP32 pipe to a
+ * float-float value of ~45 bits, finish with two FP64 correction steps
+ * (Markstein's method: P. Markstein, "IA-64 and elementary functions",
+ * 2000, ch. 8; J.-M. Muller et al., Handbook of Floating-Point Arithmetic,
+ * 2nd ed., 2018, sec. 4.7) and then CERTIFY the result exactly: the
+ * remainder of the candidate is computed with one fma and compared, on the
+ * integer pipe, with the half-ulp bound that characterises round-to-nearest.
+ * A candidate that is not certified (about one in 10^4, or special
+ * operands) is discarded and the native operation runs, so the returned
+ * value is always the correctly rounded one.  5 FP64 instructions each. */
+
+/* binary32 -> binary64 by bit manipulation (exact for normal x; zero and
+ * subnormal x give 0, an error the certification absorbs) */
+__device__ __forceinline__ double f2d_bits(float x)
+{
+    unsigned u = __float_as_uint(x);
+    unsigned e = (u >> 23) & 0xffu;
+    unsigned long long r = ((unsigned long long)(u & 0x80000000u) << 32) |
+                           ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return e == 0u ? 0.0 : __longlong_as_double((long long)r);
+}
+/* a binary64 in [1, 2) (bit pattern b) as hi + lo binary32, hi holding
+ * the leading 24 bits */
+__device__ __forceinline__ void split_unit(long long b, float &hi, float &lo)
+{
+    hi = __uint_as_float(0x3F800000u | (unsigned)((b >> 29) & 0x7fffffLL));
+    lo = __uint2float_rn((unsigned)(b & 0x1fffffffLL)) * 0x1p-52f;
+}
+__device__ __forceinline__ float rcp_seed(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_seed(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+/* r = RN(q / p) for 0 <= q <= p; false when not certified */
+__device__ __forceinline__ bool div_fast(double q, double p, double &r)
+{
+    long long pb = dbits(p), qb = dbits(q);
+    if (qb == 0) { r = 0.0; return true; }                /* q = +0 */
+    int ep = (int)(pb >> 52), eq = (int)(qb >> 52);
+    if (eq < 1 || eq > ep || ep > 2046 || ep - eq > 900) return false;
+    /* P = p scaled into [1, 2), Q = q by the same power of two: Q / P = q / p */
+    double P = __longlong_as_double((pb & 0x000FFFFFFFFFFFFFLL) | (1023LL << 52));
+    double Q = __longlong_as_double(qb - (long long)(ep - 1023) * (1LL << 52));
+    float ph, pl;
+    split_unit(dbits(P), ph, pl);
+    float y0 = rcp_seed(ph);                              /* 1/P to ~2^-23 */
+    float e = fmaf(-ph, y0, 1.0f);
+    e = fmaf(-pl, y0, e);                                 /* 1 - P y0 to ~2^-46 */
+    float yl = y0 * e;                                    /* 1/P ~ y0 + yl to ~2^-45 */
+    double y0d = f2d_bits(y0), yld = f2d_bits(yl);
+    double q0 = __fma_rn(Q, yld, __dmul_rn(Q, y0d));      /* ~2^-45 */
+    double rem = __fma_rn(-P, q0, Q);
+    double q1 = __fma_rn(rem, y0d, q0);                   /* ~2^-67 */
+    double rem1 = __fma_rn(-P, q1, Q);                    /* exact when q1 is faithful */
+    long long rb = dbits(rem1) & SEVC_ABSMASK, b1 = dbits(q1);
+    r = q1;
+    if (rb == 0) return true;                             /* Q = P q1 exactly */
+    /* RN(Q/P) = q1 iff |Q - P q1| < ulp(q1)/2 * P for q1 not a power of two
+     * (a power of two has a narrower interval below); ties cannot occur.
+     * RN is monotonic and the bound is a binary64, so the rounded
+     * remainder decides it even where the remainder is not exact. */
+    int e1 = (int)(b1 >> 52);
+    if (b1 <= 0 || e1 < 54 || e1 > 2046 || (b1 & 0x000FFFFFFFFFFFFFLL) == 0) return false;
+    long long half_ulp_P = dbits(P) + (long long)(e1 - 1076) * (1LL << 52);
+    return rb < half_ulp_P;
+}
+
+/* r = RN(sqrt(t)) for t in [1, 2); false when not certified */
+__device__ __forceinline__ bool sqrt_fast(double t, double &r)
+{
+    long long tb = dbits(t);
+    if ((tb >> 52) != 1023) return false;
+    float th, tl;
+    split_unit(tb, th, tl);
+    float y0 = rsqrt_seed(th);                            /* 1/sqrt(t) to ~2^-23 */
+    float ah = y0 * y0, al = fmaf(y0, y0, -ah);           /* y0^2 = ah + al exactly */
+    float e = fmaf(-th, ah, 1.0f);
+    e = fmaf(-th, al, e);
+    e = fmaf(-tl, ah, e);                                 /* 1 - t y0^2 to ~2^-46 */
+    float yl = 0.5f * (y0 * e);                           /* Newton: 1/sqrt(t) ~ y0 + yl */
+    double y0d = f2d_bits(y0), yld = f2d_bits(yl);
+    double s0 = __fma_rn(t, yld, __dmul_rn(t, y0d));      /* sqrt(t) to ~2^-45 */
+    double d = __fma_rn(-s0, s0, t);
+    double s1 = __fma_rn(d, __longlong_as_double(dbits(y0d) - (1LL << 52)), s0);   /* + d y0/2: ~2^-67 */
+    double e1 = __fma_rn(-s1, s1, t);
+    long long eb = dbits(e1) & SEVC_ABSMASK, sb = dbits(s1);
+    r = s1;
+    if (eb == 0) return true;                             /* t = s1^2 exactly */
+    /* For s1 in (1, 2), u = ulp(s1) = 2^-52: RN(sqrt t) = s1 iff
+     * |t - s1^2| < s1 u - u^2/4 on both sides.  |RN(t - s1^2)| < s1 u (a
+     * binary64 whose predecessor is s1 u - 2^-104) implies it, the
+     * rounding of the remainder being at most 2^-105. */
+    if ((sb >> 52) != 1023 || (sb & 0x000FFFFFFFFFFFFFLL) == 0) return false;
+    return eb < sb - (52LL << 52);
+}
+
+/* vector2_mag (src/geometry.h:217): p sqrt(1 + (q/p)^2) with p = max(|x|,
+ * |y|), q = min, every operation correctly rounded as in the reference */
+__device__ __forceinline__ double vmag_native(double x, double y)
 {
     long long ax = dbits(x) & SEVC_ABSMASK, ay = dbits(y) & SEVC_ABSMASK;
     long long pb = ax > ay ? ax : ay, qb = ax > ay ? ay : ax;    /* fmax / fmin of |x|, |y| */
@@ -214,6 +323,19 @@ __device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :
     double p = __longlong_as_double(pb), q = __longlong_as_double(qb);
     double r = q / p;
     return p * sqrt(1.0 + r * r);
+}
+static __device__ __noinline__ double sqrt_slow(double t) { return sqrt(t); }
+__device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :217 */
+{
+    long long ax = dbits(x) & SEVC_ABSMASK, ay = dbits(y) & SEVC_ABSMASK;
+    long long pb = ax > ay ? ax : ay, qb = ax > ay ? ay : ax;    /* fmax / fmin of |x|, |y| */
+    if (pb == 0) return 0;
+    double p = __longlong_as_double(pb), q = __longlong_as_double(qb);
+    double r, s;
+    if (!div_fast(q, p, r)) r = ddiv_slow(q, p);
+    double t = 1.0 + r * r;
+    if (!sqrt_fast(t, s)) s = sqrt_slow(t);
+    return p * s;
 }
 /* x / SEVC_GRAD_EPS_D, correctly rounded, with one multiplication and one
  * fma instead of a division: the divisor y is known in advance

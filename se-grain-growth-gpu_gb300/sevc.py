@@ -26,7 +26,7 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
            "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
            "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs", "sevc_measure_fp64_rate",
-           "sevc_autotune"]
+           "sevc_autotune", "sevc_selftest_arith"]
 
 
 class SevcError(RuntimeError):
@@ -187,6 +187,19 @@ def measure_fp64_rate():
     L.sevc_measure_fp64_rate.argtypes = [C.POINTER(C.c_double)]
     _check(L.sevc_measure_fp64_rate(C.byref(r)))
     return r.value
+
+
+def selftest_arith(n, seed=1):
+    """Bit-for-bit check of the certified division / square root behind
+    the arclengths against the native operations on n random cases; a dict
+    of the counts sevc_selftest_arith returns."""
+    c = (C.c_longlong * 8)()
+    L = lib()
+    L.sevc_selftest_arith.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
+    _check(L.sevc_selftest_arith(int(n), int(seed), c))
+    keys = ["div", "div_mismatch", "div_uncertified", "sqrt", "sqrt_mismatch", "sqrt_uncertified", "vmag",
+            "vmag_mismatch"]
+    return dict(zip(keys, list(c)))
 
 
 def format_fixed16(x):

@@ -65,3 +65,16 @@ def test_device_check_matches_host(gpu):
             d, h = gpu.check_mesh(bad), gpu.check_mesh_host(bad)
             assert d == h and d > 0, (kind, d, h)
     e.close()
+
+
+def test_certified_division_and_sqrt_are_correctly_rounded(gpu):
+    """Every arclength divides and takes a square root with the certified
+    fast operations; on 2^26 random cases (general operands, quotients and
+    roots next to rounding midpoints, special operands) each certified
+    result, and each whole vector2_mag, equals the native operation bit for
+    bit, and only a small share falls back to the native path."""
+    for seed in (1, 2):
+        c = gpu.selftest_arith(1 << 26, seed=seed)
+        assert c["div"] == c["sqrt"] == c["vmag"] == 1 << 26
+        assert c["div_mismatch"] == 0 and c["sqrt_mismatch"] == 0 and c["vmag_mismatch"] == 0, c
+        assert c["div_uncertified"] < 0.1 * c["div"] and c["sqrt_uncertified"] < 0.1 * c["sqrt"], c
