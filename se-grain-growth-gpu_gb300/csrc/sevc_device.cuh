@@ -19,6 +19,7 @@
 #ifndef SEVC_DEVICE_CUH
 #define SEVC_DEVICE_CUH
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -137,24 +138,37 @@ __device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int
  * 64-bit order of the patterns of non-negative values is their numeric
  * order, so every branch takes the same side as the floating-point
  * comparison of the reference while the (scarce) FP64 pipe only executes
- * the arithmetic.  Inputs are never NaN. */
+ * the arithmetic.  Inputs are never NaN.
+ *
+ * Two compiler behaviours are kept away from the FP64 pipe (counted with
+ * ncu: each cost one FP64 instruction per call):
+ *  - a short branch whose body is FP64 arithmetic gets if-converted, the
+ *    arithmetic then runs for every thread; rare bodies are therefore
+ *    calls (the *_slow functions), which cannot be speculated;
+ *  - an absolute value taken by masking the sign bit is recognised as
+ *    fabs and emitted as an FP64 instruction; magnitudes are therefore
+ *    compared through the sign-free pattern (b << 1) or, for a negative
+ *    b, through b itself (b = magnitude - 2^63). */
 #define SEVC_ABSMASK 0x7FFFFFFFFFFFFFFFLL
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 __device__ __forceinline__ double dabs(double x) { return __longlong_as_double(dbits(x) & SEVC_ABSMASK); }
+/* the magnitude's bit pattern shifted left by one: ordered like |x| */
+__device__ __forceinline__ unsigned long long mag2(double x) { return (unsigned long long)dbits(x) << 1; }
+
+static __device__ __noinline__ double dadd_slow(double a, double b) { return a + b; }
+static __device__ __noinline__ double dsub_slow(double a, double b) { return a - b; }
+static __device__ __noinline__ double dmul_slow(double x, double s) { return x * s; }
+static __device__ __noinline__ double ddiv_slow(double x, double y) { return x / y; }
 
 __device__ __forceinline__ double dmod(double a, double D)        /* dom_mod :133 */
 {
     long long b = dbits(a);
-    if (b < 0 && (b & SEVC_ABSMASK) != 0) return a + D;          /* a < 0 */
-    else if (b >= dbits(D)) return a - D;                         /* a >= D (D > 0) */
+    if (b < 0 && b != (long long)0x8000000000000000ULL) return dadd_slow(a, D);   /* a < 0 (not -0) */
+    else if (b >= dbits(D)) return dsub_slow(a, D);                               /* a >= D (D > 0) */
     return a;
 }
 /* Exact scalings and divisions kept off the FP64 pipe (on GB300 one FP64
- * operation costs as much issue time as dozens of integer ones).  The
- * slow paths are calls, so that the compiler cannot turn the branch into
- * predicated FP64 instructions that would occupy the pipe anyway. */
-static __device__ __noinline__ double dmul_slow(double x, double s) { return x * s; }
-static __device__ __noinline__ double ddiv_slow(double x, double y) { return x / y; }
+ * operation costs as much issue time as dozens of integer ones). */
 
 /* x * 2^-K (K = 1..3), exactly: an exponent decrement on the integer pipe
  * when x and the result are normal, else the multiplication */
@@ -190,8 +204,8 @@ template <int N> __device__ __forceinline__ double div_small(double x)
     } else if constexpr (N == 8) {
         return dscale_down<3>(x);
     } else {
-        long long b = dbits(x) & 0x7FFFFFFFFFFFFFFFLL;
-        if (b >= 0x07B0000000000000LL && b < 0x7830000000000000LL)
+        unsigned long long b = mag2(x);
+        if (b >= (0x07B0000000000000ULL << 1) && b < (0x7830000000000000ULL << 1))
             return __fma_rn(x, InvSplit<N>::hi, __dmul_rn(x, InvSplit<N>::lo));
         return ddiv_slow(x, (double)N);
     }
@@ -202,8 +216,8 @@ __device__ __forceinline__ double wrapd(double dest, double orig, double D) /* w
     double d = dest - orig;
     /* D/2 by an exponent decrement (D is a positive normal domain bound) */
     long long b = dbits(d), h = dbits(D) - (1LL << 52);
-    if (b > h) return (d - D);                                    /* d > +D/2 */
-    if (b < 0 && (b & SEVC_ABSMASK) > h) return (D + d);          /* d < -D/2 */
+    if (b > h) return dsub_slow(d, D);                            /* d > +D/2 */
+    if (b < 0 && b > h + LLONG_MIN) return dadd_slow(D, d);       /* d < -D/2 */
     return d;
 }
 /* ---- correctly rounded division and square root for vector2_mag ----
@@ -271,7 +285,8 @@ __device__ __forceinline__ bool div_fast(double q, double p, double &r)
     double rem = __fma_rn(-P, q0, Q);
     double q1 = __fma_rn(rem, y0d, q0);                   /* ~2^-67 */
     double rem1 = __fma_rn(-P, q1, Q);                    /* exact when q1 is faithful */
-    long long rb = dbits(rem1) & SEVC_ABSMASK, b1 = dbits(q1);
+    unsigned long long rb = mag2(rem1);
+    long long b1 = dbits(q1);
     r = q1;
     if (rb == 0) return true;                             /* Q = P q1 exactly */
     /* RN(Q/P) = q1 iff |Q - P q1| < ulp(q1)/2 * P for q1 not a power of two
@@ -281,7 +296,7 @@ __device__ __forceinline__ bool div_fast(double q, double p, double &r)
     int e1 = (int)(b1 >> 52);
     if (b1 <= 0 || e1 < 54 || e1 > 2046 || (b1 & 0x000FFFFFFFFFFFFFLL) == 0) return false;
     long long half_ulp_P = dbits(P) + (long long)(e1 - 1076) * (1LL << 52);
-    return rb < half_ulp_P;
+    return rb < ((unsigned long long)half_ulp_P << 1);
 }
 
 /* r = RN(sqrt(t)) for t in [1, 2); false when not certified */
@@ -302,7 +317,8 @@ __device__ __forceinline__ bool sqrt_fast(double t, double &r)
     double d = __fma_rn(-s0, s0, t);
     double s1 = __fma_rn(d, __longlong_as_double(dbits(y0d) - (1LL << 52)), s0);   /* + d y0/2: ~2^-67 */
     double e1 = __fma_rn(-s1, s1, t);
-    long long eb = dbits(e1) & SEVC_ABSMASK, sb = dbits(s1);
+    unsigned long long eb = mag2(e1);
+    long long sb = dbits(s1);
     r = s1;
     if (eb == 0) return true;                             /* t = s1^2 exactly */
     /* For s1 in (1, 2), u = ulp(s1) = 2^-52: RN(sqrt t) = s1 iff
@@ -310,7 +326,7 @@ __device__ __forceinline__ bool sqrt_fast(double t, double &r)
      * binary64 whose predecessor is s1 u - 2^-104) implies it, the
      * rounding of the remainder being at most 2^-105. */
     if ((sb >> 52) != 1023 || (sb & 0x000FFFFFFFFFFFFFLL) == 0) return false;
-    return eb < sb - (52LL << 52);
+    return eb < ((unsigned long long)(sb - (52LL << 52)) << 1);
 }
 
 /* vector2_mag (src/geometry.h:217): p sqrt(1 + (q/p)^2) with p = max(|x|,
@@ -352,8 +368,8 @@ __device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :
 #define SEVC_INV_EPS_LO (-0x1.1f8eb76e8p-29)
 __device__ __forceinline__ double div_grad_eps(double x)
 {
-    long long b = dbits(x) & SEVC_ABSMASK;
-    if (b >= 0x0210000000000000LL && b < 0x7DD0000000000000LL)
+    unsigned long long b = mag2(x);
+    if (b >= (0x0210000000000000ULL << 1) && b < (0x7DD0000000000000ULL << 1))
         return __fma_rn(x, SEVC_INV_EPS_HI, __dmul_rn(x, SEVC_INV_EPS_LO));
     return ddiv_slow(x, SEVC_GRAD_EPS_D);
 }
