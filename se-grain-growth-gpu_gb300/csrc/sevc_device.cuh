@@ -145,15 +145,21 @@ __device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int
  *  - a short branch whose body is FP64 arithmetic gets if-converted, the
  *    arithmetic then runs for every thread; rare bodies are therefore
  *    calls (the *_slow functions), which cannot be speculated;
- *  - an absolute value taken by masking the sign bit is recognised as
- *    fabs and emitted as an FP64 instruction; magnitudes are therefore
- *    compared through the sign-free pattern (b << 1) or, for a negative
- *    b, through b itself (b = magnitude - 2^63). */
+ *  - an absolute value taken from the bit pattern (sign masked or shifted
+ *    out) and compared is recognised as an FP comparison of fabs and
+ *    emitted on the FP64 pipe; magnitudes are therefore compared through
+ *    mag2, whose shift is opaque inline PTX, or, for a negative b, through
+ *    b itself (b = magnitude - 2^63). */
 #define SEVC_ABSMASK 0x7FFFFFFFFFFFFFFFLL
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 __device__ __forceinline__ double dabs(double x) { return __longlong_as_double(dbits(x) & SEVC_ABSMASK); }
 /* the magnitude's bit pattern shifted left by one: ordered like |x| */
-__device__ __forceinline__ unsigned long long mag2(double x) { return (unsigned long long)dbits(x) << 1; }
+__device__ __forceinline__ unsigned long long mag2(double x)
+{
+    unsigned long long r;
+    asm("shl.b64 %0, %1, 1;" : "=l"(r) : "l"(dbits(x)));
+    return r;
+}
 
 static __device__ __noinline__ double dadd_slow(double a, double b) { return a + b; }
 static __device__ __noinline__ double dsub_slow(double a, double b) { return a - b; }
@@ -288,15 +294,18 @@ __device__ __forceinline__ bool div_fast(double q, double p, double &r)
     unsigned long long rb = mag2(rem1);
     long long b1 = dbits(q1);
     r = q1;
-    if (rb == 0) return true;                             /* Q = P q1 exactly */
-    /* RN(Q/P) = q1 iff |Q - P q1| < ulp(q1)/2 * P for q1 not a power of two
-     * (a power of two has a narrower interval below); ties cannot occur.
-     * RN is monotonic and the bound is a binary64, so the rounded
-     * remainder decides it even where the remainder is not exact. */
-    int e1 = (int)(b1 >> 52);
-    if (b1 <= 0 || e1 < 54 || e1 > 2046 || (b1 & 0x000FFFFFFFFFFFFFLL) == 0) return false;
-    long long half_ulp_P = dbits(P) + (long long)(e1 - 1076) * (1LL << 52);
-    return rb < ((unsigned long long)half_ulp_P << 1);
+    /* RN(Q/P) = q1 iff Q/P is within ulp(q1)/2 of q1 (within ulp(q1)/4
+     * below a power of two, whose lower neighbour is closer); ties cannot
+     * occur.  Sufficient: |Q - P q1| < P ulp(q1)/2 (or /4 for a power of
+     * two, on both sides).  RN is monotonic and the bound is a binary64, so
+     * the rounded remainder decides it even where the remainder is not
+     * exact.  (No separate test for a zero remainder: the compiler would
+     * make it an FP64 comparison.) */
+    int e1 = (int)(b1 >> 52);                             /* negative for a negative q1 */
+    if (e1 < 55 || e1 > 2046) return false;
+    int sh = (b1 & 0x000FFFFFFFFFFFFFLL) == 0 ? 1077 : 1076;
+    long long bound = dbits(P) + (long long)(e1 - sh) * (1LL << 52);
+    return rb < ((unsigned long long)bound << 1);
 }
 
 /* r = RN(sqrt(t)) for t in [1, 2); false when not certified */
@@ -320,12 +329,13 @@ __device__ __forceinline__ bool sqrt_fast(double t, double &r)
     unsigned long long eb = mag2(e1);
     long long sb = dbits(s1);
     r = s1;
-    if (eb == 0) return true;                             /* t = s1^2 exactly */
     /* For s1 in (1, 2), u = ulp(s1) = 2^-52: RN(sqrt t) = s1 iff
      * |t - s1^2| < s1 u - u^2/4 on both sides.  |RN(t - s1^2)| < s1 u (a
      * binary64 whose predecessor is s1 u - 2^-104) implies it, the
-     * rounding of the remainder being at most 2^-105. */
-    if ((sb >> 52) != 1023 || (sb & 0x000FFFFFFFFFFFFFLL) == 0) return false;
+     * rounding of the remainder being at most 2^-105.  For s1 = 1 the
+     * remainder t - 1 is exact and t >= 1, so the narrower interval below
+     * 1 never matters and the same test certifies exactly t = 1. */
+    if ((sb >> 52) != 1023) return false;
     return eb < ((unsigned long long)(sb - (52LL << 52)) << 1);
 }
 
@@ -341,9 +351,16 @@ __device__ __forceinline__ double vmag_native(double x, double y)
     return p * sqrt(1.0 + r * r);
 }
 static __device__ __noinline__ double sqrt_slow(double t) { return sqrt(t); }
+/* |x|'s bit pattern, masked in opaque inline PTX (see mag2) */
+__device__ __forceinline__ long long absbits(double x)
+{
+    long long r;
+    asm("and.b64 %0, %1, 0x7FFFFFFFFFFFFFFF;" : "=l"(r) : "l"(dbits(x)));
+    return r;
+}
 __device__ __forceinline__ double vmag(double x, double y)      /* vector2_mag :217 */
 {
-    long long ax = dbits(x) & SEVC_ABSMASK, ay = dbits(y) & SEVC_ABSMASK;
+    long long ax = absbits(x), ay = absbits(y);
     long long pb = ax > ay ? ax : ay, qb = ax > ay ? ay : ax;    /* fmax / fmin of |x|, |y| */
     if (pb == 0) return 0;
     double p = __longlong_as_double(pb), q = __longlong_as_double(qb);
