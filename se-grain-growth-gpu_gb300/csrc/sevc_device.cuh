@@ -176,6 +176,14 @@ __device__ __forceinline__ double dmod(double a, double D)        /* dom_mod :13
 /* Exact scalings and divisions kept off the FP64 pipe (on GB300 one FP64
  * operation costs as much issue time as dozens of integer ones). */
 
+/* +0.0 + x, exactly, on the integer pipe: x, except that -0 becomes +0
+ * (for the first term of a sum the reference starts from 0.0) */
+__device__ __forceinline__ double zero_plus(double x)
+{
+    long long b = dbits(x);
+    return __longlong_as_double(b == LLONG_MIN ? 0LL : b);
+}
+
 /* x * 2^-K (K = 1..3), exactly: an exponent decrement on the integer pipe
  * when x and the result are normal, else the multiplication */
 template <int K> __device__ __forceinline__ double dscale_down(double x)

@@ -93,6 +93,11 @@ struct sevc_handle {
     StepGraph g_pre[2], g_poll, g_post;
     bool use_graphs = true;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    /* side streams of the first half of the step (branches that do not
+     * depend on each other run concurrently; captured as graph branches)
+     * and the fork / join events between them */
+    cudaStream_t side[2] = { nullptr, nullptr };
+    cudaEvent_t evfork[6] = {};
     bool profiling = false;
     std::map<std::string, ProfEntry> prof;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -316,8 +321,12 @@ sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handl
     h->curr_n_grains = h->ng;
     /* readback: counters, events, polling iterations, 2x3 counts per instance */
     h->h_big_ints = (size_t)ninst * (CTR_COUNT + EVT_COUNT + 1 + TWO_THREE_PASSES) + 64;
-    if (!cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream") ||
-        !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") ||
+    bool streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+    for (int k = 0; streams_ok && k < 2; k++)
+        streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking), "stream");
+    for (int k = 0; streams_ok && k < 6; k++)
+        streams_ok = cuda_ok(cudaEventCreateWithFlags(&h->evfork[k], cudaEventDisableTiming), "event");
+    if (!streams_ok || !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") ||
         !cuda_ok(cudaMallocHost(&h->h_big, h->h_big_ints * sizeof(int)), "pinned") ||
         !cuda_ok(cudaMallocHost(&h->h_on, ninst * sizeof(int)), "pinned") ||
         !cuda_ok(cudaMallocHost(&h->h_flags, 4 * sizeof(int)), "pinned") || !alloc_device(h) ||
@@ -445,21 +454,63 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
     cudaMemsetAsync(m.gexact, 0, (size_t)h->ng, s);
     launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
-    { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :124-130 */
     if (nucleation) {
+        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :124-130 */
         { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
-        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :171-181 */
     }
-    { Prof pr(h, "grain_fd"); launch_grain_fd(m, x, h->p.shape, s); }                                         /* :127,:203 */
-    { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, h->p.shape, s); }                                 /* :133,:203 */
-    /* The first count of the 2x3 loop (:228) depends only on the topology,
-     * which nothing changes before that loop: count now, and decide on the
-     * device whether this step must compute every output-only value. */
-    { Prof pr(h, "two_three_count"); launch_two_three_first(m, x, x.list_b, x.n_b, s); }
-    launch_full_flag(m, x, s);
-    { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }                                     /* :206 */
-    { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, h->p.shape, s); }                               /* :212-216 */
-    { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
+    /* From here three branches that share no written data run concurrently
+     * (side streams, graph branches when captured):
+     *   main   side-count order, thread-per-grain grain pass
+     *   side0  boundary arclengths and energies (:124-130 / :171-181)
+     *   side1  warp-per-grain grain pass of the widest grains; the first
+     *          2x3 count (:228), which depends only on the topology that
+     *          nothing changes before that loop; the device-side decision
+     *          whether this step computes every output-only value
+     * and join before the vertex pass, which reads all of them.  After it,
+     * dA/dt of the 3-sided grains (side0) runs beside the t_ext labels.
+     * While profiling everything stays on the main stream, in order. */
+    /* every boundary energy this step is 1 * 1 exactly (k_boundary_geometry) */
+    const bool unit_gamma = o.GB_eps == 0.0 && o.GB_scaling == 1.0;
+    if (h->profiling) {
+        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); }
+        {
+            Prof pr(h, "grain_fd");
+            launch_grain_sort(m, x, s);
+            launch_grain_fd_wide(m, x, h->p.shape, s);
+            launch_grain_fd_sorted(m, x, h->p.shape, s);
+        }
+        { Prof pr(h, "two_three_count"); launch_two_three_first(m, x, x.list_b, x.n_b, s); }
+        launch_full_flag(m, x, s);
+        { Prof pr(h, "vertex_fd"); launch_vertex_fd(m, h->p.mu, unit_gamma, h->p.shape, s); }
+        { Prof pr(h, "grain_dadt"); launch_grain_dadt(m, x, s); }
+        { Prof pr(h, "text_label"); launch_text_label(m, x, o.dt, h->p.shape, s); }
+        { Prof pr(h, "compact"); launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s); }
+    } else {
+        cudaStream_t s0 = h->side[0], s1 = h->side[1];
+        cudaEvent_t *ev = h->evfork;
+        cudaEventRecord(ev[0], s);
+        cudaStreamWaitEvent(s0, ev[0], 0);
+        launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s0);          /* :124-130, :171-181 */
+        cudaEventRecord(ev[1], s0);
+        launch_grain_sort(m, x, s);
+        cudaEventRecord(ev[2], s);
+        cudaStreamWaitEvent(s1, ev[2], 0);
+        launch_grain_fd_wide(m, x, h->p.shape, s1);                                    /* :127,:203 */
+        launch_two_three_first(m, x, x.list_b, x.n_b, s1);                             /* :228 */
+        launch_full_flag(m, x, s1);
+        cudaEventRecord(ev[3], s1);
+        launch_grain_fd_sorted(m, x, h->p.shape, s);                                   /* :127,:203 */
+        cudaStreamWaitEvent(s, ev[1], 0);
+        cudaStreamWaitEvent(s, ev[3], 0);
+        launch_vertex_fd(m, h->p.mu, unit_gamma, h->p.shape, s);                       /* :133,:203 */
+        cudaEventRecord(ev[4], s);
+        cudaStreamWaitEvent(s0, ev[4], 0);
+        launch_grain_dadt(m, x, s0);                                                   /* :206 */
+        cudaEventRecord(ev[5], s0);
+        launch_text_label(m, x, o.dt, h->p.shape, s);                                  /* :212-216 */
+        launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s);
+        cudaStreamWaitEvent(s, ev[5], 0);
+    }
     cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
     cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);
 }
@@ -654,6 +705,8 @@ void sevc_destroy(sevc_handle *h)
     drop_graphs(h);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    for (auto e : h->evfork) if (e) cudaEventDestroy(e);
+    for (auto sd : h->side) if (sd) { cudaStreamSynchronize(sd); cudaStreamDestroy(sd); }
     for (auto e : h->evpool) cudaEventDestroy(e);
     for (auto &pe : h->pending) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
     if (h->stream) cudaStreamDestroy(h->stream);

@@ -81,6 +81,7 @@ __device__ __forceinline__ double moved_area(const DevMesh &m, const int *__rest
 #pragma unroll
     for (int k = 1; k < N; k++) {
         if (k < p) Pm[k] = A0[k];
+        else if (k == 1) Pm[k] = zero_plus(k == p ? wrapd(moved, R[0], D) : wrapd(R[1], moved, D));   /* +0 + w */
         else if (k == p) Pm[k] = A0[k - 1] + wrapd(moved, R[k - 1], D);
         else if (k == p + 1) Pm[k] = Pm[k - 1] + wrapd(R[k], moved, D);
         else Pm[k] = Pm[k - 1] + DD[k];
@@ -89,8 +90,8 @@ __device__ __forceinline__ double moved_area(const DevMesh &m, const int *__rest
 #pragma unroll
     for (int k = 1; k < N - 1; k++) {
         if (k < p - 1) continue;
-        if (C == 0) a += Pm[k] * B0[k + 1] - B0[k] * Pm[k + 1];
-        else a += B0[k] * Pm[k + 1] - Pm[k] * B0[k + 1];
+        double term = C == 0 ? Pm[k] * B0[k + 1] - B0[k] * Pm[k + 1] : B0[k] * Pm[k + 1] - Pm[k] * B0[k + 1];
+        a = (k == 1 && p <= 2) ? zero_plus(term) : a + term;   /* the sum is still +0 */
     }
     a = C == 0 ? add_closing_term(a, Pm[N - 1], B0[N - 1]) : add_closing_term(a, B0[N - 1], Pm[N - 1]);
     return dscale_down<1>(a);
@@ -114,14 +115,15 @@ __device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const in
     for (int k = 1; k < N; k++) {
         DX[k] = wrapd(RX[k], RX[k - 1], D);
         DY[k] = wrapd(RY[k], RY[k - 1], D);
-        AX[k] = AX[k - 1] + DX[k];
-        AY[k] = AY[k - 1] + DY[k];
+        AX[k] = k == 1 ? zero_plus(DX[k]) : AX[k - 1] + DX[k];   /* AX[0] = +0 */
+        AY[k] = k == 1 ? zero_plus(DY[k]) : AY[k - 1] + DY[k];
     }
     double acc = 0;                    /* terms 0 and N-1 involve the origin */
     S[0] = 0;
 #pragma unroll
     for (int k = 1; k < N - 1; k++) {
-        acc += AX[k] * AY[k + 1] - AY[k] * AX[k + 1];
+        double term = AX[k] * AY[k + 1] - AY[k] * AX[k + 1];
+        acc = k == 1 ? zero_plus(term) : acc + term;
         S[k] = acc;
     }
     acc = add_closing_term(acc, AX[N - 1], AY[N - 1]);
@@ -344,7 +346,14 @@ __global__ void k_grain_fd(DevMesh m)
 }
 
 /* vertex pass: src/calculus.h:19-73 (boundary part) and :143-154;
- * vertex_compute_energy src/geometry.h:472-479 */
+ * vertex_compute_energy src/geometry.h:472-479.
+ *
+ * UNIT_GAMMA: every boundary energy is exactly 1 this step (isotropic
+ * boundaries, GB_scaling = 1: the geometry pass wrote 1 * 1 into every
+ * enabled boundary), so the products gamma * x are x and are skipped.
+ * Sums that the reference starts from 0.0 take their first term through
+ * zero_plus, which keeps the first addition off the FP64 pipe. */
+template <bool UNIT_GAMMA>
 __global__ void k_vertex_fd(DevMesh m, double mu)
 {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,10 +378,13 @@ __global__ void k_vertex_fd(DevMesh m, double mu)
         np.x = dmod(np.x, m.D);
         np.y = dmod(np.y, m.D);
         double bt = 0.0, gt = 0.0;
+#pragma unroll
         for (int j = 0; j < 3; j++) {
             double Lj = arclen(np, q[j], m.D);
-            bt += (gam[j] * (Lj - len[j]));
-            gt += (c == 0 ? cg[j].x : cg[j].y);
+            double term = UNIT_GAMMA ? (Lj - len[j]) : (gam[j] * (Lj - len[j]));
+            double gj = c == 0 ? cg[j].x : cg[j].y;
+            if (j == 0) { bt = zero_plus(term); gt = zero_plus(gj); }
+            else { bt += term; gt += gj; }
         }
         if (c == 0) { t.bx = bt; t.gx = gt; } else { t.by = bt; t.gy = gt; }
         vel[c] = div_grad_eps(-(bt + gt));
@@ -381,9 +393,11 @@ __global__ void k_vertex_fd(DevMesh m, double mu)
     m.terms[v] = t;
     m.vel[v] = make_double2(vel[0], vel[1]);
     double e = 0.0;
+#pragma unroll
     for (int j = 0; j < 3; j++) {
         int g = slot3(sg, j);
-        e += dscale_down<1>(len[j] * gam[j]);
+        double ej = dscale_down<1>(UNIT_GAMMA ? len[j] : (len[j] * gam[j]));
+        e = j == 0 ? zero_plus(ej) : e + ej;
         e += g >= 0 ? m.gq[g] : 0.0;
     }
     m.venergy[v] = e;
@@ -594,21 +608,28 @@ void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cons
     int t = sh.tpb_boundary;
     COUNT_LAUNCHES(1), k_boundary_geometry<<<(m.nb + t - 1) / t, t, 0, s>>>(m, eps, scaling);
 }
-void launch_grain_fd(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
+void launch_grain_sort(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
     COUNT_LAUNCHES(1), k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
     COUNT_LAUNCHES(1), k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
+}
+void launch_grain_fd_wide(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
+{
     COUNT_LAUNCHES(1), k_grain_fd_wide<<<2 * 152, 32 * WIDE_WARPS, 0, s>>>(m, x.perm, x.vbucket, x.n_perm, sh.wide_sides);
+}
+void launch_grain_fd_sorted(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
+{
     COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
 }
 
 /* the unsorted per-grain pass, kept for A/B timing */
 void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_vertex_fd(const DevMesh &m, double mu, const LaunchShape &sh, cudaStream_t s)
+void launch_vertex_fd(const DevMesh &m, double mu, bool unit_gamma, const LaunchShape &sh, cudaStream_t s)
 {
     int t = sh.tpb_vertex;
-    COUNT_LAUNCHES(1), k_vertex_fd<<<(m.nv + t - 1) / t, t, 0, s>>>(m, mu);
+    if (unit_gamma) COUNT_LAUNCHES(1), k_vertex_fd<true><<<(m.nv + t - 1) / t, t, 0, s>>>(m, mu);
+    else COUNT_LAUNCHES(1), k_vertex_fd<false><<<(m.nv + t - 1) / t, t, 0, s>>>(m, mu);
 }
 void launch_full_flag(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {

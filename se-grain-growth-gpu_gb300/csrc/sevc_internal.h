@@ -66,8 +66,14 @@ struct StepParams {
 
 /* geometry (sevc_geometry.cu) */
 void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, const LaunchShape &sh, cudaStream_t s);
-void launch_grain_fd(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s);
-void launch_vertex_fd(const DevMesh &m, double mu, const LaunchShape &sh, cudaStream_t s);
+/* grain pass: side-count order (x.perm / x.vbucket), then the warp-per-grain
+ * kernel for grains of wide_sides or more and the thread-per-grain kernel
+ * for the rest (disjoint grains: the two may run concurrently) */
+void launch_grain_sort(const DevMesh &m, const DevScratch &x, cudaStream_t s);
+void launch_grain_fd_wide(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s);
+void launch_grain_fd_sorted(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s);
+/* unit_gamma: every boundary energy is exactly 1 (GB_eps = 0, GB_scaling = 1) */
+void launch_vertex_fd(const DevMesh &m, double mu, bool unit_gamma, const LaunchShape &sh, cudaStream_t s);
 /* side-count histogram layout in DevScratch::vbucket */
 #define VB_START(b) (32 + (b))
 #define VB_COUNT(b) (48 + (b))
