@@ -315,7 +315,7 @@ NCU_TRAFFIC_PER_UNIT = {
 NCU_FP64_ACTIVE = {"grain_fd": 0.726, "vertex_fd": 0.783}
 # DADD + DMUL + DFMA thread instructions per unit, ncu counters on the
 # 200K-grain mesh (the FP64 instruction summary kept with the profiles)
-NCU_FP64_INST_PER_UNIT = {"grain_fd": (54.652e6 + 0.702e6) / 200000, "vertex_fd": 48.405e6 / 400000}
+NCU_FP64_INST_PER_UNIT = {"grain_fd": (54.652e6 + 0.702e6) / 200000, "vertex_fd": 39.605e6 / 400000}
 
 
 def run_engine(args):

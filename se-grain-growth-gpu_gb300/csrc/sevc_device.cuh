@@ -236,17 +236,18 @@ __device__ __forceinline__ double wrapd(double dest, double orig, double D) /* w
 }
 /* ---- correctly rounded division and square root for vector2_mag ----
  * On GB300 a binary64 division or square root costs ~10-12 FP64
- * instructions (ncu: 22 for the pair).  These versions take a binary32
- * seed from the special-function unit, refine it on the FP32 pipe to a
- * float-float value of ~45 bits, finish with two FP64 correction steps
+ * instructions (ncu: 16 for the pair).  These versions take a binary32
+ * seed from the special-function unit and refine it on the FP32 pipe to a
+ * float-float approximation of the result (~45 bits), assembled into a
+ * binary64 on the integer pipe; one FP64 correction step follows
  * (Markstein's method: P. Markstein, "IA-64 and elementary functions",
  * 2000, ch. 8; J.-M. Muller et al., Handbook of Floating-Point Arithmetic,
- * 2nd ed., 2018, sec. 4.7) and then CERTIFY the result exactly: the
+ * 2nd ed., 2018, sec. 4.7) and then the result is CERTIFIED exactly: the
  * remainder of the candidate is computed with one fma and compared, on the
  * integer pipe, with the half-ulp bound that characterises round-to-nearest.
  * A candidate that is not certified (about one in 10^4, or special
  * operands) is discarded and the native operation runs, so the returned
- * value is always the correctly rounded one.  5 FP64 instructions each. */
+ * value is always the correctly rounded one.  3 FP64 instructions each. */
 
 /* binary32 -> binary64 by bit manipulation (exact for normal x; zero and
  * subnormal x give 0, an error the certification absorbs) */
@@ -264,6 +265,32 @@ __device__ __forceinline__ void split_unit(long long b, float &hi, float &lo)
 {
     hi = __uint_as_float(0x3F800000u | (unsigned)((b >> 29) & 0x7fffffLL));
     lo = __uint2float_rn((unsigned)(b & 0x1fffffffLL)) * 0x1p-52f;
+}
+/* the same for a positive binary64 of biased exponent 949..1150 */
+__device__ __forceinline__ void split_pos(long long b, float &hi, float &lo)
+{
+    unsigned eb = (unsigned)(b >> 52);
+    hi = __uint_as_float(((eb - 896u) << 23) | (unsigned)((b >> 29) & 0x7fffffLL));
+    lo = __uint2float_rn((unsigned)(b & 0x1fffffffLL)) * __uint_as_float((eb - 948u) << 23);
+}
+/* hi + lo as a binary64, on the integer pipe, for binary32 hi > 0 (normal)
+ * and |lo| < 2^-8 hi: the 53-bit significand of hi plus lo's significand
+ * shifted into its units, renormalised by one bit if needed.  Bits of lo
+ * below hi's 53-bit window are cut: the result is within 2^-52 (relative)
+ * of hi + lo. */
+__device__ __forceinline__ double ff_to_double(float hi, float lo)
+{
+    unsigned uh = __float_as_uint(hi), ul = __float_as_uint(lo);
+    int eh = (int)(uh >> 23), el = (int)((ul >> 23) & 0xffu);
+    long long M = (long long)((uh & 0x7fffffu) | 0x800000u) << 29;
+    long long ml = (long long)((ul & 0x7fffffu) | 0x800000u);
+    int s = el - eh + 29;
+    long long add = (el == 0 || s <= -24) ? 0LL : (s >= 0 ? (ml << s) : (ml >> -s));
+    M += (int)ul < 0 ? -add : add;
+    int e = eh + 896;
+    if (M >= (1LL << 53)) { M >>= 1; e++; }
+    else if (M < (1LL << 52)) { M <<= 1; e--; }
+    return __longlong_as_double(((long long)e << 52) | (M & 0x000FFFFFFFFFFFFFLL));
 }
 __device__ __forceinline__ float rcp_seed(float x)
 {
@@ -284,18 +311,24 @@ __device__ __forceinline__ bool div_fast(double q, double p, double &r)
     long long pb = dbits(p), qb = dbits(q);
     if (qb == 0) { r = 0.0; return true; }                /* q = +0 */
     int ep = (int)(pb >> 52), eq = (int)(qb >> 52);
-    if (eq < 1 || eq > ep || ep > 2046 || ep - eq > 900) return false;
-    /* P = p scaled into [1, 2), Q = q by the same power of two: Q / P = q / p */
+    if (eq < 1 || eq > ep || ep > 2046 || ep - eq > 60) return false;
+    /* P = p scaled into [1, 2), Q = q by the same power of two (Q / P =
+     * q / p, Q >= 2^-60) */
     double P = __longlong_as_double((pb & 0x000FFFFFFFFFFFFFLL) | (1023LL << 52));
     double Q = __longlong_as_double(qb - (long long)(ep - 1023) * (1LL << 52));
-    float ph, pl;
+    float ph, pl, qh, ql;
     split_unit(dbits(P), ph, pl);
+    split_pos(dbits(Q), qh, ql);
     float y0 = rcp_seed(ph);                              /* 1/P to ~2^-23 */
     float e = fmaf(-ph, y0, 1.0f);
     e = fmaf(-pl, y0, e);                                 /* 1 - P y0 to ~2^-46 */
     float yl = y0 * e;                                    /* 1/P ~ y0 + yl to ~2^-45 */
-    double y0d = f2d_bits(y0), yld = f2d_bits(yl);
-    double q0 = __fma_rn(Q, yld, __dmul_rn(Q, y0d));      /* ~2^-45 */
+    float ah = qh * y0;                                   /* Q (y0 + yl) as ah + al */
+    float al = fmaf(qh, y0, -ah);
+    al = fmaf(qh, yl, al);
+    al = fmaf(ql, y0, al);
+    double y0d = f2d_bits(y0);
+    double q0 = ff_to_double(ah, al);                     /* ~2^-44 */
     double rem = __fma_rn(-P, q0, Q);
     double q1 = __fma_rn(rem, y0d, q0);                   /* ~2^-67 */
     double rem1 = __fma_rn(-P, q1, Q);                    /* exact when q1 is faithful */
@@ -329,8 +362,12 @@ __device__ __forceinline__ bool sqrt_fast(double t, double &r)
     e = fmaf(-th, al, e);
     e = fmaf(-tl, ah, e);                                 /* 1 - t y0^2 to ~2^-46 */
     float yl = 0.5f * (y0 * e);                           /* Newton: 1/sqrt(t) ~ y0 + yl */
-    double y0d = f2d_bits(y0), yld = f2d_bits(yl);
-    double s0 = __fma_rn(t, yld, __dmul_rn(t, y0d));      /* sqrt(t) to ~2^-45 */
+    float sh = th * y0;                                   /* t (y0 + yl) as sh + sl */
+    float sl = fmaf(th, y0, -sh);
+    sl = fmaf(th, yl, sl);
+    sl = fmaf(tl, y0, sl);
+    double y0d = f2d_bits(y0);
+    double s0 = ff_to_double(sh, sl);                     /* sqrt(t) to ~2^-44 */
     double d = __fma_rn(-s0, s0, t);
     double s1 = __fma_rn(d, __longlong_as_double(dbits(y0d) - (1LL << 52)), s0);   /* + d y0/2: ~2^-67 */
     double e1 = __fma_rn(-s1, s1, t);
