@@ -174,6 +174,87 @@ __global__ void k_compact_scatter(DevMesh m, int n, const int *blockcnt, int *ou
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *n_out = off;
 }
 
+/* The same compaction for the kinds whose predicate is a byte flag (or the
+ * AND of two): each thread owns 16 consecutive items, read as one 16-byte
+ * word per flag array, so a tile costs one round trip to memory instead of
+ * sixteen.  Items keep ascending order (thread order, then bit order).
+ * Flag arrays are allocated in 256-byte multiples, so the word of the last
+ * partial group stays inside its allocation; items >= n are masked off. */
+template <int KIND>
+__device__ __forceinline__ unsigned flag_mask16(const DevMesh &m, int i0, int n)
+{
+    const uint8_t *a = KIND == CK_CAND ? m.ben : (KIND == CK_GRAIN_CAND ? m.gen : m.bmark);
+    uint4 w = *reinterpret_cast<const uint4 *>(a + i0);
+    if constexpr (KIND == CK_CAND || KIND == CK_GRAIN_CAND) {
+        const uint8_t *b = KIND == CK_CAND ? m.bcand : m.gcand;
+        uint4 v = *reinterpret_cast<const uint4 *>(b + i0);
+        w.x &= v.x; w.y &= v.y; w.z &= v.z; w.w &= v.w;   /* flags are 0 / 1 */
+    }
+    unsigned q[4] = { w.x, w.y, w.z, w.w }, mask = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            mask |= (((q[j] >> (8 * k)) & 0xffu) != 0u ? 1u : 0u) << (4 * j + k);
+    int valid = n - i0;
+    return valid >= 16 ? mask : (mask & ((1u << valid) - 1u));
+}
+template <int KIND>
+__global__ void k_flag_count(DevMesh m, int n, int *blockcnt)
+{
+    int i0 = (blockIdx.x * TPB + threadIdx.x) * CT_ITEMS;
+    int c = i0 < n ? __popc(flag_mask16<KIND>(m, i0, n)) : 0;
+    __shared__ int s[TPB / 32];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < TPB / 32; w++) t += s[w];
+        blockcnt[blockIdx.x] = t;
+    }
+}
+template <int KIND>
+__global__ void k_flag_scatter(DevMesh m, int n, const int *blockcnt, int *out, int *n_out)
+{
+    __shared__ int s[TPB / 32];
+    __shared__ int base_off, tot;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int part = 0;
+    for (int j = threadIdx.x; j < (int)blockIdx.x; j += TPB) part += blockcnt[j];
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    if (lane == 0) s[warp] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < TPB / 32; w++) t += s[w];
+        base_off = t;
+    }
+    __syncthreads();
+    int i0 = (blockIdx.x * TPB + threadIdx.x) * CT_ITEMS;
+    unsigned mask = i0 < n ? flag_mask16<KIND>(m, i0, n) : 0u;
+    int c = __popc(mask), incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int w = 0; w < TPB / 32; w++) { int t = s[w]; s[w] = acc; acc += t; }
+        tot = acc;
+    }
+    __syncthreads();
+    int pos = base_off + s[warp] + incl - c;
+    while (mask) {
+        int k = __ffs(mask) - 1;
+        mask &= mask - 1;
+        out[pos++] = i0 + k;
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *n_out = base_off + tot;
+}
+
 /* ------------------------------------------------------------------ */
 /* polling system, src/topological.h:362-578                           */
 /* ------------------------------------------------------------------ */
@@ -680,6 +761,44 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
     m.vel[B] = make_double2(0, 0);
 }
 
+/* Before lane 0 applies a flip (one long chain of dependent loads), the
+ * warp brings the flip's neighbourhood into the SM's L1 in a few parallel
+ * rounds: the two vertices' slots, positions and velocities; the boundary
+ * ends and grain records around them; the lists of those grains; and the
+ * positions, velocities and save stamps of the listed vertices (read by
+ * finalize_grain).  Loads only, every index checked against its array. */
+__device__ __forceinline__ void touch(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ void prefetch_flip(const DevMesh &m, int bnd, int lane)
+{
+    int2 e = m.bv[bnd];
+    if (e.x < 0 || e.x >= m.nv || e.y < 0 || e.y >= m.nv) return;
+    int4 gA = m.vg[e.x], gB = m.vg[e.y], bA = m.vb[e.x], bB = m.vb[e.y];
+    int gs[6] = { gA.x, gA.y, gA.z, gB.x, gB.y, gB.z }, bs[6] = { bA.x, bA.y, bA.z, bB.x, bB.y, bB.z };
+    if (lane < 6) {
+        int g = gs[lane];
+        if (g >= 0 && g < m.ng) { touch(m.gvlen + g); touch(m.gexact + g); touch(m.gfix + g); }
+        int b = bs[lane];
+        if (b >= 0 && b < m.nb) touch(m.bv + b);
+    } else if (lane < 8) {
+        int v = lane == 6 ? e.x : e.y;
+        touch(m.pos + v); touch(m.vel + v); touch(m.vstamp + v); touch(m.vmod + 4 * (size_t)v);
+    }
+    /* lists of the grains: lane 5k + j reads entries j, j + 5, ... of grain k */
+    int k = lane / 5, j = lane % 5;
+    if (k < 6) {
+        int g = gs[k];
+        if (g >= 0 && g < m.ng) {
+            int n = m.gvlen[g];
+            n = n < SEVC_MAXV ? n : SEVC_MAXV;
+            const int *L = m.glist + (size_t)SEVC_MAXV * g;
+            for (int i = j; i < n; i += 5) {
+                int v = L[i];
+                if (v >= 0 && v < m.nv) { touch(m.pos + v); touch(m.vel + v); touch(m.vstamp + v); }
+            }
+        }
+    }
+}
+
 /* apply_flippings (:1016-1026); flips that share no vertex commute, the
  * rest are applied in ascending boundary order */
 /* One warp per instance.  A flip changes no boundary's enabled or
@@ -689,19 +808,32 @@ __global__ void k_flips(DevMesh m, double eps, const int *list, const int *n)
 {
     int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (inst >= m.ninst) return;
-    int lo = lower_bound_i(list, *n, m.boff[inst]);
-    int hi = lower_bound_i(list, *n, m.boff[inst + 1]);
+    int lo = 0, hi = *n;
+    if (m.ninst > 1) {
+        lo = lower_bound_i(list, hi, m.boff[inst]);
+        hi = lower_bound_i(list, hi, m.boff[inst + 1]);
+    }
     for (int base = lo; base < hi; base += 32) {
         int i = base + lane;
-        bool f = i < hi && m.ben[list[i]] && m.bcand[list[i]];
+        bool f = false;
+        if (i < hi) {
+            int b = list[i];
+            uint8_t en = m.ben[b], ca = m.bcand[b];   /* both loads in flight together */
+            f = en && ca;
+        }
         unsigned hits = __ballot_sync(0xffffffffu, f);
-        if (lane == 0)
-            while (hits) {
-                int j = __ffs(hits) - 1;
-                hits &= hits - 1;
-                flip_dev(m, list[base + j], eps);
+        while (hits) {
+            int j = __ffs(hits) - 1;
+            hits &= hits - 1;
+            int b = list[base + j];
+            prefetch_flip(m, b, lane);
+            __syncwarp();
+            if (lane == 0) {
+                flip_dev(m, b, eps);
                 m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
             }
+            __syncwarp();
+        }
         __syncwarp();
     }
 }
@@ -801,8 +933,18 @@ void compact_impl(const DevMesh &m, const DevScratch &x, int n, int *out, int *n
 {
     int tiles = (n + CT_TILE - 1) / CT_TILE;
     if (tiles == 0) { cudaMemsetAsync(n_out, 0, sizeof(int), s); return; }
-    k_compact_count<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt);
-    k_compact_scatter<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt, out, n_out);
+    /* the 16-byte flag reads need 16-byte aligned arrays (the handle's
+     * allocation gives 256) */
+    uintptr_t al = KIND == CK_CAND ? ((uintptr_t)m.ben | (uintptr_t)m.bcand)
+                 : KIND == CK_GRAIN_CAND ? ((uintptr_t)m.gen | (uintptr_t)m.gcand) : (uintptr_t)m.bmark;
+    bool flags16 = (KIND == CK_CAND || KIND == CK_GRAIN_CAND || KIND == CK_MARKED) && (al & 15u) == 0;
+    if (flags16) {
+        COUNT_LAUNCHES(1), k_flag_count<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt);
+        COUNT_LAUNCHES(1), k_flag_scatter<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt, out, n_out);
+    } else {
+        COUNT_LAUNCHES(1), k_compact_count<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt);
+        COUNT_LAUNCHES(1), k_compact_scatter<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt, out, n_out);
+    }
 }
 
 inline int listgrid(int cap) { int g = (cap + TPB - 1) / TPB; return g < 4 * WL_BLOCKS ? g : 4 * WL_BLOCKS; }
