@@ -545,6 +545,12 @@ __device__ __forceinline__ double text_exact(double2 pi, double2 pe, double2 vi,
     double aux = tx * (ve.x - vi.x) + ty * (ve.y - vi.y);
     return (aux == 0) ? 100 : -norm / aux;
 }
+/* text_exact as a call, for kernels where it is the rare branch (keeps its
+ * FP64 work from being speculated into the common path) */
+static __device__ __noinline__ double text_exact_call(double2 pi, double2 pe, double2 vi, double2 ve, double D)
+{
+    return text_exact(pi, pe, vi, ve, D);
+}
 
 /* binary64 -> binary32 by cutting the significand, on the integer pipe:
  * for 2^-126 <= |x| < 2^128 the result has x's sign and

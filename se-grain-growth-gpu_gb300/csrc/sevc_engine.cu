@@ -521,16 +521,18 @@ void enqueue_poll(sevc_handle *h)
     launch_poll_iteration(h->m, h->x, h->x.list_a, h->x.n_a, h->p, h->stream);
 }
 
-/* from the 3-sided labels to the end of the step (src/main.cu:252-325) */
-void enqueue_tail(sevc_handle *h)
+/* from the 3-sided labels to the end of the step (src/main.cu:252-325);
+ * lists_unchanged: no 2x3 removal edited a list since the side-count order */
+void enqueue_tail(sevc_handle *h, bool lists_unchanged)
 {
     cudaStream_t s = h->stream;
     const sevc_options &o = h->opt;
     DevMesh &m = h->m;
     DevScratch &x = h->x;
-    { Prof pr(h, "label_3sided"); launch_label_3sided(m, o.dt, s); }                              /* :252-255 */
+    { Prof pr(h, "label_3sided"); launch_label_3sided(m, x, o.dt, lists_unchanged, s); }        /* :252-255 */
     { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
     { Prof pr(h, "remove_grains"); launch_remove_grains(m, x.list_c, x.n_c, s); }                 /* :259 */
+    launch_clear_grain_cand(m, x.list_c, x.n_c, s);
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
     { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
     { Prof pr(h, "unlabel_st2"); launch_unlabel_st2(m, x.list_a, x.n_a, s); }                     /* :282 */
@@ -545,7 +547,7 @@ void enqueue_tail(sevc_handle *h)
 void enqueue_post(sevc_handle *h)
 {
     { Prof pr(h, "conflicts"); launch_conflicts(h->m, h->x.list_a, h->x.n_a, h->stream); }         /* :222-225 */
-    enqueue_tail(h);
+    enqueue_tail(h, true);
 }
 
 sevc_status err_bits_to_status(int bits)
@@ -791,7 +793,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
             { Prof pr(h, "two_three_remove"); launch_remove_two_three(m, x, x.list_b, x.n_b, k, s); }
             { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }
         }
-        enqueue_tail(h);
+        enqueue_tail(h, false);
     }
     cudaEventRecord(h->ev1, s);
 

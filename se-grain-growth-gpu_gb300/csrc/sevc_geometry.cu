@@ -435,27 +435,16 @@ __device__ void dadt_of(const DevMesh &m, int g)
  * labels (this kernel's and label_3sided's) see what they would see; the
  * value itself is not observed: exports happen only on steps that compute
  * every value, and a boundary an event disables gets its exact value then
- * (finalize_boundary).
- *
- * Certificate.  With d the unwrapped edge vector, P = v_end - v_ini and
- * s = d.P, the reference's denominator is aux = T.P with T = (cos, sin) of
- * atan2(d): |aux - s/|d|| <= 16u(|Px|+|Py|) + rounding (u = 2^-53, a few
- * ulp of libm error per component).  The boundary is a candidate iff
- * aux <= -|d|/dt (then t = -|d|/aux lies in [0, dt]).  So if
- *   s > -|d|^2/dt + margin,
- *   margin = 1e-12 |d|^2/dt + 1e-14 (|dx|+|dy|)(|Px|+|Py|) + 1e-15 (|dx Px| + |dy Py|)
- * (each term at least five times the error it covers) it is not one.
+ * (finalize_boundary).  The proof that a boundary is not a candidate is the
+ * binary32 certificate text_outside_dt.
  */
-__global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, const int *flags)
+__device__ __forceinline__ void text_label_one(const DevMesh &m, int b, uint8_t en, double2 pi, double2 pe,
+                                               double2 vi, double2 ve, double dt, float Df, float hDf, float inv_dt,
+                                               int full)
 {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= m.nb) return;
-    double text;
-    if (m.ben[b]) {
-        int2 e = m.bv[b];
-        double2 pi = m.pos[e.x], pe = m.pos[e.y];
-        double2 vi = m.vel[e.x], ve = m.vel[e.y];
-        if (!flags[0] && text_outside_dt(pi, pe, vi, ve, Df, hDf, inv_dt)) {
+    long long tb;
+    if (en) {
+        if (!full && text_outside_dt(pi, pe, vi, ve, Df, hDf, inv_dt)) {
             /* not a candidate: its t_ext is outside [0, dt]; the value
              * itself is only observed if an event disables the boundary,
              * which then computes it (finalize_boundary) */
@@ -465,14 +454,38 @@ __global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float in
             m.bconf[b] = -1;
             return;
         }
-        text = text_exact(pi, pe, vi, ve, m.D);
+        double text = text_exact_call(pi, pe, vi, ve, m.D);
         m.btext[b] = text;
         m.bexact[b] = 1;
+        tb = dbits(text);
     } else {
-        text = m.btext[b];
+        tb = dbits(m.btext[b]);
     }
-    m.bcand[b] = (text >= 0 && text <= dt) ? 1 : 0;
+    /* text >= 0 && text <= dt on the bit pattern (dt > 0): +-0, or a
+     * non-negative pattern not above dt's; NaN fails as in the comparison.
+     * Written in PTX so that it stays two integer comparisons (as C the
+     * compiler may turn it back into FP64 ones). */
+    unsigned cand;
+    asm("{\n\t.reg .pred p, q, z;\n\t"
+        "setp.ge.s64 p, %1, 0;\n\t"
+        "setp.le.s64 q, %1, %2;\n\t"
+        "setp.eq.s64 z, %1, 0x8000000000000000;\n\t"
+        "and.pred p, p, q;\n\t"
+        "or.pred p, p, z;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(cand) : "l"(tb), "l"(dbits(dt)));
+    m.bcand[b] = (uint8_t)cand;
     m.bconf[b] = -1;
+}
+__global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, const int *flags)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.nb) return;
+    uint8_t en = m.ben[b];
+    int2 e = m.bv[b];                      /* loaded beside the flag: one round trip less */
+    double2 z = make_double2(0, 0), pi = z, pe = z, vi = z, ve = z;
+    if (en) { pi = m.pos[e.x]; pe = m.pos[e.y]; vi = m.vel[e.x]; ve = m.vel[e.y]; }
+    text_label_one(m, b, en, pi, pe, vi, ve, dt, Df, hDf, inv_dt, flags[0]);
 }
 
 /* compute_grain_areas, src/calculus.h:224 */
@@ -646,7 +659,7 @@ void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const L
     /* binary32 copies for the certificate (text_outside_dt): rounded to
      * nearest, within 2^-24 of the binary64 values */
     float Df = (float)m.D, hDf = (float)(m.D / 2.0), inv_dt = (float)(1.0 / dt);
-    COUNT_LAUNCHES(1), k_text_label<<<(m.nb + t - 1) / t, t, 0, s>>>(m, dt, Df, hDf, inv_dt, x.flags);
+    if (m.nb > 0) COUNT_LAUNCHES(1), k_text_label<<<(m.nb + t - 1) / t, t, 0, s>>>(m, dt, Df, hDf, inv_dt, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)

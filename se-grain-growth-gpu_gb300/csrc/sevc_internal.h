@@ -103,8 +103,12 @@ void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaS
 /* pass `pass` of the 2x3 loop (per-instance counts go to x.segcnt) */
 void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, int pass,
                              cudaStream_t s);
-void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s);
+/* bucket: no grain list changed since this step's side-count order, so
+ * only its 3-sided bucket is visited */
+void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool bucket, cudaStream_t s);
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s);
+/* clears the candidate flag of every listed grain (after the removals) */
+void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cudaStream_t s);
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s);
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s);

@@ -318,6 +318,40 @@ __global__ void k_poll_compare_write(DevMesh m, int *threadfail, int grid)
     if (en && c != m.bcandbuf[b]) threadfail[(size_t)inst * grid + (b - m.boff[inst]) % grid] = 1;
     m.bcandbuf[b] = en ? c : 0;
 }
+/* The same for a single instance: 16 consecutive boundaries per thread,
+ * the three flag arrays read and the buffer written as 16-byte words
+ * (allocations are 256-byte multiples; bytes past nb are written back
+ * unchanged).  grid >= 16. */
+__global__ void k_poll_compare_write16(DevMesh m, int *threadfail, int grid)
+{
+    int b0 = (blockIdx.x * blockDim.x + threadIdx.x) * 16;
+    if (b0 >= m.nb || m.pdone[0]) return;
+    uint4 we = *reinterpret_cast<const uint4 *>(m.ben + b0);
+    uint4 wc = *reinterpret_cast<const uint4 *>(m.bcand + b0);
+    uint4 wb = *reinterpret_cast<const uint4 *>(m.bcandbuf + b0);
+    unsigned e4[4] = { we.x, we.y, we.z, we.w }, c4[4] = { wc.x, wc.y, wc.z, wc.w }, b4[4] = { wb.x, wb.y, wb.z, wb.w };
+    int slot = b0 % grid;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        unsigned nb4 = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int i = 4 * j + k;
+            unsigned e = (e4[j] >> (8 * k)) & 0xffu, c = (c4[j] >> (8 * k)) & 0xffu, o = (b4[j] >> (8 * k)) & 0xffu;
+            unsigned nbyte = o;
+            if (b0 + i < m.nb) {
+                if (e && c != o) {
+                    int t = slot + i;
+                    threadfail[t >= grid ? t - grid : t] = 1;
+                }
+                nbyte = e ? c : 0u;
+            }
+            nb4 |= nbyte << (8 * k);
+        }
+        b4[j] = nb4;
+    }
+    *reinterpret_cast<uint4 *>(m.bcandbuf + b0) = make_uint4(b4[0], b4[1], b4[2], b4[3]);
+}
 /* part two, on the reference's grid (blockIdx.y = instance): per thread
  * AND over its stride set (already folded into threadfail), per block the
  * shared-memory tree whose bool += acts as OR (compare_candidates
@@ -554,32 +588,51 @@ __global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int
 /* ------------------------------------------------------------------ */
 /* 3-sided grain removal, src/topological.h:614-822, :994-1004         */
 /* ------------------------------------------------------------------ */
+/* label_3sided_grains (:994-1004) for one 3-sided grain */
+__device__ uint8_t label3_cand(const DevMesh &m, int g, double dt)
+{
+    uint8_t cand = 0;
+    const int *L = m.glist + (size_t)SEVC_MAXV * g;
+    int l0 = L[0], l1 = L[1], l2 = L[2];
+    int ans = 0;
+    for (int i = 0; i < 3; i++) {
+        int4 s = m.vb[L[i]];
+        for (int k = 0; k < 3; k++) {
+            int b = slot3(s, k);
+            int2 e = m.bv[b];
+            bool ii = e.x == l0 || e.x == l1 || e.x == l2;
+            bool ee = e.y == l0 || e.y == l1 || e.y == l2;
+            if (ii && ee && m.bcand[b] && m.ben[b]) { cand = 1; break; }
+            double t = m.btext[b];
+            if (ii && ee && (t >= 0 && t <= dt) && m.ben[b]) ans++;
+        }
+    }
+    ans /= 2;
+    if (ans == 3) cand = 1;
+    return cand;
+}
 /* clear_grains_state + label_3sided_grains for enabled grains */
 __global__ void k_label_3sided(DevMesh m, double dt)
 {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= m.ng || !m.gen[g]) return;
-    uint8_t cand = 0;
-    if (m.gvlen[g] == 3) {
-        const int *L = m.glist + (size_t)SEVC_MAXV * g;
-        int l0 = L[0], l1 = L[1], l2 = L[2];
-        int ans = 0;
-        for (int i = 0; i < 3; i++) {
-            int4 s = m.vb[L[i]];
-            for (int k = 0; k < 3; k++) {
-                int b = slot3(s, k);
-                int2 e = m.bv[b];
-                bool ii = e.x == l0 || e.x == l1 || e.x == l2;
-                bool ee = e.y == l0 || e.y == l1 || e.y == l2;
-                if (ii && ee && m.bcand[b] && m.ben[b]) { cand = 1; break; }
-                double t = m.btext[b];
-                if (ii && ee && (t >= 0 && t <= dt) && m.ben[b]) ans++;
-            }
-        }
-        ans /= 2;
-        if (ans == 3) cand = 1;
+    m.gcand[g] = m.gvlen[g] == 3 ? label3_cand(m, g, dt) : 0;
+}
+/* The same when no list changed since this step's side-count order: only
+ * the grains of its 3-sided bucket are visited.  Every other enabled grain
+ * already has gcand = 0, because each step clears the flag of every grain
+ * it listed as a candidate (k_clear_grain_cand). */
+__global__ void k_label_3sided_bucket(DevMesh m, double dt, const int *perm, const int *vbucket)
+{
+    int n3 = vbucket[VB_COUNT(3)], start = vbucket[VB_START(3)];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+        int g = perm[start + i];
+        m.gcand[g] = label3_cand(m, g, dt);
     }
-    m.gcand[g] = cand;
+}
+__global__ void k_clear_grain_cand(DevMesh m, const int *list, const int *n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) m.gcand[list[i]] = 0;
 }
 
 /* remove_grain (:687-822) */
@@ -978,7 +1031,13 @@ void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *can
     COUNT_LAUNCHES(1), k_poll_count<<<g, TPB, 0, s>>>(m, cand, ncand);
     COUNT_LAUNCHES(1), k_poll_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
     int grid = p.n_blocks * p.n_threads;
-    COUNT_LAUNCHES(1), k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+    bool aligned = (((uintptr_t)m.ben | (uintptr_t)m.bcand | (uintptr_t)m.bcandbuf) & 15u) == 0;
+    if (p.ninst == 1 && grid >= 16 && aligned) {
+        int th = (m.nb + 15) / 16;
+        COUNT_LAUNCHES(1), k_poll_compare_write16<<<(th + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+    } else {
+        COUNT_LAUNCHES(1), k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+    }
     COUNT_LAUNCHES(1), k_poll_final<<<dim3(p.n_blocks, p.ninst), p.n_threads, 0, s>>>(m, x.threadfail, x.pblock);
     cudaMemsetAsync(x.nrun, 0, sizeof(int), s);
     COUNT_LAUNCHES(1), k_poll_status<<<(p.ninst + 127) / 128, 128, 0, s>>>(m, x.pblock, p.n_blocks, x.piters, x.nrun);
@@ -1000,9 +1059,18 @@ void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *l
                                                                      x.segcnt + (size_t)pass * m.ninst);
 }
 
-void launch_label_3sided(const DevMesh &m, double dt, cudaStream_t s)
+void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool bucket, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_label_3sided<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, dt);
+    if (bucket) {
+        int g = (m.ng + TPB - 1) / TPB;
+        COUNT_LAUNCHES(1), k_label_3sided_bucket<<<g < 4 * 152 ? g : 4 * 152, TPB, 0, s>>>(m, dt, x.perm, x.vbucket);
+    } else {
+        COUNT_LAUNCHES(1), k_label_3sided<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, dt);
+    }
+}
+void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_clear_grain_cand<<<32, TPB, 0, s>>>(m, list, n);
 }
 
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
