@@ -372,6 +372,7 @@ __global__ void k_vertex_fd(DevMesh m, double mu)
     for (int j = 0; j < 3; j++) cg[j] = m.contrib[3 * v + j];
     DevMesh::FdTerms t;
     double vel[2];
+#pragma unroll
     for (int c = 0; c < 2; c++) {
         double2 np = p;
         if (c == 0) np.x += SEVC_GRAD_EPS_D; else np.y += SEVC_GRAD_EPS_D;
