@@ -401,6 +401,7 @@ def run_engine(args):
                    "nucleation_attempts": sum(i.nucleation_attempted for i in infos),
                    "mesh_generation_s": round(gen_s, 1), "wall_s": round(wall, 3),
                    "launch_shapes": {"tpb_vertex": shapes[0], "tpb_boundary": shapes[1], "wide_sides": shapes[2],
+                                     "grain_blocks_per_sm": shapes[3],
                                      "picked_by": "sevc_autotune, 3 steps per candidate"},
                    "launch_mode": "CUDA graphs"},
         "e2e": {"value": e_vsteps / e_wall, "unit": UNIT, "h2d_bytes_per_step": host_bytes / args.steps,

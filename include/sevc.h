@@ -273,10 +273,12 @@ sevc_status sevc_set_graphs(sevc_handle *h, int on);
 
 /* Launch-shape autotuner (no counterpart in the reference): times `steps`
  * steps from the current state for each candidate block size of the
- * vertex pass (128/256/512) and of the per-boundary passes, and each side
- * count from which grains get a warp each (9..12), one parameter at a
- * time, keeps the fastest and restores the state.  chosen (3 ints, may be
- * NULL) receives them.  Results never depend on these shapes. */
+ * vertex pass (128/256/512) and of the per-boundary passes, each side
+ * count from which grains get a warp each (9..12), and the resident blocks
+ * per SM of the thread-per-grain grain pass (4, 5, 6, 8), one parameter at a
+ * time, keeps the fastest and restores the state.  chosen (4 ints, may be
+ * NULL) receives them in that order.  Results never depend on these
+ * shapes. */
 sevc_status sevc_autotune(sevc_handle *h, int steps, int *chosen);
 
 /* Per-kernel device time accumulated while profiling is on (CUDA events

@@ -1119,10 +1119,10 @@ sevc_status sevc_autotune(sevc_handle *h, int steps, int *chosen)
         return st;
     };
     LaunchShape &sh = h->p.shape;
-    int *fields[3] = { &sh.tpb_vertex, &sh.tpb_boundary, &sh.wide_sides };
-    const std::vector<int> cands[3] = { { 128, 256, 512 }, { 128, 256, 512 }, { 9, 10, 11, 12 } };
+    int *fields[4] = { &sh.tpb_vertex, &sh.tpb_boundary, &sh.wide_sides, &sh.grain_occ };
+    const std::vector<int> cands[4] = { { 128, 256, 512 }, { 128, 256, 512 }, { 9, 10, 11, 12 }, { 4, 5, 6, 8 } };
     sevc_status st = SEVC_OK;
-    for (int f = 0; f < 3 && !st; f++) {
+    for (int f = 0; f < 4 && !st; f++) {
         int best = *fields[f];
         double best_ms = 1e300;
         for (int v : cands[f]) {
@@ -1142,7 +1142,7 @@ sevc_status sevc_autotune(sevc_handle *h, int steps, int *chosen)
     h->outputs_complete = oc;
     if (st) return st;
     if (!ok) return SEVC_ERR_CUDA;
-    if (chosen) { chosen[0] = sh.tpb_vertex; chosen[1] = sh.tpb_boundary; chosen[2] = sh.wide_sides; }
+    if (chosen) { chosen[0] = sh.tpb_vertex; chosen[1] = sh.tpb_boundary; chosen[2] = sh.wide_sides; chosen[3] = sh.grain_occ; }
     return SEVC_OK;
 }
 

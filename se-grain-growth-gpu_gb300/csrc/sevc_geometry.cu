@@ -163,11 +163,14 @@ __device__ __noinline__ void grain_fd_generic(const DevMesh &m, int g, const int
 
 /* grain pass over the grains of fewer than `wide` sides (11 by default), ordered by
  * side count (warps see one N), most sides first so that the longest
- * blocks start in the first wave.  The pass is FP64-latency bound:
- * capping registers at 128 (4 blocks of 128 per SM) measured 9% faster on
- * the 1M-grain mesh than the compiler's 218-register choice, despite a few
- * spills; an 80-register cap gained nothing more. */
-__global__ void __launch_bounds__(128, 4) k_grain_fd_sorted(DevMesh m, const int *perm, const int *vbucket, int wide)
+ * blocks start in the first wave.  The pass is FP64 bound and waits on
+ * FP64 results: OCC resident blocks of 128 per SM (4: 128 registers, 5:
+ * 96, 6: 80, 8: 64) trades registers (and spills) for warps to hide that
+ * latency; the launch-shape autotuner picks it (6 on the 1M-grain mesh).
+ * Capping registers at 128 measured 9% faster than the compiler's
+ * 218-register choice. */
+template <int OCC>
+__global__ void __launch_bounds__(128, OCC) k_grain_fd_sorted(DevMesh m, const int *perm, const int *vbucket, int wide)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int total = vbucket[VB_START(wide)];
@@ -634,7 +637,11 @@ void launch_grain_fd_wide(const DevMesh &m, const DevScratch &x, const LaunchSha
 }
 void launch_grain_fd_sorted(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_grain_fd_sorted<<<(m.ng + 127) / 128, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
+    int g = (m.ng + 127) / 128;
+    if (sh.grain_occ >= 8) COUNT_LAUNCHES(1), k_grain_fd_sorted<8><<<g, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
+    else if (sh.grain_occ >= 6) COUNT_LAUNCHES(1), k_grain_fd_sorted<6><<<g, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
+    else if (sh.grain_occ == 5) COUNT_LAUNCHES(1), k_grain_fd_sorted<5><<<g, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
+    else COUNT_LAUNCHES(1), k_grain_fd_sorted<4><<<g, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
 }
 
 /* the unsorted per-grain pass, kept for A/B timing */

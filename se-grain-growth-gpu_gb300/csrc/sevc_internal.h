@@ -48,11 +48,13 @@ enum {
 };
 #define CTR_NUCL_AREA_SLOT 8 /* double stored at counters + 8 (two ints) */
 
-/* launch shapes the autotuner may change (results do not depend on them) */
+/* launch shapes the autotuner may change (results do not depend on them);
+ * the defaults are what it picked on the 1M-grain mesh */
 struct LaunchShape {
-    int tpb_vertex = 256;    /* threads per block of the vertex pass */
-    int tpb_boundary = 256;  /* of the per-boundary passes (geometry, t_ext) */
+    int tpb_vertex = 128;    /* threads per block of the vertex pass */
+    int tpb_boundary = 128;  /* of the per-boundary passes (geometry, t_ext) */
     int wide_sides = 11;     /* grains of this many sides or more get a warp each */
+    int grain_occ = 6;       /* resident blocks per SM of the thread-per-grain grain pass (4, 5, 6, 8) */
 };
 
 struct StepParams {

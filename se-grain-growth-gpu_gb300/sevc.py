@@ -420,8 +420,9 @@ class Engine:
         _check(lib().sevc_set_exact_all(self._h, 1 if on else 0))
 
     def autotune(self, steps=5):
-        """Pick launch shapes by timing; returns (tpb_vertex, tpb_boundary, wide_sides)."""
-        out = (C.c_int * 3)()
+        """Pick launch shapes by timing; returns (tpb_vertex, tpb_boundary,
+        wide_sides, grain_occ)."""
+        out = (C.c_int * 4)()
         lib().sevc_autotune.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _check(lib().sevc_autotune(self._h, steps, out))
         return tuple(out)

@@ -126,6 +126,7 @@ def test_autotune_keeps_state_and_results(gpu):
         b.step()
     chosen = a.autotune(steps=3)
     assert chosen[0] in (128, 256, 512) and chosen[1] in (128, 256, 512) and 9 <= chosen[2] <= 12
+    assert chosen[3] in (4, 5, 6, 8)
     assert same_state(a.get_state(), b.get_state()) is None
     events = 0
     for k in range(60):
