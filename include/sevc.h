@@ -133,6 +133,11 @@ int sevc_should_continue(const sevc_handle *h);
  * step and after steps whose outputs are complete (export_due steps, or
  * every step with sevc_set_exact_all); SEVC_ERR_ARG otherwise. */
 sevc_status sevc_export_text(sevc_handle *h, const char *path, double time);
+/* The same text for a mesh held in host arrays (export_data's format,
+ * src/io.h:280-377), on the host only: the lines are formatted by all host
+ * threads in chunks and written in order, so the file is the one a serial
+ * writer produces. */
+sevc_status sevc_write_snapshot(const sevc_mesh_host *mesh, const sevc_options *opt, const char *path, double time);
 /* device_to_host, src/translation.h:184-199 (without freeing anything):
  * copy the mesh into caller-owned arrays sized like sevc_mesh_sizes. */
 sevc_status sevc_get_state(sevc_handle *h, sevc_mesh_host *out);

@@ -21,6 +21,7 @@
 #include <ftw.h>
 #include <map>
 #include <string>
+#include <thread>
 #include <sys/stat.h>
 #include <unistd.h>
 #include <vector>
@@ -1475,8 +1476,22 @@ sevc_status sevc_run_program(const sevc_options *opt_in, int verbose)
     sevc_status st = sevc_create(&opt, &h);
     if (st) return st;
     if (verbose) printf("%d grains loaded.\nData loaded.\n", h->ng);
-    sevc_hmesh hm;
-    if (sevc_hmesh_alloc(&hm, h->nv, h->nb, h->ng)) { sevc_destroy(h); return SEVC_ERR_CAPACITY; }
+    /* Snapshots are written by a host thread while the next steps run: the
+     * state is downloaded into one of two host copies, the previous writer
+     * is joined, and a new one formats and writes the copy.  The validity
+     * check that gates a save (src/main.cu:331-338) runs on the device
+     * before the download, with the same rules as the host check. */
+    sevc_hmesh hm[2];
+    if (sevc_hmesh_alloc(&hm[0], h->nv, h->nb, h->ng)) { sevc_destroy(h); return SEVC_ERR_CAPACITY; }
+    if (sevc_hmesh_alloc(&hm[1], h->nv, h->nb, h->ng)) { sevc_hmesh_free(&hm[0]); sevc_destroy(h); return SEVC_ERR_CAPACITY; }
+    std::thread writer;
+    int wstat = 0;
+    std::string wpath;
+    auto join_writer = [&]() -> sevc_status {
+        if (writer.joinable()) writer.join();
+        if (wstat) { sevc_set_error("write error on %s", wpath.c_str()); return (sevc_status)wstat; }
+        return SEVC_OK;
+    };
     int prog = 0;
     while (sevc_should_continue(h)) {
         if (verbose) printf("n = %d, t = %f\n", h->n, h->t);
@@ -1493,25 +1508,36 @@ sevc_status sevc_run_program(const sevc_options *opt_in, int verbose)
             if (verbose)
                 printf("Saving at n=%d, t=%.16f, n_grains=%d, nucl_area=%.16f\n", inf.n, inf.t, inf.curr_n_grains,
                        inf.nucleated_area);
-            if ((st = sevc_get_state(h, &hm.m))) break;
-            if (sevc_host_check(&hm.m)) {
+            int bad = 0;
+            if ((st = sevc_check_data(h, &bad))) break;
+            if (bad) {
                 if (verbose) printf("Error while saving output file. Exiting...\n");
                 break;
             }
             if (verbose) printf("Valid data. Saving...\n");
+            sevc_hmesh &buf = hm[prog & 1];
+            if ((st = sevc_get_state(h, &buf.m))) break;
+            if ((st = join_writer())) break;
             char path[600];
             snprintf(path, sizeof path, "%s/%06d.txt", opt.output_folder, prog);
-            if ((st = (sevc_status)sevc_host_export(&hm.m, &h->opt, path, inf.t))) break;
+            wpath = path;
+            sevc_options o = h->opt;
+            double t = inf.t;
+            std::string p = path;
+            writer = std::thread([&wstat, &buf, o, p, t]() { wstat = sevc_host_export(&buf.m, &o, p.c_str(), t); });
             prog++;
         }
         if (!inf.keep_going) break;
     }
+    sevc_status ws = join_writer();
+    if (!st) st = ws;
     if (verbose) {
         printf("\nPerformed %d iterations.\n", h->n - 1);
         printf("Number of grains: %d\n", h->curr_n_grains);
         printf("Done.\n");
     }
-    sevc_hmesh_free(&hm);
+    sevc_hmesh_free(&hm[0]);
+    sevc_hmesh_free(&hm[1]);
     sevc_destroy(h);
     return st;
 }

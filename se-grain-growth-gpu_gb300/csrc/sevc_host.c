@@ -496,28 +496,100 @@ int sevc_format_fixed16(double x, char *out)
 /* ---------------------------------------------------------------- */
 /* snapshot text, src/io.h:280-377                                   */
 /* ---------------------------------------------------------------- */
-/* lines are formatted into a buffer with the exact formatter above and
- * written in large blocks */
-typedef struct { FILE *f; char *buf, *p; size_t cap; int err; } outbuf;
+/* lines are formatted with the exact formatter above into per-thread
+ * blocks and written in large writes */
 
-static void ob_flush(outbuf *b)
+/* One line of each section.  A binary64 in %.16f takes at most 327
+ * characters (309 integer digits, sign, point, 16 decimals), an int 11. */
+#define F16_MAX 330
+#define VLINE_MAX (9 * (F16_MAX + 1) + 8 * 12 + 2)
+#define BLINE_MAX (3 * (F16_MAX + 1) + 5 * 12 + 2)
+#define GLINE_MAX (4 * (F16_MAX + 1) + (4 + SEVC_MAX_VRT_PER_GRN) * 12 + 2)
+static char *line_vertex(const sevc_mesh_host *m, int i, char *p)
 {
-    size_t n = (size_t)(b->p - b->buf);
-    if (n && fwrite(b->buf, 1, n, b->f) != n) b->err = 1;
-    b->p = b->buf;
+    const int *s = &m->vb[3 * i];
+    int nbr[3];
+    for (int j = 0; j < 3; j++)
+        nbr[j] = s[j] < 0 ? -1 : (m->bini[s[j]] == i ? m->bend[s[j]] : m->bini[s[j]]);
+    p = put_int(p, i); *p++ = ' ';
+    p = put_int(p, m->ven[i] ? 1 : 0);
+    const double vals[9] = { m->venergy[i], m->px[i], m->py[i], m->vx[i], m->vy[i], m->vel_bnd_x[i],
+                             m->vel_grn_x[i], m->vel_bnd_y[i], m->vel_grn_y[i] };
+    for (int k = 0; k < 9; k++) { *p++ = ' '; p = put_f16(p, vals[k]); }
+    const int ints[6] = { m->vg[3 * i], m->vg[3 * i + 1], m->vg[3 * i + 2], nbr[0], nbr[1], nbr[2] };
+    for (int k = 0; k < 6; k++) { *p++ = ' '; p = put_int(p, ints[k]); }
+    *p++ = '\n';
+    return p;
 }
-static void ob_room(outbuf *b, size_t need)
+static char *line_boundary(const sevc_mesh_host *m, int i, char *p)
 {
-    if ((size_t)(b->p - b->buf) + need > b->cap) ob_flush(b);
+    p = put_int(p, i); *p++ = ' ';
+    p = put_int(p, m->ben[i] ? 1 : 0); *p++ = ' ';
+    p = put_int(p, m->bini[i]); *p++ = ' ';
+    p = put_int(p, m->bend[i]); *p++ = ' ';
+    p = put_f16(p, m->benergy[i]); *p++ = ' ';
+    p = put_f16(p, m->blen[i]); *p++ = ' ';
+    p = put_f16(p, m->btext[i]); *p++ = ' ';
+    p = put_int(p, m->bcand[i] ? 1 : 0);
+    *p++ = '\n';
+    return p;
+}
+static char *line_grain(const sevc_mesh_host *m, int i, char *p)
+{
+    int n = m->gvlen[i];
+    p = put_int(p, i); *p++ = ' ';
+    p = put_int(p, m->gen[i] ? 1 : 0); *p++ = ' ';
+    p = put_int(p, (int)m->gtype[i]); *p++ = ' ';
+    p = put_f16(p, m->gori[i]); *p++ = ' ';
+    p = put_f16(p, m->gse[i]); *p++ = ' ';
+    p = put_f16(p, m->garea[i]); *p++ = ' ';
+    p = put_f16(p, m->gdadt[i]); *p++ = ' ';
+    p = put_int(p, n); *p++ = ' ';
+    const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * i];
+    for (int j = 0; j < SEVC_MAX_VRT_PER_GRN; j++) {
+        if (j < n) { p = put_int(p, L[j]); *p++ = ' '; }
+        else if (j == SEVC_MAX_VRT_PER_GRN - 1) { *p++ = '-'; *p++ = '1'; }
+        else { *p++ = '-'; *p++ = '1'; *p++ = ' '; }
+    }
+    *p++ = '\n';
+    return p;
+}
+
+/* A section's lines, formatted in chunks of SEC_LINES by the OpenMP
+ * threads, a round of chunks at a time, and written in order: the file is
+ * byte for byte the serial one. */
+#define SEC_LINES 512
+static int write_section(FILE *f, const sevc_mesh_host *m, int n, char *(*line)(const sevc_mesh_host *, int, char *),
+                         size_t maxline)
+{
+    int nchunks = (n + SEC_LINES - 1) / SEC_LINES;
+    if (nchunks == 0) return 0;
+    int per_round = 64;
+    size_t chunk_bytes = (size_t)SEC_LINES * maxline;
+    char *pool = (char *)malloc((size_t)per_round * chunk_bytes);
+    size_t lens[64];
+    if (!pool) return -1;
+    int err = 0;
+    for (int c0 = 0; c0 < nchunks && !err; c0 += per_round) {
+        int cn = nchunks - c0 < per_round ? nchunks - c0 : per_round;
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int c = 0; c < cn; c++) {
+            int lo = (c0 + c) * SEC_LINES, hi = lo + SEC_LINES < n ? lo + SEC_LINES : n;
+            char *b = pool + (size_t)c * chunk_bytes, *p = b;
+            for (int i = lo; i < hi; i++) p = line(m, i, p);
+            lens[c] = (size_t)(p - b);
+        }
+        for (int c = 0; c < cn && !err; c++)
+            if (fwrite(pool + (size_t)c * chunk_bytes, 1, lens[c], f) != lens[c]) err = 1;
+    }
+    free(pool);
+    return err;
 }
 
 int sevc_host_export(const sevc_mesh_host *m, const sevc_options *o, const char *path, double time)
 {
     FILE *f = fopen(path, "w");
     if (!f) { sevc_set_error("cannot write %s", path); return SEVC_ERR_IO; }
-    outbuf ob = { f, NULL, NULL, (size_t)1 << 24, 0 };
-    ob.buf = ob.p = (char *)malloc(ob.cap);
-    if (!ob.buf) { fclose(f); sevc_set_error("out of host memory"); return SEVC_ERR_CAPACITY; }
     int cv = 0, cb = 0, cg = 0;
     for (int i = 0; i < m->nv; i++) cv += m->ven[i] != 0;
     for (int i = 0; i < m->nb; i++) cb += m->ben[i] != 0;
@@ -530,68 +602,20 @@ int sevc_host_export(const sevc_mesh_host *m, const sevc_options *o, const char 
             o->nucleation_scaling, SEVC_MAX_VRT_PER_GRN);
     fprintf(f, "VERTICES %d\nBOUNDARIES %d\nGRAINS %d\nCURR VERTICES %d\nCURR BOUNDARIES %d\nCURR GRAINS %d\n",
             m->nv, m->nb, m->ng, cv, cb, cg);
-    fflush(f);
-#define SP (*ob.p++ = ' ')
-    const char *vh = "#VERTEX ENABLED ENERGY X Y VX VY VXbnd VXgrn VYbnd VYgrn VG1 G2 G3 N1 N2 N3\n";
-    ob_room(&ob, strlen(vh));
-    memcpy(ob.p, vh, strlen(vh)); ob.p += strlen(vh);
-    for (int i = 0; i < m->nv; i++) {
-        const int *s = &m->vb[3 * i];
-        int nbr[3];
-        for (int j = 0; j < 3; j++)
-            nbr[j] = s[j] < 0 ? -1 : (m->bini[s[j]] == i ? m->bend[s[j]] : m->bini[s[j]]);
-        ob_room(&ob, 1024);
-        ob.p = put_int(ob.p, i); SP;
-        ob.p = put_int(ob.p, m->ven[i] ? 1 : 0);
-        const double vals[9] = { m->venergy[i], m->px[i], m->py[i], m->vx[i], m->vy[i], m->vel_bnd_x[i],
-                                 m->vel_grn_x[i], m->vel_bnd_y[i], m->vel_grn_y[i] };
-        for (int k = 0; k < 9; k++) { SP; ob.p = put_f16(ob.p, vals[k]); }
-        const int ints[6] = { m->vg[3 * i], m->vg[3 * i + 1], m->vg[3 * i + 2], nbr[0], nbr[1], nbr[2] };
-        for (int k = 0; k < 6; k++) { SP; ob.p = put_int(ob.p, ints[k]); }
-        *ob.p++ = '\n';
-    }
-    const char *bh = "#BOUNDARY ENABLED INI END ENERGY ARCLEN EXTTIME CANDIDATE\n";
-    ob_room(&ob, strlen(bh));
-    memcpy(ob.p, bh, strlen(bh)); ob.p += strlen(bh);
-    for (int i = 0; i < m->nb; i++) {
-        ob_room(&ob, 512);
-        ob.p = put_int(ob.p, i); SP;
-        ob.p = put_int(ob.p, m->ben[i] ? 1 : 0); SP;
-        ob.p = put_int(ob.p, m->bini[i]); SP;
-        ob.p = put_int(ob.p, m->bend[i]); SP;
-        ob.p = put_f16(ob.p, m->benergy[i]); SP;
-        ob.p = put_f16(ob.p, m->blen[i]); SP;
-        ob.p = put_f16(ob.p, m->btext[i]); SP;
-        ob.p = put_int(ob.p, m->bcand[i] ? 1 : 0);
-        *ob.p++ = '\n';
-    }
-    const char *gh = "#GRAIN ID ENABLED NUCLEATED ORIENT SE AREA dAdt VLEN VERTICES\n";
-    ob_room(&ob, strlen(gh));
-    memcpy(ob.p, gh, strlen(gh)); ob.p += strlen(gh);
-    for (int i = 0; i < m->ng; i++) {
-        int n = m->gvlen[i];
-        ob_room(&ob, 512 + 12 * SEVC_MAX_VRT_PER_GRN);
-        ob.p = put_int(ob.p, i); SP;
-        ob.p = put_int(ob.p, m->gen[i] ? 1 : 0); SP;
-        ob.p = put_int(ob.p, (int)m->gtype[i]); SP;
-        ob.p = put_f16(ob.p, m->gori[i]); SP;
-        ob.p = put_f16(ob.p, m->gse[i]); SP;
-        ob.p = put_f16(ob.p, m->garea[i]); SP;
-        ob.p = put_f16(ob.p, m->gdadt[i]); SP;
-        ob.p = put_int(ob.p, n); SP;
-        const int *L = &m->glist[(size_t)SEVC_MAX_VRT_PER_GRN * i];
-        for (int j = 0; j < SEVC_MAX_VRT_PER_GRN; j++) {
-            if (j < n) { ob.p = put_int(ob.p, L[j]); SP; }
-            else if (j == SEVC_MAX_VRT_PER_GRN - 1) { *ob.p++ = '-'; *ob.p++ = '1'; }
-            else { *ob.p++ = '-'; *ob.p++ = '1'; SP; }
-        }
-        *ob.p++ = '\n';
-    }
-#undef SP
-    ob_flush(&ob);
-    free(ob.buf);
-    if (fclose(f) || ob.err) { sevc_set_error("write error on %s", path); return SEVC_ERR_IO; }
+    int err = fputs("#VERTEX ENABLED ENERGY X Y VX VY VXbnd VXgrn VYbnd VYgrn VG1 G2 G3 N1 N2 N3\n", f) < 0;
+    if (!err) err = write_section(f, m, m->nv, line_vertex, VLINE_MAX) != 0;
+    if (!err) err = fputs("#BOUNDARY ENABLED INI END ENERGY ARCLEN EXTTIME CANDIDATE\n", f) < 0;
+    if (!err) err = write_section(f, m, m->nb, line_boundary, BLINE_MAX) != 0;
+    if (!err) err = fputs("#GRAIN ID ENABLED NUCLEATED ORIENT SE AREA dAdt VLEN VERTICES\n", f) < 0;
+    if (!err) err = write_section(f, m, m->ng, line_grain, GLINE_MAX) != 0;
+    if (fclose(f) || err) { sevc_set_error("write error on %s", path); return SEVC_ERR_IO; }
     return SEVC_OK;
+}
+
+sevc_status sevc_write_snapshot(const sevc_mesh_host *mesh, const sevc_options *opt, const char *path, double time)
+{
+    if (!mesh || !opt || !path) return SEVC_ERR_ARG;
+    return (sevc_status)sevc_host_export(mesh, opt, path, time);
 }
 
 /* ---------------------------------------------------------------- */

@@ -26,7 +26,7 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
            "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
            "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs", "sevc_measure_fp64_rate",
-           "sevc_autotune", "sevc_selftest_arith"]
+           "sevc_autotune", "sevc_selftest_arith", "sevc_write_snapshot"]
 
 
 class SevcError(RuntimeError):
@@ -178,6 +178,16 @@ def check_mesh_host(arrs):
     L = lib()
     L.sevc_host_check.argtypes = [C.POINTER(MeshHost)]
     return int(L.sevc_host_check(C.byref(mh)))
+
+
+def write_snapshot(arrs, opt, path, time):
+    """The snapshot text (src/io.h:280-377) of a mesh held in host arrays
+    (keys of get_state / load_mesh_host); host only."""
+    arrs = {f: np.ascontiguousarray(arrs[f], dt) for f, _, dt in _MESH_FIELDS}
+    mh = mesh_host_of(arrs)
+    L = lib()
+    L.sevc_write_snapshot.argtypes = [C.POINTER(MeshHost), C.POINTER(Options), C.c_char_p, C.c_double]
+    _check(L.sevc_write_snapshot(C.byref(mh), C.byref(opt), path.encode(), float(time)))
 
 
 def measure_fp64_rate():

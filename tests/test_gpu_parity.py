@@ -265,3 +265,35 @@ def test_anisotropic_free_run_agrees_statistically(gpu, oracle_mod, tmp_path):
     ks = stats.ks_2samp(ag / ag.mean(), ao / ao.mean())
     assert ks.statistic < 0.1, ks
     assert abs(ag.std() / ag.mean() - ao.std() / ao.mean()) < 0.05 * (ao.std() / ao.mean())
+
+
+def test_program_loop_snapshots_match_reference(gpu, tmp_path):
+    """The drop-in program loop (sevc_run_program: snapshots written by a
+    host thread while the next steps run) writes the files the reference
+    writes: every snapshot before the first nucleation attempt has the
+    digest of the reference's own, and the files are the ones the step-by-
+    step API exports."""
+    name = "plain_unit"
+    _, _, keys, _, mg = configs.CONFIGS[name]
+    out = os.path.join(str(tmp_path), "prog")
+    ini = configs.write_ini(os.path.join(str(tmp_path), name + ".ini"), name, out)
+    opt = gpu.load_ini(ini)
+    opt.min_grains = mg
+    rc = gpu.lib().sevc_run_program(gpu.C.byref(opt), 0)
+    assert rc == 0, gpu.lib().sevc_last_error()
+    files = sorted(f for f in os.listdir(os.path.join(out, "DATA")) if f.endswith(".txt"))
+    g = GOLDEN[name]
+    assert len(files) >= 5
+    for prog, f in enumerate(files[:len(g["snapshots"])]):
+        full, topo = snapshot.digests(os.path.join(out, "DATA", f))
+        assert topo == g["snapshots"][prog][1], (f, prog)
+    eng = gpu.Engine.from_files(opt)
+    prog = 0
+    while prog < 3:
+        info = eng.step()
+        if info.export_due:
+            path = os.path.join(str(tmp_path), "api_%06d.txt" % prog)
+            eng.export(path, info.t)
+            assert open(path, "rb").read() == open(os.path.join(out, "DATA", files[prog]), "rb").read()
+            prog += 1
+    eng.close()

@@ -191,3 +191,18 @@ def test_host_check_counts_planted_faults(engine_mod, tmp_path):
     for kind in ["boundary_off", "dup_boundary_slot", "dup_grain_slot", "self_loop", "short_list", "grain_off",
                  "vertex_off", "foreign_grain"]:
         assert engine_mod.check_mesh_host(plant(st, kind, rng)) > 0, kind
+
+
+@pytest.mark.parametrize("name", ["plain_unit", "perstep_nucl"])
+def test_snapshot_writer_matches_oracle_export(engine_mod, oracle_mod, name, tmp_path):
+    """The library's snapshot writer (chunks formatted by all host threads,
+    written in order) gives the oracle's printf export byte for byte, here
+    for the freshly loaded mesh (no GPU needed)."""
+    ini = configs.write_ini(str(tmp_path / "r.ini"), name, str(tmp_path / "out"))
+    opt = engine_mod.load_ini(ini)
+    mine = engine_mod.load_mesh_host(opt)
+    a, b = str(tmp_path / "lib.txt"), str(tmp_path / "orc.txt")
+    engine_mod.write_snapshot(mine, opt, a, 0.0)
+    o = oracle_mod.Oracle.from_files(oracle_mod.parse_ini(ini))
+    o.export(b, 0.0)
+    assert open(a, "rb").read() == open(b, "rb").read()
