@@ -633,7 +633,10 @@ void launch_grain_sort(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 }
 void launch_grain_fd_wide(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_grain_fd_wide<<<2 * 152, 32 * WIDE_WARPS, 0, s>>>(m, x.perm, x.vbucket, x.n_perm, sh.wide_sides);
+    /* one warp per grain, grid-stride: enough warps that each takes only a
+     * few of the widest grains (their areas are chains of dependent FP64
+     * operations, so warps in flight hide the latency) */
+    COUNT_LAUNCHES(1), k_grain_fd_wide<<<8 * 152, 32 * WIDE_WARPS, 0, s>>>(m, x.perm, x.vbucket, x.n_perm, sh.wide_sides);
 }
 void launch_grain_fd_sorted(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)
 {
