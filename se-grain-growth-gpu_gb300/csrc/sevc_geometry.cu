@@ -64,10 +64,60 @@ __device__ __forceinline__ void put_contrib(const DevMesh &m, int g, int v, doub
 /* Area of the polygon with vertex p moved along component C (0 = x,
  * 1 = y).  R/A0/DD are the moved component's raw positions, unwrapped
  * coordinates and wrapped deltas, Ro/B0 the other component's. */
+__device__ __noinline__ double area_stream_slow(const int *__restrict__ L, int n, const double2 *__restrict__ pos,
+                                                int ps, double2 pp, double D)
+{
+    return area_stream(L, n, pos, ps, pp, D);
+}
+
+/* shoelace term k of the moved component C: P = its unwrapped
+ * coordinates k and k+1, B = the other component's */
+template <int C>
+__device__ __forceinline__ double moved_term(double pk, double bk, double pk1, double bk1)
+{
+    return C == 0 ? pk * bk1 - bk * pk1 : bk * pk1 - pk * bk1;
+}
+
+/* Moving vertex p (0 < p < N-1) changes the unwrapped chain at p, then
+ * at p+1 by the wrapped deltas into and out of the moved point.  When the
+ * moved chain arrives at p+1 on the unmoved value (bit for bit: the two
+ * deltas cancel exactly, which they do unless a wrap or a tiny coordinate
+ * makes a difference inexact), every later coordinate is the same
+ * operation on the same values as in the unmoved pass, so terms p+1.. are
+ * the unmoved terms T[k] and only the running sum is redone.  Otherwise
+ * the polygon is recomputed from memory. */
+template <int N, int C>
+__device__ __forceinline__ double moved_area_mid(const DevMesh &m, const int *__restrict__ L, int p, double moved,
+                                                 double other, const double (&R)[N], const double (&A0)[N],
+                                                 const double (&B0)[N], const double (&S)[N], const double (&T)[N])
+{
+    const double D = m.D;
+    double pp = p == 1 ? zero_plus(wrapd(moved, R[0], D)) : A0[p - 1] + wrapd(moved, R[p - 1], D);
+    double pn = pp + wrapd(R[p + 1], moved, D);
+    if (dbits(pn) != dbits(A0[p + 1])) {
+        double2 q = C == 0 ? make_double2(moved, other) : make_double2(other, moved);
+        return area_stream_slow(L, N, m.pos, p, q, D);
+    }
+    /* terms p-1 and p (the products that involve only unmoved
+     * coordinates are the unmoved pass's; the compiler shares them) */
+    double a = 0;
+    if (p >= 2) {
+        double t = moved_term<C>(A0[p - 1], B0[p - 1], pp, B0[p]);
+        a = p == 2 ? zero_plus(t) : S[p - 2] + t;
+    }
+    double t = moved_term<C>(pp, B0[p], A0[p + 1], B0[p + 1]);
+    a = p == 1 ? zero_plus(t) : a + t;
+#pragma unroll
+    for (int k = 2; k < N - 1; k++)
+        if (k > p) a = a + T[k];
+    a = C == 0 ? add_closing_term(a, A0[N - 1], B0[N - 1]) : add_closing_term(a, B0[N - 1], A0[N - 1]);
+    return dscale_down<1>(a);
+}
+
 template <int N, int C>
 __device__ __forceinline__ double moved_area(const DevMesh &m, const int *__restrict__ L, int p, const double (&R)[N],
                                              const double (&Ro)[N], const double (&A0)[N], const double (&B0)[N],
-                                             const double (&DD)[N], const double (&S)[N])
+                                             const double (&DD)[N], const double (&S)[N], const double (&T)[N])
 {
     const double D = m.D;
     double moved = dmod(R[p] + SEVC_GRAD_EPS_D, D);
@@ -76,6 +126,7 @@ __device__ __forceinline__ double moved_area(const DevMesh &m, const int *__rest
         double2 pp = C == 0 ? make_double2(moved, other) : make_double2(other, moved);
         return area_stream(L, N, m.pos, p, pp, D);
     }
+    if (p > 0 && p < N - 1) return moved_area_mid<N, C>(m, L, p, moved, other, R, A0, B0, S, T);
     double Pm[N];
     Pm[0] = 0;
 #pragma unroll
@@ -102,7 +153,7 @@ __device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const in
 {
     const double D = m.D;
     int V[N];
-    double RX[N], RY[N], AX[N], AY[N], DX[N], DY[N], S[N];
+    double RX[N], RY[N], AX[N], AY[N], DX[N], DY[N], S[N], T[N];
 #pragma unroll
     for (int k = 0; k < N; k++) {
         V[k] = L[k];
@@ -120,12 +171,15 @@ __device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const in
     }
     double acc = 0;                    /* terms 0 and N-1 involve the origin */
     S[0] = 0;
+    T[0] = 0;
 #pragma unroll
     for (int k = 1; k < N - 1; k++) {
         double term = AX[k] * AY[k + 1] - AY[k] * AX[k + 1];
+        T[k] = term;
         acc = k == 1 ? zero_plus(term) : acc + term;
         S[k] = acc;
     }
+    T[N - 1] = 0;
     acc = add_closing_term(acc, AX[N - 1], AY[N - 1]);
     S[N - 1] = acc;
     double A = dscale_down<1>(acc);
@@ -135,8 +189,8 @@ __device__ __forceinline__ void grain_fd_fixed(const DevMesh &m, int g, const in
     double absA = dabs(A);
 #pragma unroll
     for (int p = 0; p < N; p++) {
-        double ax = moved_area<N, 0>(m, L, p, RX, RY, AX, AY, DX, S);
-        double ay = moved_area<N, 1>(m, L, p, RY, RX, AY, AX, DY, S);
+        double ax = moved_area<N, 0>(m, L, p, RX, RY, AX, AY, DX, S, T);
+        double ay = moved_area<N, 1>(m, L, p, RY, RX, AY, AX, DY, S, T);
         put_contrib(m, g, V[p], se, absA, ax, ay);
     }
 }
