@@ -591,25 +591,34 @@ __global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int
 /* label_3sided_grains (:994-1004) for one 3-sided grain */
 __device__ uint8_t label3_cand(const DevMesh &m, int g, double dt)
 {
-    uint8_t cand = 0;
+    /* The reference breaks out of a vertex's boundary loop once a flip
+     * candidate inside the grain is found; that sets the result to 1 for
+     * good, so testing every boundary gives the same answer and lets all
+     * nine records load at once. */
     const int *L = m.glist + (size_t)SEVC_MAXV * g;
     int l0 = L[0], l1 = L[1], l2 = L[2];
+    int4 s[3] = { m.vb[l0], m.vb[l1], m.vb[l2] };
+    int bs[9];
+    int2 e[9];
+#pragma unroll
+    for (int j = 0; j < 9; j++) bs[j] = slot3(s[j / 3], j % 3);
+#pragma unroll
+    for (int j = 0; j < 9; j++) e[j] = m.bv[bs[j]];
+    bool cand = false;
     int ans = 0;
-    for (int i = 0; i < 3; i++) {
-        int4 s = m.vb[L[i]];
-        for (int k = 0; k < 3; k++) {
-            int b = slot3(s, k);
-            int2 e = m.bv[b];
-            bool ii = e.x == l0 || e.x == l1 || e.x == l2;
-            bool ee = e.y == l0 || e.y == l1 || e.y == l2;
-            if (ii && ee && m.bcand[b] && m.ben[b]) { cand = 1; break; }
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        bool ii = e[j].x == l0 || e[j].x == l1 || e[j].x == l2;
+        bool ee = e[j].y == l0 || e[j].y == l1 || e[j].y == l2;
+        if (ii && ee) {
+            int b = bs[j];
+            uint8_t en = m.ben[b], ca = m.bcand[b];
             double t = m.btext[b];
-            if (ii && ee && (t >= 0 && t <= dt) && m.ben[b]) ans++;
+            cand |= ca && en;
+            ans += (t >= 0 && t <= dt) && en;
         }
     }
-    ans /= 2;
-    if (ans == 3) cand = 1;
-    return cand;
+    return cand || ans / 2 == 3;
 }
 /* clear_grains_state + label_3sided_grains for enabled grains */
 __global__ void k_label_3sided(DevMesh m, double dt)
@@ -852,42 +861,91 @@ __device__ void prefetch_flip(const DevMesh &m, int bnd, int lane)
     }
 }
 
+/* The four grains a flip queues for the fix-up pass (mark_fix) have their
+ * dA/dt settled first, each by its own lane, instead of one after another
+ * inside the flip.  finalize_grain reads only the grain's list and its
+ * vertices' positions and velocities at the start of the step, which
+ * nothing in a flip changes before those calls, so the values are the
+ * ones the flip would compute; the flip then finds each grain settled.
+ * The grains are found the way flip_dev finds them (lanes 0-7 scan the
+ * lists); on any inconsistency nothing is settled and the flip reports
+ * it. */
+__device__ void flip_settle_grains(const DevMesh &m, int bnd, int lane)
+{
+    int2 eb = m.bv[bnd];
+    int A = eb.x, B = eb.y;
+    if (A < 0 || A >= m.nv || B < 0 || B >= m.nv) return;
+    int4 ga = m.vg[A], gb = m.vg[B], sa = m.vb[A], sb = m.vb[B];
+    int gic[2], gnic[2];
+    if (gintersect(ga, gb, gic) < 2) return;
+    gsymdiff(ga, gb, gnic);
+    int AC = -1, BE = -1;
+    for (int k = 0; k < 3; k++) if (slot3(sa, k) == bnd) { AC = slot3(sa, (k + 1) % 3); break; }
+    for (int k = 0; k < 3; k++) if (slot3(sb, k) == bnd) { BE = slot3(sb, (k + 1) % 3); break; }
+    if (AC < 0 || BE < 0 || gnic[0] < 0 || gnic[1] < 0) return;
+    bool hit = false;
+    if (lane < 4) hit = glist_consecutive(m, gic[lane & 1], lane < 2 ? A : B, lane < 2 ? B : A) == 1;
+    else if (lane < 8) hit = glist_find(m, gnic[lane & 1], lane < 6 ? A : B) >= 0;
+    unsigned h = __ballot_sync(0xffffffffu, hit);
+    int g2 = (h & 1) ? 0 : (h & 2) ? 1 : 2, g4 = (h & 4) ? 0 : (h & 8) ? 1 : 2;
+    int g3 = (h & 16) ? 0 : (h & 32) ? 1 : 2, g1 = (h & 64) ? 0 : (h & 128) ? 1 : 2;
+    if (g1 == 2 || g2 == 2 || g3 == 2 || g4 == 2) return;
+    int G[4] = { gic[g2], gic[g4], gnic[g3], gnic[g1] };
+    if (lane < 4) {
+        int g = G[lane];
+        bool dup = false;
+        for (int k = 0; k < lane; k++) dup |= G[k] == g;
+        if (!dup) finalize_grain(m, g);
+    }
+}
+
 /* apply_flippings (:1016-1026); flips that share no vertex commute, the
  * rest are applied in ascending boundary order */
-/* One warp per instance.  A flip changes no boundary's enabled or
+/* One block per instance.  A flip changes no boundary's enabled or
  * candidate flag, so which listed boundaries flip is known up front: the
- * warp tests 32 at a time and lane 0 applies the hits in list order. */
-__global__ void k_flips(DevMesh m, double eps, const int *list, const int *n)
+ * block tests FLIP_TPB entries at a time (the list is long and hits are
+ * few, so the scan's dependent loads are the cost) and warp 0 applies the
+ * hits in list order, its lanes prefetching each flip's records. */
+constexpr int FLIP_TPB = 512;
+__global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const int *list, const int *n)
 {
-    int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (inst >= m.ninst) return;
+    __shared__ unsigned hitmask[FLIP_TPB / 32];
+    int inst = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int lo = 0, hi = *n;
     if (m.ninst > 1) {
         lo = lower_bound_i(list, hi, m.boff[inst]);
         hi = lower_bound_i(list, hi, m.boff[inst + 1]);
     }
-    for (int base = lo; base < hi; base += 32) {
-        int i = base + lane;
+    for (int base = lo; base < hi; base += FLIP_TPB) {
+        int i = base + (int)threadIdx.x;
         bool f = false;
         if (i < hi) {
             int b = list[i];
             uint8_t en = m.ben[b], ca = m.bcand[b];   /* both loads in flight together */
             f = en && ca;
         }
-        unsigned hits = __ballot_sync(0xffffffffu, f);
-        while (hits) {
-            int j = __ffs(hits) - 1;
-            hits &= hits - 1;
-            int b = list[base + j];
-            prefetch_flip(m, b, lane);
-            __syncwarp();
-            if (lane == 0) {
-                flip_dev(m, b, eps);
-                m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
+        unsigned w = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) hitmask[warp] = w;
+        if (!__syncthreads_or(f)) continue;           /* the barrier also publishes hitmask */
+        if (warp == 0) {
+            for (int k = 0; k < FLIP_TPB / 32; k++) {
+                unsigned hits = hitmask[k];
+                while (hits) {
+                    int j = __ffs(hits) - 1;
+                    hits &= hits - 1;
+                    int b = list[base + 32 * k + j];
+                    prefetch_flip(m, b, lane);
+                    flip_settle_grains(m, b, lane);
+                    __syncwarp();
+                    if (lane == 0) {
+                        flip_dev(m, b, eps);
+                        m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
+                    }
+                    __syncwarp();
+                }
             }
-            __syncwarp();
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -1087,7 +1145,7 @@ void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncan
                   cudaStream_t s)
 {
     (void)x;
-    COUNT_LAUNCHES(1), k_flips<<<m.ninst, 32, 0, s>>>(m, eps, cand, ncand);
+    COUNT_LAUNCHES(1), k_flips<<<m.ninst, FLIP_TPB, 0, s>>>(m, eps, cand, ncand);
 }
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)
