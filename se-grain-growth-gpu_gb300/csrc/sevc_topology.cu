@@ -782,14 +782,14 @@ __device__ void flip_dev(const DevMesh &m, int bnd, double eps)
     int2 e = m.bv[AC]; if (e.x == A) e.x = B; else e.y = B; m.bv[AC] = e;
     e = m.bv[BE]; if (e.x == B) e.x = A; else e.y = A; m.bv[BE] = e;
     int g1, g2, g3, g4;
-    for (g2 = 0; g2 < 2; g2++)
-        if (glist_consecutive(m, gic[g2], A, B) == 1) { set_mod(m, A, 0, FIX_REMOVE, gic[g2], A, -2); mark_fix(m, gic[g2]); break; }
-    for (g4 = 0; g4 < 2; g4++)
-        if (glist_consecutive(m, gic[g4], B, A) == 1) { set_mod(m, B, 0, FIX_REMOVE, gic[g4], B, -2); mark_fix(m, gic[g4]); break; }
-    for (g3 = 0; g3 < 2; g3++)
-        if (glist_find(m, gnic[g3], A) >= 0) { set_mod(m, A, 1, FIX_ADD, gnic[g3], B, A); mark_fix(m, gnic[g3]); break; }
-    for (g1 = 0; g1 < 2; g1++)
-        if (glist_find(m, gnic[g1], B) >= 0) { set_mod(m, B, 1, FIX_ADD, gnic[g1], A, B); mark_fix(m, gnic[g1]); break; }
+    for (g2 = 0; g2 < 2; g2++) if (glist_consecutive(m, gic[g2], A, B) == 1) break;
+    for (g4 = 0; g4 < 2; g4++) if (glist_consecutive(m, gic[g4], B, A) == 1) break;
+    for (g3 = 0; g3 < 2; g3++) if (glist_find(m, gnic[g3], A) >= 0) break;
+    for (g1 = 0; g1 < 2; g1++) if (glist_find(m, gnic[g1], B) >= 0) break;
+    if (g2 < 2) { set_mod(m, A, 0, FIX_REMOVE, gic[g2], A, -2); mark_fix(m, gic[g2]); }
+    if (g4 < 2) { set_mod(m, B, 0, FIX_REMOVE, gic[g4], B, -2); mark_fix(m, gic[g4]); }
+    if (g3 < 2) { set_mod(m, A, 1, FIX_ADD, gnic[g3], B, A); mark_fix(m, gnic[g3]); }
+    if (g1 < 2) { set_mod(m, B, 1, FIX_ADD, gnic[g1], A, B); mark_fix(m, gnic[g1]); }
     if (g1 == 2 || g2 == 2 || g3 == 2 || g4 == 2) { raise_err(m, ERRB_TOPOLOGY); return; }
     int4 ga = m.vg[A], gb = m.vg[B];
     for (int k = 0; k < 3; k++) {
@@ -861,42 +861,157 @@ __device__ void prefetch_flip(const DevMesh &m, int bnd, int lane)
     }
 }
 
-/* The four grains a flip queues for the fix-up pass (mark_fix) have their
- * dA/dt settled first, each by its own lane, instead of one after another
- * inside the flip.  finalize_grain reads only the grain's list and its
- * vertices' positions and velocities at the start of the step, which
- * nothing in a flip changes before those calls, so the values are the
- * ones the flip would compute; the flip then finds each grain settled.
- * The grains are found the way flip_dev finds them (lanes 0-7 scan the
- * lists); on any inconsistency nothing is settled and the flip reports
- * it. */
-__device__ void flip_settle_grains(const DevMesh &m, int bnd, int lane)
+/* What flip_dev derives before it writes anything: the two ends, their
+ * other boundaries AC and BE (the successors of bnd in their slot
+ * orders, at slots i and j), the grains on both sides (gic) and at the
+ * ends (gnic), the ends' slot and grain records, and which of those grains
+ * get which list edit (g1..g4, as flip_dev names them). */
+struct FlipPlan {
+    int A, B, AC, BE, i, j, g1, g2, g3, g4;
+    int gic[2], gnic[2];
+    int4 sa, sb, ga, gb;
+};
+
+/* Every lane of the warp derives the flip's plan; lanes 0-7 scan the four
+ * grain lists at once (a flip edits no list, so the answers are the ones
+ * flip_dev's own scans give).  The four grains the flip queues for the
+ * fix-up pass (mark_fix) then have their dA/dt settled, each by its own
+ * lane: finalize_grain reads only the grain's list and its vertices'
+ * positions and velocities at the start of the step, which nothing in a
+ * flip changes before those calls, so the values are the ones the flip
+ * would compute.  Returns false (nothing settled) on any inconsistency;
+ * the flip then runs its own checks and reports it. */
+__device__ bool flip_plan(const DevMesh &m, int bnd, int lane, FlipPlan &P)
 {
     int2 eb = m.bv[bnd];
     int A = eb.x, B = eb.y;
-    if (A < 0 || A >= m.nv || B < 0 || B >= m.nv) return;
-    int4 ga = m.vg[A], gb = m.vg[B], sa = m.vb[A], sb = m.vb[B];
-    int gic[2], gnic[2];
-    if (gintersect(ga, gb, gic) < 2) return;
-    gsymdiff(ga, gb, gnic);
-    int AC = -1, BE = -1;
-    for (int k = 0; k < 3; k++) if (slot3(sa, k) == bnd) { AC = slot3(sa, (k + 1) % 3); break; }
-    for (int k = 0; k < 3; k++) if (slot3(sb, k) == bnd) { BE = slot3(sb, (k + 1) % 3); break; }
-    if (AC < 0 || BE < 0 || gnic[0] < 0 || gnic[1] < 0) return;
+    if (A < 0 || A >= m.nv || B < 0 || B >= m.nv || A == B) return false;
+    P.A = A; P.B = B;
+    P.ga = m.vg[A]; P.gb = m.vg[B]; P.sa = m.vb[A]; P.sb = m.vb[B];
+    if (gintersect(P.ga, P.gb, P.gic) < 2) return false;
+    gsymdiff(P.ga, P.gb, P.gnic);
+    P.i = P.j = P.AC = P.BE = -1;
+    for (int k = 0; k < 3; k++) if (slot3(P.sa, k) == bnd) { P.i = (k + 1) % 3; P.AC = slot3(P.sa, P.i); break; }
+    for (int k = 0; k < 3; k++) if (slot3(P.sb, k) == bnd) { P.j = (k + 1) % 3; P.BE = slot3(P.sb, P.j); break; }
+    if (P.AC < 0 || P.BE < 0 || P.gnic[0] < 0 || P.gnic[1] < 0) return false;
     bool hit = false;
-    if (lane < 4) hit = glist_consecutive(m, gic[lane & 1], lane < 2 ? A : B, lane < 2 ? B : A) == 1;
-    else if (lane < 8) hit = glist_find(m, gnic[lane & 1], lane < 6 ? A : B) >= 0;
+    if (lane < 4) hit = glist_consecutive(m, P.gic[lane & 1], lane < 2 ? A : B, lane < 2 ? B : A) == 1;
+    else if (lane < 8) hit = glist_find(m, P.gnic[lane & 1], lane < 6 ? A : B) >= 0;
     unsigned h = __ballot_sync(0xffffffffu, hit);
-    int g2 = (h & 1) ? 0 : (h & 2) ? 1 : 2, g4 = (h & 4) ? 0 : (h & 8) ? 1 : 2;
-    int g3 = (h & 16) ? 0 : (h & 32) ? 1 : 2, g1 = (h & 64) ? 0 : (h & 128) ? 1 : 2;
-    if (g1 == 2 || g2 == 2 || g3 == 2 || g4 == 2) return;
-    int G[4] = { gic[g2], gic[g4], gnic[g3], gnic[g1] };
+    P.g2 = (h & 1) ? 0 : (h & 2) ? 1 : 2;
+    P.g4 = (h & 4) ? 0 : (h & 8) ? 1 : 2;
+    P.g3 = (h & 16) ? 0 : (h & 32) ? 1 : 2;
+    P.g1 = (h & 64) ? 0 : (h & 128) ? 1 : 2;
+    if (P.g1 == 2 || P.g2 == 2 || P.g3 == 2 || P.g4 == 2) return false;
+    int G[4] = { P.gic[P.g2], P.gic[P.g4], P.gnic[P.g3], P.gnic[P.g1] };
     if (lane < 4) {
         int g = G[lane];
         bool dup = false;
         for (int k = 0; k < lane; k++) dup |= G[k] == g;
         if (!dup) finalize_grain(m, g);
     }
+    return true;
+}
+
+/* flip_dev from a plan, for the usual case AC != BE: the same writes with
+ * the same values, but every record the flip reads is loaded up front in
+ * one round trip instead of behind the writes that precede it, and the
+ * work-list appends of the mod slots and of the fix-up grains take one
+ * atomic each (the appended entries and their order are the ones the
+ * one-at-a-time appends give). */
+__device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPlan &P)
+{
+    const int A = P.A, B = P.B, AC = P.AC, BE = P.BE;
+    const int G[4] = { P.gic[P.g2], P.gic[P.g4], P.gnic[P.g3], P.gnic[P.g1] };
+    unsigned st = *m.stamp;
+    unsigned sAC = m.bstamp[AC], sBE = m.bstamp[BE], stA = m.vstamp[A], stB = m.vstamp[B];
+    int2 eAC = m.bv[AC], eBE = m.bv[BE];
+    int4 mA0 = m.vmod[4 * (size_t)A], mB0 = m.vmod[4 * (size_t)B];
+    uint8_t mkA = m.vmodmark[A], mkB = m.vmodmark[B];
+    uint8_t fx[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) fx[k] = m.gfix[G[k]];
+    double2 pa = m.pos[A], pb = m.pos[B], va = m.vel[A], vb = m.vel[B];
+    log_event(m, EV_FLIP, A, B, -1, pa, pb, pb);
+    /* boundary slots, then vertex_invert_boundary_order */
+    int4 sa = P.sa, sb = P.sb;
+    set_slot3(sa, P.i, BE);
+    set_slot3(sb, P.j, AC);
+    { int t = sa.y; sa.y = sa.x; sa.x = t; }
+    { int t = sb.y; sb.y = sb.x; sb.x = t; }
+    m.vb[A] = sa;
+    m.vb[B] = sb;
+    if (sAC != st) { m.bv0[AC] = eAC; m.bstamp[AC] = st; }      /* save_ends */
+    if (sBE != st) { m.bv0[BE] = eBE; m.bstamp[BE] = st; }
+    if (eAC.x == A) eAC.x = B; else eAC.y = B;
+    if (eBE.x == B) eBE.x = A; else eBE.y = A;
+    m.bv[AC] = eAC;
+    m.bv[BE] = eBE;
+    /* set_mod(A, 0, REMOVE), (B, 0, REMOVE), (A, 1, ADD), (B, 1, ADD) */
+    mA0.x = G[0]; mA0.y = A; mA0.w = FIX_REMOVE;
+    mB0.x = G[1]; mB0.y = B; mB0.w = FIX_REMOVE;
+    m.vmod[4 * (size_t)A] = mA0;
+    m.vmod[4 * (size_t)B] = mB0;
+    m.vmod[4 * (size_t)A + 1] = make_int4(G[2], B, A, FIX_ADD);
+    m.vmod[4 * (size_t)B + 1] = make_int4(G[3], A, B, FIX_ADD);
+    int nm = (mkA ? 0 : 1) + (mkB ? 0 : 1);
+    if (nm) {
+        int i0 = atomicAdd(m.nmod, nm);
+        if (!mkA) {
+            m.vmodmark[A] = 1;
+            if (i0 < m.nv) m.modlist[i0] = A; else raise_err(m, ERRB_WORKLIST);
+            i0++;
+        }
+        if (!mkB) {
+            m.vmodmark[B] = 1;
+            if (i0 < m.nv) m.modlist[i0] = B; else raise_err(m, ERRB_WORKLIST);
+        }
+    }
+    /* mark_fix of the four grains (their dA/dt is settled) */
+    bool nf[4];
+    int nfix = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        bool dup = false;
+        for (int q = 0; q < k; q++) dup |= G[q] == G[k];
+        nf[k] = !fx[k] && !dup;
+        nfix += nf[k];
+    }
+    if (nfix) {
+        int i0 = atomicAdd(m.nfix, nfix);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (nf[k]) {
+                m.gfix[G[k]] = 1;
+                if (i0 < m.ng) m.fixlist[i0] = G[k]; else raise_err(m, ERRB_WORKLIST);
+                i0++;
+            }
+    }
+    int4 ga = P.ga, gb = P.gb;
+    for (int k = 0; k < 3; k++) {
+        if (slot3(ga, k) == G[0]) set_slot3(ga, k, G[3]);
+        if (slot3(gb, k) == G[1]) set_slot3(gb, k, G[2]);
+    }
+    m.vg[A] = ga;
+    m.vg[B] = gb;
+    double2 c = pa;                                         /* vector2_mean, src/geometry.h:311 */
+    c.x += wrapd(pb.x, pa.x, m.D) / 2;
+    c.y += wrapd(pb.y, pa.y, m.D) / 2;
+    c.x = dmod(c.x, m.D);
+    c.y = dmod(c.y, m.D);
+    if (stA != st) { m.pos0[A] = pa; m.vel0[A] = va; m.vstamp[A] = st; }   /* save_vertex */
+    if (stB != st) { m.pos0[B] = pb; m.vel0[B] = vb; m.vstamp[B] = st; }
+    m.pos[A] = c;
+    m.pos[B] = c;
+    if (eps == 0.0) {
+        m.benergy[bnd] = 1.0;
+    } else {
+        int g2c[2];
+        if (gintersect(ga, gb, g2c) < 2) { raise_err(m, ERRB_TOPOLOGY); return; }
+        m.benergy[bnd] = gb_energy(m.gori[g2c[0]] - m.gori[g2c[1]], eps);
+    }
+    m.vel[A] = make_double2(0, 0);
+    m.vel[B] = make_double2(0, 0);
 }
 
 /* apply_flippings (:1016-1026); flips that share no vertex commute, the
@@ -935,10 +1050,12 @@ __global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const
                     hits &= hits - 1;
                     int b = list[base + 32 * k + j];
                     prefetch_flip(m, b, lane);
-                    flip_settle_grains(m, b, lane);
+                    FlipPlan P;
+                    bool planned = flip_plan(m, b, lane, P) && P.AC != P.BE;
                     __syncwarp();
                     if (lane == 0) {
-                        flip_dev(m, b, eps);
+                        if (planned) flip_planned(m, b, eps, P);
+                        else flip_dev(m, b, eps);
                         m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
                     }
                     __syncwarp();
