@@ -308,14 +308,14 @@ KERNEL_BYTES = {
 # k_vertex_fd under profiles/); traffic grows with the units processed, so
 # a full launch is scaled by its units.
 NCU_TRAFFIC_PER_UNIT = {
-    "grain_fd": (52.844e6 + 12.018e6) / 200000,
-    "vertex_fd": (50.048e6 + 0.988e6) / 400000,
+    "grain_fd": (52.807e6 + 11.475e6) / 200000,
+    "vertex_fd": (50.061e6 + 0.945e6) / 400000,
 }
 # FP64 pipe activity of the same captures (of elapsed cycles)
-NCU_FP64_ACTIVE = {"grain_fd": 0.554, "vertex_fd": 0.782}
+NCU_FP64_ACTIVE = {"grain_fd": 0.557, "vertex_fd": 0.650}
 # DADD + DMUL + DFMA thread instructions per unit, ncu counters on the
 # 200K-grain mesh (the FP64 instruction summary kept with the profiles)
-NCU_FP64_INST_PER_UNIT = {"grain_fd": (46.032e6 + 0.702e6) / 200000, "vertex_fd": 38.805e6 / 400000}
+NCU_FP64_INST_PER_UNIT = {"grain_fd": (46.032e6 + 0.702e6) / 200000, "vertex_fd": 24.405e6 / 400000}
 
 
 def run_engine(args):

@@ -236,18 +236,28 @@ __device__ __forceinline__ double wrapd(double dest, double orig, double D) /* w
 }
 /* ---- correctly rounded division and square root for vector2_mag ----
  * On GB300 a binary64 division or square root costs ~10-12 FP64
- * instructions (ncu: 16 for the pair).  These versions take a binary32
- * seed from the special-function unit and refine it on the FP32 pipe to a
- * float-float approximation of the result (~45 bits), assembled into a
- * binary64 on the integer pipe; one FP64 correction step follows
- * (Markstein's method: P. Markstein, "IA-64 and elementary functions",
- * 2000, ch. 8; J.-M. Muller et al., Handbook of Floating-Point Arithmetic,
- * 2nd ed., 2018, sec. 4.7) and then the result is CERTIFIED exactly: the
- * remainder of the candidate is computed with one fma and compared, on the
- * integer pipe, with the half-ulp bound that characterises round-to-nearest.
- * A candidate that is not certified (about one in 10^4, or special
- * operands) is discarded and the native operation runs, so the returned
- * value is always the correctly rounded one.  3 FP64 instructions each. */
+ * instructions (ncu: 16 for the pair), and the FP64 pipe is the scarce
+ * one (1/64 of the binary32 rate).  These versions use none: a binary32
+ * seed from the special-function unit is refined on the FP32 pipe to a
+ * float-float approximation of the result (~45 bits), its 53-bit
+ * significand K is formed on the integer pipe, and the result is then
+ * corrected and CERTIFIED in integer arithmetic.  With the operands'
+ * significands as integers, the exact quotient or root X lies in one
+ * binade [2^52, 2^53) of the integer scale, and K = RN(X) exactly when
+ * the remainder (N - K Mp for a quotient N / Mp, M - K^2 for a root of M)
+ * lies inside the half-unit band (neither a quotient of two 53-bit
+ * significands nor a square root is ever a rounding midpoint).  The
+ * remainder is formed as a 128-bit integer (64-bit multiply low and
+ * high), so the test is exact; one correction step (remainder times the
+ * binary32 reciprocal, rounded to an integer) and a final +-1 bring K to
+ * the nearest integer.  A candidate that does not pass (special operands,
+ * or a seed too far off) is discarded and the native operation runs, so
+ * the returned value is always the correctly rounded one; the error
+ * analysis of the seed only bounds how often that happens.  The method is
+ * the exact-remainder test of Markstein (P. Markstein, "IA-64 and
+ * elementary functions", 2000, ch. 8; J.-M. Muller et al., Handbook of
+ * Floating-Point Arithmetic, 2nd ed., 2018, sec. 4.7 and 5.5) carried out
+ * on integer significands. */
 
 /* binary32 -> binary64 by bit manipulation (exact for normal x; zero and
  * subnormal x give 0, an error the certification absorbs) */
@@ -305,6 +315,35 @@ __device__ __forceinline__ float rsqrt_seed(float x)
     return r;
 }
 
+constexpr unsigned long long SEVC_MANT = 0x000FFFFFFFFFFFFFULL, SEVC_HIDDEN = 1ULL << 52;
+
+/* r = x - y z for the 128-bit x = (xhi, xlo) and 64-bit y, z, all
+ * unsigned, wrapping; true when the difference fits in a signed 64-bit
+ * integer (then r is its exact value) */
+__device__ __forceinline__ bool rem128(unsigned long long xhi, unsigned long long xlo, unsigned long long y,
+                                       unsigned long long z, long long &r)
+{
+    unsigned long long plo = y * z, phi = __umul64hi(y, z);
+    unsigned long long lo = xlo - plo, hi = xhi - phi - (xlo < plo ? 1ULL : 0ULL);
+    r = (long long)lo;
+    return hi == (unsigned long long)(r >> 63);
+}
+/* the significand of the binary64 pattern b as an integer aligned to the
+ * binade of biased exponent E (2^52 <= result < 2^53 when b's exponent is
+ * E); false when b is more than one binade away */
+__device__ __forceinline__ bool sig_at(long long b, int E, unsigned long long &K)
+{
+    int e = (int)(b >> 52);
+    unsigned long long M = ((unsigned long long)b & SEVC_MANT) | SEVC_HIDDEN;
+    if (e == E) K = M;
+    else if (e == E + 1) K = M << 1;
+    else if (e == E - 1) K = M >> 1;
+    else return false;
+    return true;
+}
+/* binary32 estimate of x / 2^32 for a signed 64-bit x, on the FP32 side */
+__device__ __forceinline__ float hi32f(long long x) { return __int2float_rn((int)(x >> 32)); }
+
 /* r = RN(q / p) for 0 <= q <= p; false when not certified */
 __device__ __forceinline__ bool div_fast(double q, double p, double &r)
 {
@@ -327,26 +366,29 @@ __device__ __forceinline__ bool div_fast(double q, double p, double &r)
     float al = fmaf(qh, y0, -ah);
     al = fmaf(qh, yl, al);
     al = fmaf(ql, y0, al);
-    double y0d = f2d_bits(y0);
-    double q0 = ff_to_double(ah, al);                     /* ~2^-44 */
-    double rem = __fma_rn(-P, q0, Q);
-    double q1 = __fma_rn(rem, y0d, q0);                   /* ~2^-67 */
-    double rem1 = __fma_rn(-P, q1, Q);                    /* exact when q1 is faithful */
-    unsigned long long rb = mag2(rem1);
-    long long b1 = dbits(q1);
-    r = q1;
-    /* RN(Q/P) = q1 iff Q/P is within ulp(q1)/2 of q1 (within ulp(q1)/4
-     * below a power of two, whose lower neighbour is closer); ties cannot
-     * occur.  Sufficient: |Q - P q1| < P ulp(q1)/2 (or /4 for a power of
-     * two, on both sides).  RN is monotonic and the bound is a binary64, so
-     * the rounded remainder decides it even where the remainder is not
-     * exact.  (No separate test for a zero remainder: the compiler would
-     * make it an FP64 comparison.) */
-    int e1 = (int)(b1 >> 52);                             /* negative for a negative q1 */
-    if (e1 < 55 || e1 > 2046) return false;
-    int sh = (b1 & 0x000FFFFFFFFFFFFFLL) == 0 ? 1077 : 1076;
-    long long bound = dbits(P) + (long long)(e1 - sh) * (1LL << 52);
-    return rb < ((unsigned long long)bound << 1);
+    /* integer scale: X = N / Mp in [2^52, 2^53), the result's biased
+     * exponent E */
+    unsigned long long Mp = ((unsigned long long)pb & SEVC_MANT) | SEVC_HIDDEN;
+    unsigned long long Mq = ((unsigned long long)qb & SEVC_MANT) | SEVC_HIDDEN;
+    int up = Mq >= Mp ? 0 : 1;
+    int E = eq - ep + 1023 - up, sh = 52 + up;
+    unsigned long long Nhi = Mq >> (64 - sh), Nlo = Mq << sh;
+    unsigned long long K;
+    if (!sig_at(dbits(ff_to_double(ah, al)), E, K)) return false;
+    long long R;                                          /* N - K Mp */
+    if (!rem128(Nhi, Nlo, K, Mp, R)) return false;
+    /* K += R / Mp (1/Mp = y0 2^-52) rounded, then the nearest integer */
+    int d = __float2int_rn(hi32f(R) * y0 * 0x1p-20f);
+    K += (unsigned long long)(long long)d;
+    unsigned long long Ru = (unsigned long long)R - (unsigned long long)(long long)d * Mp;
+    long long half = (long long)((Mp - 1) >> 1);          /* |R| < Mp/2 <=> |R| <= half */
+    if ((long long)Ru > half) K += 1;
+    else if ((long long)Ru < -half) K -= 1;
+    if (!rem128(Nhi, Nlo, K, Mp, R) || R > half || R < -half) return false;
+    if (K < SEVC_HIDDEN || K > (SEVC_HIDDEN << 1)) return false;
+    /* K = 2^53 carries into the exponent */
+    r = __longlong_as_double(((long long)E << 52) + (long long)(K - SEVC_HIDDEN));
+    return true;
 }
 
 /* r = RN(sqrt(t)) for t in [1, 2); false when not certified */
@@ -366,22 +408,27 @@ __device__ __forceinline__ bool sqrt_fast(double t, double &r)
     float sl = fmaf(th, y0, -sh);
     sl = fmaf(th, yl, sl);
     sl = fmaf(tl, y0, sl);
-    double y0d = f2d_bits(y0);
-    double s0 = ff_to_double(sh, sl);                     /* sqrt(t) to ~2^-44 */
-    double d = __fma_rn(-s0, s0, t);
-    double s1 = __fma_rn(d, __longlong_as_double(dbits(y0d) - (1LL << 52)), s0);   /* + d y0/2: ~2^-67 */
-    double e1 = __fma_rn(-s1, s1, t);
-    unsigned long long eb = mag2(e1);
-    long long sb = dbits(s1);
-    r = s1;
-    /* For s1 in (1, 2), u = ulp(s1) = 2^-52: RN(sqrt t) = s1 iff
-     * |t - s1^2| < s1 u - u^2/4 on both sides.  |RN(t - s1^2)| < s1 u (a
-     * binary64 whose predecessor is s1 u - 2^-104) implies it, the
-     * rounding of the remainder being at most 2^-105.  For s1 = 1 the
-     * remainder t - 1 is exact and t >= 1, so the narrower interval below
-     * 1 never matters and the same test certifies exactly t = 1. */
-    if ((sb >> 52) != 1023) return false;
-    return eb < ((unsigned long long)(sb - (52LL << 52)) << 1);
+    /* integer scale: X = sqrt(M) for M = Mt 2^52, X in [2^52, 2^52.5),
+     * result exponent 1023; RN(X) = S iff -S < M - S^2 <= S */
+    unsigned long long Mt = ((unsigned long long)tb & SEVC_MANT) | SEVC_HIDDEN;
+    unsigned long long Mhi = Mt >> 12, Mlo = Mt << 52;
+    long long b0 = dbits(ff_to_double(sh, sl));
+    unsigned long long S;
+    if ((b0 >> 52) == 1022) S = SEVC_HIDDEN;              /* just below 1 */
+    else if (!sig_at(b0, 1023, S)) return false;
+    long long F;                                          /* M - S^2 */
+    if (!rem128(Mhi, Mlo, S, S, F)) return false;
+    /* S += F / (2 S) (1/(2S) = y0 2^-53) rounded, then the nearest integer */
+    int d = __float2int_rn(hi32f(F) * y0 * 0x1p-21f);
+    unsigned long long dd = (unsigned long long)(long long)d;
+    unsigned long long Fu = (unsigned long long)F - 2 * S * dd - dd * dd;
+    S += dd;
+    if ((long long)Fu > (long long)S) S += 1;
+    else if ((long long)Fu <= -(long long)S) S -= 1;
+    if (!rem128(Mhi, Mlo, S, S, F) || F > (long long)S || F <= -(long long)S) return false;
+    if (S < SEVC_HIDDEN || S >= (SEVC_HIDDEN << 1)) return false;
+    r = __longlong_as_double((1023LL << 52) + (long long)(S - SEVC_HIDDEN));
+    return true;
 }
 
 /* vector2_mag (src/geometry.h:217): p sqrt(1 + (q/p)^2) with p = max(|x|,
