@@ -535,15 +535,32 @@ __device__ __forceinline__ void text_label_one(const DevMesh &m, int b, uint8_t 
     m.bcand[b] = (uint8_t)cand;
     m.bconf[b] = -1;
 }
+/* Two boundaries per thread (b and b + blockDim.x of the block's pair of
+ * tiles), every load of both issued before either is labelled: the pass
+ * waits on two rounds of gathers, and twice the loads in flight per thread
+ * hide more of that latency than the registers they cost. */
 __global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, const int *flags)
 {
-    int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= m.nb) return;
-    uint8_t en = m.ben[b];
-    int2 e = m.bv[b];                      /* loaded beside the flag: one round trip less */
-    double2 z = make_double2(0, 0), pi = z, pe = z, vi = z, ve = z;
-    if (en) { pi = m.pos[e.x]; pe = m.pos[e.y]; vi = m.vel[e.x]; ve = m.vel[e.y]; }
-    text_label_one(m, b, en, pi, pe, vi, ve, dt, Df, hDf, inv_dt, flags[0]);
+    int b0 = 2 * blockIdx.x * blockDim.x + threadIdx.x;
+    int full = flags[0];
+    uint8_t en[2];
+    int2 e[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        int b = b0 + k * blockDim.x;
+        bool in = b < m.nb;
+        en[k] = in ? m.ben[b] : 0;
+        e[k] = in ? m.bv[b] : make_int2(0, 0);   /* loaded beside the flag: one round trip less */
+    }
+    double2 z = make_double2(0, 0), pi[2] = { z, z }, pe[2] = { z, z }, vi[2] = { z, z }, ve[2] = { z, z };
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+        if (en[k]) { pi[k] = m.pos[e[k].x]; pe[k] = m.pos[e[k].y]; vi[k] = m.vel[e[k].x]; ve[k] = m.vel[e[k].y]; }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        int b = b0 + k * blockDim.x;
+        if (b < m.nb) text_label_one(m, b, en[k], pi[k], pe[k], vi[k], ve[k], dt, Df, hDf, inv_dt, full);
+    }
 }
 
 /* compute_grain_areas, src/calculus.h:224 */
@@ -724,7 +741,7 @@ void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const L
     /* binary32 copies for the certificate (text_outside_dt): rounded to
      * nearest, within 2^-24 of the binary64 values */
     float Df = (float)m.D, hDf = (float)(m.D / 2.0), inv_dt = (float)(1.0 / dt);
-    if (m.nb > 0) COUNT_LAUNCHES(1), k_text_label<<<(m.nb + t - 1) / t, t, 0, s>>>(m, dt, Df, hDf, inv_dt, x.flags);
+    if (m.nb > 0) COUNT_LAUNCHES(1), k_text_label<<<(m.nb + 2 * t - 1) / (2 * t), t, 0, s>>>(m, dt, Df, hDf, inv_dt, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
