@@ -101,6 +101,7 @@ struct DevMesh {
     unsigned *vstamp, *bstamp, *stamp;
     uint8_t *bexact, *gexact;
     uint8_t *bmark;      /* boundaries marked by a sparse pass, compacted next */
+    int *lastblk;        /* arrival counters of last_block, zero between launches */
 };
 
 enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
@@ -130,6 +131,23 @@ __device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int
     EventRec r;
     r.type = type; r.a = a; r.b = b; r.c = c; r.pa = pa; r.pb = pb; r.pc = pc;
     L.buf[i] = r;
+}
+
+/* True in the last block of the grid to get here: every other block has
+ * finished (its reads of work-list counts included), so that block may
+ * reset state the whole grid read.  All threads of every block must call
+ * it; *ctr is zero on entry and left zero. */
+__device__ __forceinline__ bool last_block(int *ctr)
+{
+    __shared__ int last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ctr, 1) == (int)(gridDim.x * gridDim.y) - 1;
+        if (last) *ctr = 0;
+    }
+    __syncthreads();
+    return last != 0;
 }
 
 /* ---- periodic geometry, src/geometry.h:133-331 ----

@@ -195,7 +195,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
         { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.vstamp, V * 4 },
         { (void **)&m.bstamp, B * 4 }, { (void **)&m.stamp, 4 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
-        { (void **)&m.bmark, B },
+        { (void **)&m.bmark, B }, { (void **)&m.lastblk, 8 * 4 },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);

@@ -588,8 +588,8 @@ __global__ void k_area_dirty(DevMesh m, int compute)
         }
         m.gadirty[g] = 0;
     }
+    if (last_block(m.lastblk + 1) && threadIdx.x == 0) *m.nadirty = 0;   /* the list is consumed */
 }
-__global__ void k_reset_count(int *c) { *c = 0; }
 
 /* the step's summary in one buffer, for one readback: counters, events,
  * error bits, polling iterations, 2x3 pass counts (all per instance) and
@@ -747,7 +747,6 @@ void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_area_dirty<<<152, TPB, 0, s>>>(m, compute);
-    COUNT_LAUNCHES(1), k_reset_count<<<1, 1, 0, s>>>(m.nadirty);
 }
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { COUNT_LAUNCHES(1), k_update<<<nblk(m.nv), TPB, 0, s>>>(m, dt); }
 

@@ -1139,11 +1139,11 @@ __global__ void k_fix_clear(DevMesh m)
         if (listed)
             for (int j = 0; j < 4; j++) m.vmod[4 * (size_t)v + j] = make_int4(-1, -1, -1, FIX_NONE);
     }
-}
-__global__ void k_fix_reset(DevMesh m)
-{
-    *m.nfix = 0;
-    *m.nmod = 0;
+    /* empty both work lists once every block has read their lengths */
+    if (last_block(m.lastblk + 0) && threadIdx.x == 0) {
+        *m.nfix = 0;
+        *m.nmod = 0;
+    }
 }
 
 /* instance of every boundary and grain from the offset tables */
@@ -1269,7 +1269,6 @@ void launch_fix_lists(const DevMesh &m, cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_fix_edit<<<WL_BLOCKS, TPB, 0, s>>>(m);
     COUNT_LAUNCHES(1), k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    COUNT_LAUNCHES(1), k_fix_reset<<<1, 1, 0, s>>>(m);
 }
 
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s)
