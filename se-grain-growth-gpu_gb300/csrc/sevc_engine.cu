@@ -94,11 +94,11 @@ struct sevc_handle {
     StepGraph g_pre[2], g_poll, g_post;
     bool use_graphs = true;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    /* side streams of the first half of the step (branches that do not
-     * depend on each other run concurrently; captured as graph branches)
-     * and the fork / join events between them */
+    /* side streams of the step (branches that do not depend on each other
+     * run concurrently; captured as graph branches) and the fork / join
+     * events between them: 0-5 in the first half, 6-7 in the tail */
     cudaStream_t side[2] = { nullptr, nullptr };
-    cudaEvent_t evfork[6] = {};
+    cudaEvent_t evfork[8] = {};
     bool profiling = false;
     std::map<std::string, ProfEntry> prof;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -325,7 +325,7 @@ sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handl
     bool streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
     for (int k = 0; streams_ok && k < 2; k++)
         streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking), "stream");
-    for (int k = 0; streams_ok && k < 6; k++)
+    for (int k = 0; streams_ok && k < 8; k++)
         streams_ok = cuda_ok(cudaEventCreateWithFlags(&h->evfork[k], cudaEventDisableTiming), "event");
     if (!streams_ok || !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") ||
         !cuda_ok(cudaMallocHost(&h->h_big, h->h_big_ints * sizeof(int)), "pinned") ||
@@ -536,11 +536,22 @@ void enqueue_tail(sevc_handle *h, bool lists_unchanged)
     launch_clear_grain_cand(m, x.list_c, x.n_c, s);
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
     { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
+    /* The counts (:317-325) read only grain flags, types and areas, which
+     * are final here (the flips and the list fix-up after them change
+     * none): side0 computes them beside the flips, the fix-up and the
+     * position update, joining before the summary. */
+    if (!h->profiling) {
+        cudaEventRecord(h->evfork[6], s);
+        cudaStreamWaitEvent(h->side[0], h->evfork[6], 0);
+        launch_counts(m, x, h->p, h->side[0]);
+        cudaEventRecord(h->evfork[7], h->side[0]);
+    }
     { Prof pr(h, "unlabel_st2"); launch_unlabel_st2(m, x.list_a, x.n_a, s); }                     /* :282 */
     { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }                     /* :289 */
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :294 */
     { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                                /* :314 */
-    { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }                                       /* :317-325 */
+    if (h->profiling) { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }
+    else cudaStreamWaitEvent(s, h->evfork[7], 0);
     launch_pack_summary(m, x, h->ninst, x.summary, s);
 }
 
