@@ -133,6 +133,11 @@ __device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int
     L.buf[i] = r;
 }
 
+/* first statement of a kernel launched with launch_dep: wait until the
+ * previous kernel of the stream has completed and its writes are visible
+ * (a no-op for a kernel launched without the attribute) */
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 /* True in the last block of the grid to get here: every other block has
  * finished (its reads of work-list counts included), so that block may
  * reset state the whole grid read.  All threads of every block must call

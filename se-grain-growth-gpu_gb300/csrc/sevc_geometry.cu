@@ -541,6 +541,7 @@ __device__ __forceinline__ void text_label_one(const DevMesh &m, int b, uint8_t 
  * hide more of that latency than the registers they cost. */
 __global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, const int *flags)
 {
+    griddep_wait();
     int b0 = 2 * blockIdx.x * blockDim.x + threadIdx.x;
     int full = flags[0];
     uint8_t en[2];
@@ -579,6 +580,7 @@ __global__ void k_grain_area(DevMesh m)
  * the list (marks made by the flips' fix-up after this point). */
 __global__ void k_area_dirty(DevMesh m, int compute)
 {
+    griddep_wait();
     int n = *m.nadirty;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int g = m.adirty[i];
@@ -596,6 +598,7 @@ __global__ void k_area_dirty(DevMesh m, int compute)
  * the output decision */
 __global__ void k_pack_summary(DevMesh m, DevScratch x, int ninst, int *out)
 {
+    griddep_wait();
     size_t nc = (size_t)ninst * CTR_COUNT, ne = (size_t)ninst * EVT_COUNT, np = ninst,
            ns = (size_t)ninst * TWO_THREE_PASSES;
     size_t total = nc + ne + 4 + np + ns + 1;
@@ -620,6 +623,7 @@ __global__ void k_reset_ngrains(int *counters, int ninst)
 /* update_vertices_positions, src/calculus.h:391-404 */
 __global__ void k_update(DevMesh m, double dt)
 {
+    griddep_wait();
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= m.nv || !m.ven[v]) return;
     double2 p = m.pos[v], w = m.vel[v];
@@ -741,20 +745,20 @@ void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const L
     /* binary32 copies for the certificate (text_outside_dt): rounded to
      * nearest, within 2^-24 of the binary64 values */
     float Df = (float)m.D, hDf = (float)(m.D / 2.0), inv_dt = (float)(1.0 / dt);
-    if (m.nb > 0) COUNT_LAUNCHES(1), k_text_label<<<(m.nb + 2 * t - 1) / (2 * t), t, 0, s>>>(m, dt, Df, hDf, inv_dt, x.flags);
+    if (m.nb > 0) launch_dep(k_text_label, (m.nb + 2 * t - 1) / (2 * t), t, s, m, dt, Df, hDf, inv_dt, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_area_dirty<<<152, TPB, 0, s>>>(m, compute);
+    launch_dep(k_area_dirty, 152, TPB, s, m, compute);
 }
-void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { COUNT_LAUNCHES(1), k_update<<<nblk(m.nv), TPB, 0, s>>>(m, dt); }
+void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { launch_dep(k_update, nblk(m.nv), TPB, s, m, dt); }
 
 void launch_pack_summary(const DevMesh &m, const DevScratch &x, int ninst, int *out, cudaStream_t s)
 {
     size_t total = (size_t)ninst * (CTR_COUNT + EVT_COUNT + 1 + TWO_THREE_PASSES) + 5;
     int g = (int)((total + TPB - 1) / TPB);
-    COUNT_LAUNCHES(1), k_pack_summary<<<g < 152 ? g : 152, TPB, 0, s>>>(m, x, ninst, out);
+    launch_dep(k_pack_summary, g < 152 ? g : 152, TPB, s, m, x, ninst, out);
 }
 
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s)

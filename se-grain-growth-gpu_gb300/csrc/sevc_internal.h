@@ -159,4 +159,27 @@ void launch_grain_stats(const DevMesh &m, int lo, int hi, double *out, cudaStrea
 extern long long sevc_kernel_launches;
 #define COUNT_LAUNCHES(k) (sevc_kernel_launches += (k))
 
+/* Launch with programmatic dependent launch allowed: the grid may be
+ * scheduled while the previous kernel of the stream drains, which hides
+ * most of the launch gap between the short kernels of the step's sparse
+ * half.  Every kernel launched this way calls griddep_wait() before its
+ * first global memory access; that returns once the previous kernel has
+ * completed and its writes are visible, so only the scheduling overlaps. */
+template <typename... P, typename... A>
+inline void launch_dep(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s, A &&...args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    COUNT_LAUNCHES(1);
+    cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(args)...);
+}
+
 #endif

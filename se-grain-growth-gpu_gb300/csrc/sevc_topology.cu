@@ -202,6 +202,7 @@ __device__ __forceinline__ unsigned flag_mask16(const DevMesh &m, int i0, int n)
 template <int KIND>
 __global__ void k_flag_count(DevMesh m, int n, int *blockcnt)
 {
+    griddep_wait();
     int i0 = (blockIdx.x * TPB + threadIdx.x) * CT_ITEMS;
     int c = i0 < n ? __popc(flag_mask16<KIND>(m, i0, n)) : 0;
     __shared__ int s[TPB / 32];
@@ -217,6 +218,7 @@ __global__ void k_flag_count(DevMesh m, int n, int *blockcnt)
 template <int KIND>
 __global__ void k_flag_scatter(DevMesh m, int n, const int *blockcnt, int *out, int *n_out)
 {
+    griddep_wait();
     __shared__ int s[TPB / 32];
     __shared__ int base_off, tot;
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -261,6 +263,7 @@ __global__ void k_flag_scatter(DevMesh m, int n, const int *blockcnt, int *out, 
 /* vertices_vote (:362) for the endpoints of listed boundaries */
 __global__ void k_poll_vote(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
     if (m.pdone[m.binst[list[i]]]) continue;
     int2 e = m.bv[list[i]];
@@ -281,6 +284,7 @@ __global__ void k_poll_vote(DevMesh m, const int *list, const int *n)
 /* count_boundaries_votes (:406) */
 __global__ void k_poll_count(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int b = list[i];
         if (!(m.ben[b] && m.bcand[b]) || m.pdone[m.binst[b]]) continue;
@@ -293,6 +297,7 @@ __global__ void k_poll_count(DevMesh m, const int *list, const int *n)
  * writes cannot change any thread's decision. */
 __global__ void k_poll_unlabel(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int b = list[i];
         if (!(m.ben[b] && m.bcand[b] && m.bvotes[b] == 2) || m.pdone[m.binst[b]]) continue;
@@ -310,6 +315,7 @@ __global__ void k_poll_unlabel(DevMesh m, const int *list, const int *n)
  * write_candidate_results (:466-477) for the same element. */
 __global__ void k_poll_compare_write(DevMesh m, int *threadfail, int grid)
 {
+    griddep_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= m.nb) return;
     int inst = m.binst[b];
@@ -324,6 +330,7 @@ __global__ void k_poll_compare_write(DevMesh m, int *threadfail, int grid)
  * unchanged).  grid >= 16. */
 __global__ void k_poll_compare_write16(DevMesh m, int *threadfail, int grid)
 {
+    griddep_wait();
     int b0 = (blockIdx.x * blockDim.x + threadIdx.x) * 16;
     if (b0 >= m.nb || m.pdone[0]) return;
     uint4 we = *reinterpret_cast<const uint4 *>(m.ben + b0);
@@ -358,6 +365,7 @@ __global__ void k_poll_compare_write16(DevMesh m, int *threadfail, int grid)
  * :526-537) */
 __global__ void k_poll_final(DevMesh m, int *threadfail, int *pblock)
 {
+    griddep_wait();
     __shared__ int t[256];
     int inst = blockIdx.y;
     if (m.pdone[inst]) return;
@@ -375,6 +383,7 @@ __global__ void k_poll_final(DevMesh m, int *threadfail, int *pblock)
  * passed has converged and takes no further iteration this step */
 __global__ void k_poll_status(DevMesh m, const int *pblock, int nblocks, int *piters, int *nrun)
 {
+    griddep_wait();
     int inst = blockIdx.x * blockDim.x + threadIdx.x;
     if (inst >= m.ninst || m.pdone[inst]) return;
     piters[inst]++;
@@ -413,6 +422,7 @@ __device__ void conflict_check_one(const DevMesh &m, int b)
  * to a candidate (the only ones it can mark) */
 __global__ void k_conflict_check(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int c = list[i];
         if (!(m.ben[c] && m.bcand[c])) continue;
@@ -428,6 +438,7 @@ __global__ void k_conflict_check(DevMesh m, const int *list, const int *n)
 }
 __global__ void k_conflict_unlabel(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int b = list[i];
         if (!(m.ben[b] && m.bcand[b])) continue;
@@ -623,6 +634,7 @@ __device__ uint8_t label3_cand(const DevMesh &m, int g, double dt)
 /* clear_grains_state + label_3sided_grains for enabled grains */
 __global__ void k_label_3sided(DevMesh m, double dt)
 {
+    griddep_wait();
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= m.ng || !m.gen[g]) return;
     m.gcand[g] = m.gvlen[g] == 3 ? label3_cand(m, g, dt) : 0;
@@ -633,6 +645,7 @@ __global__ void k_label_3sided(DevMesh m, double dt)
  * it listed as a candidate (k_clear_grain_cand). */
 __global__ void k_label_3sided_bucket(DevMesh m, double dt, const int *perm, const int *vbucket)
 {
+    griddep_wait();
     int n3 = vbucket[VB_COUNT(3)], start = vbucket[VB_START(3)];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
         int g = perm[start + i];
@@ -641,6 +654,7 @@ __global__ void k_label_3sided_bucket(DevMesh m, double dt, const int *perm, con
 }
 __global__ void k_clear_grain_cand(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) m.gcand[list[i]] = 0;
 }
 
@@ -726,6 +740,7 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
  * them in list order */
 __global__ void k_remove_grains(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (inst >= m.ninst) return;
     int lo = lower_bound_i(list, *n, m.goff[inst]);
@@ -748,6 +763,7 @@ __global__ void k_remove_grains(DevMesh m, const int *list, const int *n)
 /* unlabel_boundaries_st2 (:588-606) */
 __global__ void k_unlabel_st2(DevMesh m, const int *list, const int *n)
 {
+    griddep_wait();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
         int b = list[i];
         if (!(m.ben[b] && m.bcand[b])) continue;
@@ -1024,6 +1040,7 @@ __device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPl
 constexpr int FLIP_TPB = 512;
 __global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const int *list, const int *n)
 {
+    griddep_wait();
     __shared__ unsigned hitmask[FLIP_TPB / 32];
     int inst = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int lo = 0, hi = *n;
@@ -1104,6 +1121,7 @@ __device__ void fix_grain(const DevMesh &m, int g)
 }
 __global__ void k_fix_edit(DevMesh m)
 {
+    griddep_wait();
     int nf = *m.nfix;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
         int g = m.fixlist[w];
@@ -1115,6 +1133,7 @@ __global__ void k_fix_edit(DevMesh m)
  * grains can have fix set and only marked vertices can hold mods. */
 __global__ void k_fix_clear(DevMesh m)
 {
+    griddep_wait();
     int nf = *m.nfix, nm = *m.nmod;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
         int g = m.fixlist[w];
@@ -1167,8 +1186,8 @@ void compact_impl(const DevMesh &m, const DevScratch &x, int n, int *out, int *n
                  : KIND == CK_GRAIN_CAND ? ((uintptr_t)m.gen | (uintptr_t)m.gcand) : (uintptr_t)m.bmark;
     bool flags16 = (KIND == CK_CAND || KIND == CK_GRAIN_CAND || KIND == CK_MARKED) && (al & 15u) == 0;
     if (flags16) {
-        COUNT_LAUNCHES(1), k_flag_count<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt);
-        COUNT_LAUNCHES(1), k_flag_scatter<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt, out, n_out);
+        launch_dep(k_flag_count<KIND>, tiles, TPB, s, m, n, x.blockcnt);
+        launch_dep(k_flag_scatter<KIND>, tiles, TPB, s, m, n, x.blockcnt, out, n_out);
     } else {
         COUNT_LAUNCHES(1), k_compact_count<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt);
         COUNT_LAUNCHES(1), k_compact_scatter<KIND><<<tiles, TPB, 0, s>>>(m, n, x.blockcnt, out, n_out);
@@ -1202,27 +1221,27 @@ void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *can
                            const StepParams &p, cudaStream_t s)
 {
     int g = listgrid(m.nb);
-    COUNT_LAUNCHES(1), k_poll_vote<<<g, TPB, 0, s>>>(m, cand, ncand);
-    COUNT_LAUNCHES(1), k_poll_count<<<g, TPB, 0, s>>>(m, cand, ncand);
-    COUNT_LAUNCHES(1), k_poll_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
+    launch_dep(k_poll_vote, g, TPB, s, m, cand, ncand);
+    launch_dep(k_poll_count, g, TPB, s, m, cand, ncand);
+    launch_dep(k_poll_unlabel, g, TPB, s, m, cand, ncand);
     int grid = p.n_blocks * p.n_threads;
     bool aligned = (((uintptr_t)m.ben | (uintptr_t)m.bcand | (uintptr_t)m.bcandbuf) & 15u) == 0;
     if (p.ninst == 1 && grid >= 16 && aligned) {
         int th = (m.nb + 15) / 16;
-        COUNT_LAUNCHES(1), k_poll_compare_write16<<<(th + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+        launch_dep(k_poll_compare_write16, (th + TPB - 1) / TPB, TPB, s, m, x.threadfail, grid);
     } else {
-        COUNT_LAUNCHES(1), k_poll_compare_write<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, x.threadfail, grid);
+        launch_dep(k_poll_compare_write, (m.nb + TPB - 1) / TPB, TPB, s, m, x.threadfail, grid);
     }
-    COUNT_LAUNCHES(1), k_poll_final<<<dim3(p.n_blocks, p.ninst), p.n_threads, 0, s>>>(m, x.threadfail, x.pblock);
+    launch_dep(k_poll_final, dim3(p.n_blocks, p.ninst), p.n_threads, s, m, x.threadfail, x.pblock);
     cudaMemsetAsync(x.nrun, 0, sizeof(int), s);
-    COUNT_LAUNCHES(1), k_poll_status<<<(p.ninst + 127) / 128, 128, 0, s>>>(m, x.pblock, p.n_blocks, x.piters, x.nrun);
+    launch_dep(k_poll_status, (p.ninst + 127) / 128, 128, s, m, x.pblock, p.n_blocks, x.piters, x.nrun);
 }
 
 void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
 {
     int g = listgrid(m.nb);
-    COUNT_LAUNCHES(1), k_conflict_check<<<g, TPB, 0, s>>>(m, cand, ncand);
-    COUNT_LAUNCHES(1), k_conflict_unlabel<<<g, TPB, 0, s>>>(m, cand, ncand);
+    launch_dep(k_conflict_check, g, TPB, s, m, cand, ncand);
+    launch_dep(k_conflict_unlabel, g, TPB, s, m, cand, ncand);
 }
 
 inline int instgrid(const DevMesh &m) { return (m.ninst + 31) / 32; }
@@ -1238,37 +1257,37 @@ void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool 
 {
     if (bucket) {
         int g = (m.ng + TPB - 1) / TPB;
-        COUNT_LAUNCHES(1), k_label_3sided_bucket<<<g < 4 * 152 ? g : 4 * 152, TPB, 0, s>>>(m, dt, x.perm, x.vbucket);
+        launch_dep(k_label_3sided_bucket, g < 4 * 152 ? g : 4 * 152, TPB, s, m, dt, x.perm, x.vbucket);
     } else {
-        COUNT_LAUNCHES(1), k_label_3sided<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, dt);
+        launch_dep(k_label_3sided, (m.ng + TPB - 1) / TPB, TPB, s, m, dt);
     }
 }
 void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_clear_grain_cand<<<32, TPB, 0, s>>>(m, list, n);
+    launch_dep(k_clear_grain_cand, 32, TPB, s, m, list, n);
 }
 
 void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_remove_grains<<<m.ninst, 32, 0, s>>>(m, list, n);
+    launch_dep(k_remove_grains, m.ninst, 32, s, m, list, n);
 }
 
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_unlabel_st2<<<listgrid(m.nb), TPB, 0, s>>>(m, cand, ncand);
+    launch_dep(k_unlabel_st2, listgrid(m.nb), TPB, s, m, cand, ncand);
 }
 
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s)
 {
     (void)x;
-    COUNT_LAUNCHES(1), k_flips<<<m.ninst, FLIP_TPB, 0, s>>>(m, eps, cand, ncand);
+    launch_dep(k_flips, m.ninst, FLIP_TPB, s, m, eps, cand, ncand);
 }
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_fix_edit<<<WL_BLOCKS, TPB, 0, s>>>(m);
-    COUNT_LAUNCHES(1), k_fix_clear<<<WL_BLOCKS, TPB, 0, s>>>(m);
+    launch_dep(k_fix_edit, WL_BLOCKS, TPB, s, m);
+    launch_dep(k_fix_clear, WL_BLOCKS, TPB, s, m);
 }
 
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s)
