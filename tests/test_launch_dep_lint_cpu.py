@@ -41,3 +41,26 @@ def test_kernels_launched_with_launch_dep_wait_first():
         if first != "griddep_wait()":
             missing.append((name, first))
     assert not missing, missing
+
+
+def _kernel_bodies(text):
+    """(name, body) of every __global__ function in text, body by brace matching"""
+    for mo in re.finditer(r"__global__ void (?:__launch_bounds__\([^)]*\)\s*)?(\w+)\([^)]*\)\s*\{", text):
+        depth, i = 1, mo.end()
+        while depth:
+            depth += {"{": 1, "}": -1}.get(text[i], 0)
+            i += 1
+        yield mo.group(1), text[mo.end():i - 1]
+
+
+def test_kernels_with_last_block_never_return_early():
+    """last_block counts the blocks that reach it: a thread that returns
+    before it would leave the count short and the list counts it resets
+    would never be reset."""
+    found = 0
+    for f, text in _sources().items():
+        for name, body in _kernel_bodies(text):
+            if "last_block(" in body:
+                found += 1
+                assert not re.search(r"\breturn\b", body), name
+    assert found >= 2
