@@ -7,24 +7,31 @@ B = 3M boundaries), FP64, isotropic boundaries (GB_eps = 0, gamma = 1),
 per-grain stored energy lognormal(mu=-1, sigma=0.5), Monte-Carlo nucleation
 on (one attempt every nucleation_gap = 10 steps once 1/6 of the grains are
 gone, the reference's rule), domain [0, 1000)^2 so that grains are about one
-unit across as in the reference's example.ini, dt = 1e-4 (example.ini).
+unit across as in the reference's example.ini, dt = 2e-4.  The run is the
+configuration's: 10,000 steps or until 20% of the grains remain; the 5/6
+gate is passed after about 7,000 steps, so the last ~3,000 steps carry
+nucleation attempts and tens of removals and flips per step.
 Inputs are synthetic (seeded generator); there is no dataset.
 
 A "step" is one iteration of the reference's main loop (src/main.cu:121-389).
 metric = sum over timed steps of the enabled vertices / time.
 
-  value    device time (CUDA events on the engine's stream), mesh resident
-           in HBM, K steps after W warm-up steps;
-  e2e      the same through the C ABI from host buffers: upload of the mesh,
-           K steps with the per-step summary read back, download of the
-           final state - all inside the timed region;
-  roofline per-kernel CUDA-event times from a profiling pass of the same
-           workload; algorithmic bytes per launch are KERNEL_BYTES below.
+  value     device time (CUDA events on the engine's stream), mesh resident
+            in HBM, of K steps starting W steps past the nucleation gate
+            (from a checkpoint; the event-heavy phase of the run);
+  e2e       the configuration's whole run through the C ABI from host
+            buffers: mesh build and upload, every step with its summary
+            read back, download of the final state - all inside the timed
+            region;
+  t0_window the first K steps after W of the same run (hardly any events);
+  roofline  per-kernel CUDA-event times from a profiling pass of the same
+            window; algorithmic bytes per launch are KERNEL_BYTES below.
 
 --impl reference times the reference's algorithm on the host cores: the
-oracle restatement (the reference's CUDA program cannot run where the
-benchmark runs: its sources are not there and binaries built elsewhere are
-x86).
+oracle restatement (the reference's CUDA program is not part of this
+benchmark: its sources do not travel with the repository), on the t = 0
+window of the same configuration (a CPU cannot reach the gate in a bounded
+sample; the oracle's cost per step hardly depends on the phase).
 """
 import argparse
 import json
@@ -43,8 +50,12 @@ METRIC = "vertex-steps/s at 1M grains"
 UNIT = "vertex-steps/s"
 
 
+FULL_STEPS = 10000     # the configuration's run: 10,000 steps ...
+LEAVE = 0.2            # ... or until 20% of the grains remain
+
+
 def workload_options(mod, n, steps):
-    kw = dict(n_grains=n, dt=1e-4, dtau=1e-3, nucleation_gap=10, domain_bound=1000.0, GB_eps=0.0, GB_scaling=1.0,
+    kw = dict(n_grains=n, dt=2e-4, dtau=2e-3, nucleation_gap=10, domain_bound=1000.0, GB_eps=0.0, GB_scaling=1.0,
               SE_eps=1.0, SE_min=999.0, SE_max=999.0, do_nucleation=1, MC_k=1.0, nmax=10 ** 8, tmax=-1,
               snap_gap=10 ** 8, min_grains=-1, n_blocks=32, n_threads=256)
     o = mod.default_options(**kw)
@@ -52,18 +63,38 @@ def workload_options(mod, n, steps):
     return o
 
 
+def current_gpu_bus_id():
+    """PCI bus id of this process's CUDA device 0 (the first one visible
+    under CUDA_VISIBLE_DEVICES), the id nvidia-smi -i takes; None if the
+    runtime cannot say."""
+    import ctypes
+    import glob
+    for name in ["libcudart.so"] + sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            rt = ctypes.CDLL(name)
+        except OSError:
+            continue
+        buf = ctypes.create_string_buffer(64)
+        if rt.cudaDeviceGetPCIBusId(buf, 64, 0) == 0:
+            return buf.value.decode()
+        return None
+    return None
+
+
 class Clocks:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples of this process's GPU during the timed region."""
 
     def __init__(self):
         self.samples, self.proc = [], None
+        self.gpu = current_gpu_bus_id()
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "50", "-i", "0"],
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "50",
+                 "-i", self.gpu or "0"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
             t0 = time.time()                 # the timed region starts once sampling runs
@@ -88,7 +119,7 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples), "gpu": self.gpu or "index 0"}
 
 
 def make_mesh(n, seed, cache=None):
@@ -319,6 +350,22 @@ NCU_FP64_INST_PER_UNIT = {"grain_fd": (46.032e6 + 0.702e6) / 200000, "vertex_fd"
 
 
 def run_engine(args):
+    """The 1M-grain workload in three legs.
+
+    full run  the configuration's whole run (10,000 steps or until 20% of
+              the grains remain) through the C ABI from host buffers:
+              host mesh build and upload, every step with its summary
+              read back, the final state downloaded -> e2e.  On the way it
+              saves a checkpoint W steps after the 5/6 nucleation gate.
+    window    from that checkpoint: K steps timed with CUDA events on the
+              engine's stream (mesh resident) -> value; then the same K
+              steps again with per-kernel events -> roofline.
+    cpu       the oracle built from the window's starting state, on every
+              host core -> cpu_baseline (same window).
+    """
+    import tempfile
+
+    import numpy as np
     import sevc
     n = args.grains
     t0 = time.time()
@@ -326,18 +373,56 @@ def run_engine(args):
     gen_s = time.time() - t0
     opt = workload_options(sevc, n, args.steps)
     host_bytes = mesh["xy"].nbytes + mesh["ridges"].nbytes + mesh["oris"].nbytes + mesh["se"].nbytes
+    tmpdir = tempfile.mkdtemp(prefix="sevc_bench_")
+    ckpt = os.path.join(tmpdir, "window.ckpt")
+    W, K = args.warmup, args.steps
 
-    # ---------------- device-resident leg ----------------
+    # ---------------- full run, end to end through the C ABI ----------------
+    e0 = time.time()
     eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
-    g = n
-    for _ in range(args.warmup):
-        g = eng.step().curr_n_grains
-    shapes = eng.autotune(3)          # launch shapes for this mesh; the state is left as it was
+    g, vs, ms_full, k = n, 0, 0.0, 0
+    gate, ck_s, win_state, t0_ms, t0_vs = None, 0.0, None, 0.0, 0
+    ev_full = np.zeros(5, np.int64)
+    while k < FULL_STEPS and g > LEAVE * n:
+        if gate is not None and k == gate + W and win_state is None:
+            c0 = time.time()                     # excluded from the e2e time
+            eng.checkpoint_save(ckpt)
+            win_state = (eng.get_state(), k)
+            ck_s += time.time() - c0
+        info = eng.step()
+        vs += 2 * g
+        ms_full += info.gpu_ms
+        if W <= k < W + K:                     # the first K steps after W: the t = 0 window
+            t0_ms += info.gpu_ms
+            t0_vs += 2 * g
+        g = info.curr_n_grains
+        ev_full += (info.n_flips, info.n_removals, info.n_two_three, info.nucleation_attempted, info.n_nucleations)
+        k += 1
+        if gate is None and g <= 5 * n // 6:
+            gate = k
+        if not info.keep_going:
+            break
+    st_final = eng.get_state()
+    e_wall = time.time() - e0 - ck_s
+    eng.close()
+    state_bytes = sum(a.nbytes for a in st_final.values())
+    del st_final
+    if win_state is None:
+        raise RuntimeError("the run did not pass the nucleation gate (gate %s, %d steps)" % (gate, k))
+
+    # ---------------- the window past the gate, device-timed ----------------
+    eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    eng.checkpoint_load(ckpt)
+    shapes = eng.autotune(3)          # launch shapes for this state; the state is left as it was
+    for _ in range(W):                # graphs captured, caches warm
+        eng.step()
+    eng.checkpoint_load(ckpt)
+    g0 = int(win_state[0]["gen"].sum())
     clocks = Clocks()
     clocks.start()
-    ms, vsteps, infos = 0.0, 0, []
+    ms, vsteps, infos, g = 0.0, 0, [], g0
     w0 = time.time()
-    for _ in range(args.steps):
+    for _ in range(K):
         vsteps += 2 * g          # enabled vertices at the start of the step (V = 2G)
         info = eng.step()
         infos.append(info)
@@ -347,16 +432,17 @@ def run_engine(args):
     ck = clocks.stop()
     value = vsteps / (ms / 1e3)
 
-    # ---------------- profiling pass (per-kernel event times) ----------------
+    # ---------------- profiling pass of the same window ----------------
+    eng.checkpoint_load(ckpt)
     eng.set_profiling(True)
-    for _ in range(max(1, args.prof_steps)):
+    for _ in range(K):
         eng.step()
     prof = eng.profile()
     eng.close()
     tot = sum(v[0] for v in prof.values())
-    dom = max((k for k in prof if k in KERNEL_BYTES), key=lambda k: prof[k][0])
+    dom = max((kk for kk in prof if kk in KERNEL_BYTES), key=lambda kk: prof[kk][0])
     unit, per_unit = KERNEL_BYTES[dom]
-    units = {"grains": g, "vertices": 2 * g, "boundaries": 3 * g}[unit]
+    units = {"grains": g0, "vertices": 2 * g0, "boundaries": 3 * g0}[unit]
     avg_ms = prof[dom][0] / prof[dom][1]
     achieved = per_unit * units / (avg_ms / 1e3) / 1e9
     peaks = {}
@@ -367,67 +453,70 @@ def run_engine(args):
     peak = peaks.get("hbm_gbs", 6800.0)
     fp64_peak = sevc.measure_fp64_rate()
     fp64 = {}
-    for k in ("grain_fd", "vertex_fd"):
-        if k in prof and prof[k][1]:
-            u = {"grains": g, "vertices": 2 * g, "boundaries": 3 * g}[KERNEL_BYTES[k][0]]
-            ach = NCU_FP64_INST_PER_UNIT[k] * u / (prof[k][0] / prof[k][1] / 1e3)
-            fp64[k] = {"achieved": ach, "frac": ach / fp64_peak}
-
-    # ---------------- end-to-end leg through the C ABI ----------------
-    e0 = time.time()
-    eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
-    e_vsteps = 0
-    g = n
-    for _ in range(args.steps):
-        info = eng.step()
-        e_vsteps += 2 * g
-        g = info.curr_n_grains
-    st = eng.get_state()
-    e_wall = time.time() - e0
-    eng.close()
-    state_bytes = sum(a.nbytes for a in st.values())
+    for kk in ("grain_fd", "vertex_fd"):
+        if kk in prof and prof[kk][1]:
+            u = {"grains": g0, "vertices": 2 * g0, "boundaries": 3 * g0}[KERNEL_BYTES[kk][0]]
+            ach = NCU_FP64_INST_PER_UNIT[kk] * u / (prof[kk][0] / prof[kk][1] / 1e3)
+            fp64[kk] = {"achieved": ach, "frac": ach / fp64_peak}
+    step_bytes = algorithmic_bytes_per_step(1) * vsteps / K     # per step, at the window's sizes
+    ev_win = {"flips_per_step": sum(i.n_flips for i in infos) / K,
+              "removals_per_step": sum(i.n_removals for i in infos) / K,
+              "two_three_per_step": sum(i.n_two_three for i in infos) / K,
+              "conflicts_per_step": sum(i.n_conflicts for i in infos) / K,
+              "nucleation_attempts": sum(i.nucleation_attempted for i in infos),
+              "nucleations": sum(i.n_nucleations for i in infos)}
     step_info_bytes = 8 * 4 * 3  # counters read back per step
-
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded periodic Voronoi, lognormal stored energy)",
         "config": {"workload": "1M-grain stored-energy + nucleation vertex model", "grains": n,
-                   "vertices": 2 * n, "boundaries": 3 * n, "dt": 1e-4, "nucleation_gap": 10,
-                   "domain_bound": 1000.0, "GB_eps": 0.0, "se": "lognormal(-1,0.5)",
-                   "l2": "working set > L2 (129 MB): ~1 GB of mesh state per step",
-                   "removals_per_step": sum(i.n_removals for i in infos) / len(infos),
-                   "flips_per_step": sum(i.n_flips for i in infos) / len(infos),
-                   "nucleation_attempts": sum(i.nucleation_attempted for i in infos),
+                   "vertices": 2 * n, "boundaries": 3 * n, "dt": opt.dt, "nucleation_gap": opt.nucleation_gap,
+                   "domain_bound": opt.domain_bound, "GB_eps": 0.0, "se": "lognormal(-1,0.5)",
+                   "window": "K steps from %d steps past the 5/6 nucleation gate (step %d of the run, %d grains)"
+                             % (W, win_state[1], g0),
+                   "l2": "working set > L2 (129 MB): ~1.4 GB of mesh state per step", **ev_win,
                    "mesh_generation_s": round(gen_s, 1), "wall_s": round(wall, 3),
                    "launch_shapes": {"tpb_vertex": shapes[0], "tpb_boundary": shapes[1], "wide_sides": shapes[2],
                                      "grain_blocks_per_sm": shapes[3],
                                      "picked_by": "sevc_autotune, 3 steps per candidate"},
                    "launch_mode": "CUDA graphs"},
-        "e2e": {"value": e_vsteps / e_wall, "unit": UNIT, "h2d_bytes_per_step": host_bytes / args.steps,
-                "d2h_bytes_per_step": step_info_bytes + state_bytes / args.steps},
+        "e2e": {"value": vs / e_wall, "unit": UNIT, "h2d_bytes_per_step": host_bytes / k,
+                "d2h_bytes_per_step": step_info_bytes + state_bytes / k,
+                "run": "the configuration's whole run through the C ABI: sevc_create_from_arrays from host arrays, "
+                       "%d steps (stop: 10,000 steps or 20%% of the grains left) with every step's summary read "
+                       "back, sevc_get_state of the final mesh" % k,
+                "steps": k, "wall_s": round(e_wall, 3), "device_vertex_steps_per_s": vs / (ms_full / 1e3),
+                "gate_step": gate, "events": {"flips": int(ev_full[0]), "removals": int(ev_full[1]),
+                                              "two_three": int(ev_full[2]), "nucleation_attempts": int(ev_full[3]),
+                                              "nucleations": int(ev_full[4])}},
+        "t0_window": {"value": t0_vs / (t0_ms / 1e3), "unit": UNIT, "ms_per_step": t0_ms / K,
+                      "note": "steps %d..%d of the same run (before the gate: hardly any events)" % (W, W + K - 1)},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_PER_UNIT[dom] * units if dom in NCU_TRAFFIC_PER_UNIT else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on the 200K-grain mesh, "
                                        "scaled by units per launch",
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                     "step_frac": step_bytes / (ms / K / 1e3) / 1e9 / peak,
+                     "step_bytes": step_bytes,
                      "fp64_pipe_active_ncu": NCU_FP64_ACTIVE.get(dom),
-                     "note": "FP64-issue bound on GB300 (DRAM idle); fp64_pipe_active_ncu is the fraction "
-                             "of elapsed cycles the FP64 pipe was busy in the ncu capture"},
+                     "note": "FP64-issue bound on GB300 (DRAM idle); step_frac is the whole step's compulsory "
+                             "bytes (131.5 per vertex) over its time"},
         "roofline_fp64": {"bound": "fp64", "unit": "FP64 thread-instructions/s", "peak": fp64_peak,
                           "peak_source": "sevc_measure_fp64_rate (independent DFMA chains, this GPU, now)",
                           "kernels": fp64,
                           "inst_per_unit_source": "ncu DADD+DMUL+DFMA thread instructions per grain / vertex "
                                                   "on the 200K-grain mesh"},
-        "kernel_ms_share": {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
-        "step_bytes_rate_gbs": algorithmic_bytes_per_step(2 * n) * args.steps / (ms / 1e3) / 1e9,
+        "kernel_ms_share": {kk: round(v[0] / tot, 4) for kk, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "gpu_launches": sum(i.kernel_launches for i in infos),
-        "kernel_ms_per_step": {k: round(v[0] / v[1] if v[1] else 0, 4) for k, v in prof.items()},
+        "kernel_ms_per_step": {kk: round(v[0] / v[1] if v[1] else 0, 4) for kk, v in prof.items()},
         "clocks": ck,
     }
     if args.cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(mesh, n, args.cpu_steps)
+        line["cpu_baseline"] = cpu_baseline(win_state[0], n, args.cpu_steps, win_state[1], opt)
+    import shutil
+    shutil.rmtree(tmpdir, ignore_errors=True)
     if args.ensemble_sample > 0:
         line["ensemble"] = run_ensemble(args.ensemble_sample, args.ensemble_grains[0], args.ensemble_grains[1],
                                         10, 3, cache=args.ensemble_cache)
@@ -437,13 +526,15 @@ def run_engine(args):
     print(json.dumps(line))
 
 
-def cpu_baseline(mesh, n, steps):
+def cpu_baseline(state, n, steps, step_index, eopt):
+    """The oracle (the reference's step logic restated in C, OpenMP) on the
+    same window: built from the engine's state at the window's start."""
     from oracle import oracle as O
     O.build()
     opt = workload_options(O, n, steps)
     O.finish_options(opt)
     opt.min_grains = -1
-    orc = O.Oracle.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    orc = O.Oracle.from_state(opt, state, n=step_index, allow_nucleation=1)
     cores = os.cpu_count() or 1
     orc.set_threads(cores)
     vs, t0 = 0, time.time()
@@ -454,7 +545,8 @@ def cpu_baseline(mesh, n, steps):
         vs += 2 * g
     dt = time.time() - t0
     return {"value": vs / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d steps of the same 1M-grain workload (oracle restatement, OpenMP)" % steps}
+            "sample": "%d steps of the same window (the oracle built from the engine's state at its start, "
+                      "OpenMP on every host core)" % steps}
 
 
 def run_reference(args):

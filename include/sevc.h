@@ -93,6 +93,8 @@ typedef struct sevc_step_info {
                                   enabled grain's dA/dt was computed this step
                                   (always so on steps that can export) */
     int kernel_launches;       /* CUDA kernels the step launched             */
+    int n_conflicts;           /* boundaries marked conflictive, one device
+                                  printf each in src/topological.h:116      */
 } sevc_step_info;
 
 typedef struct sevc_handle sevc_handle;
@@ -151,6 +153,22 @@ sevc_status sevc_check_data_host(sevc_handle *h, int *n_bad);
  * device memory); indices outside their arrays count as violations. */
 sevc_status sevc_check_mesh(const sevc_mesh_host *mesh, int *n_bad);
 
+/* Digests of the mesh state, computed on the device without a download:
+ * out[f] = sum over the elements i of field f (in the layout that
+ * sevc_get_state returns) of mix(salt_f + i * 0x9E3779B97F4A7C15 + bits_i)
+ * mod 2^64, where bits_i is the element's IEEE-754 bit pattern (doubles),
+ * its value as an unsigned 32-bit integer (int32) or its byte (uint8), and
+ * mix is the splitmix64 finaliser.  Two states with equal digests are
+ * equal field by field with overwhelming probability, so a long run can be
+ * compared with a reference run every step at the cost of one small
+ * readback.  Fields f (SEVC_DIGEST_FIELDS of them, salt_f = f << 56): px, py,
+ * vx, vy, ven, vb, vg, bini, bend, benergy, blen, ben, bcand, glist (all
+ * 100 slots per grain), gvlen, garea, gori, gse, gen, gtype.  No
+ * counterpart in the reference (whose only check is check_data,
+ * src/utils.h:85-336). */
+#define SEVC_DIGEST_FIELDS 20
+sevc_status sevc_state_digest(sevc_handle *h, uint64_t *out);
+
 /* The whole program of src/main.cu:21-424 after option loading: create
  * DATA folder, load, loop with snapshots and the reference's log lines.
  * `log` (may be NULL) receives stdout-style lines. */
@@ -174,8 +192,13 @@ sevc_status sevc_rng_record(int nstreams, int ndraws, double *out);
  * (384 KiB per GPU, kept until exit); nstreams > 8192 is rejected with
  * SEVC_ERR_ARG.  The first call on each device resolves that array's
  * device address (with the device current); make that first call before
- * any stream capture.  All calls share the array: calls that overlap on
- * the GPU race and must be serialised by the caller. */
+ * any stream capture.  With CUDA's lazy module loading (the default) that
+ * first call is also when the 384 KiB are committed on the device (set
+ * CUDA_MODULE_LOADING=EAGER to commit them when the library is loaded);
+ * later calls take no device memory.  The address is kept for the life of
+ * the process: after cudaDeviceReset on a device, do not call this entry
+ * point on that device again.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 sevc_status sevc_rng_record_noalloc(int nstreams, int ndraws, double *d_out, void *stream);
 
 /* ---- batched ensembles (no counterpart in the reference) ----
@@ -268,6 +291,17 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
  * not complete is refused (SEVC_ERR_ARG).  on = 1 computes every value on
  * every step. */
 sevc_status sevc_set_exact_all(sevc_handle *h, int on);
+
+/* Limits of the step's bounded loops and work lists, for exercising the
+ * failure paths (0 keeps a value): polling_cap bounds the iterations of
+ * the polling loop (src/topological.h:555 has no bound; default 100000),
+ * past which sevc_step returns SEVC_ERR_NONCONVERGED; worklist_cap lowers
+ * the capacity of the grain-list fix-up work lists (default: every grain
+ * and every vertex, which cannot overflow), past which sevc_step returns
+ * SEVC_ERR_CAPACITY ("internal worklist overflow").  After a step that
+ * returned an error the mesh is in an undefined state: destroy the handle
+ * or load a checkpoint.  No counterpart in the reference. */
+sevc_status sevc_set_limits(sevc_handle *h, int polling_cap, int worklist_cap);
 
 /* The fixed launch sequences of a step (its first half, one polling
  * iteration, the second half of a step without 2x3 pairs) are captured

@@ -59,7 +59,7 @@ class _State(C.Structure):
         ("rng_kind", C.c_int), ("rng_seed", C.c_uint64), ("rng_nstreams", C.c_int), ("rng_ndraws", C.c_int),
         ("rng_table", C.c_void_p), ("rng_pos", C.c_void_p),
         ("ev_flips", C.c_int), ("ev_removals", C.c_int), ("ev_two_three", C.c_int), ("ev_nucleations", C.c_int),
-        ("status", C.c_int), ("nthreads_omp", C.c_int),
+        ("status", C.c_int), ("nthreads_omp", C.c_int), ("ev_conflicts", C.c_int),
     ]
 
 
@@ -94,6 +94,10 @@ def lib():
                   "orc_compute_vertex_energies", "orc_compute_vertex_velocities", "orc_compute_grain_dadts",
                   "orc_compute_t_ext"):
             getattr(L, f).argtypes = [P]
+        L.orc_alloc_blank.argtypes = [C.POINTER(Options), C.c_int, C.c_int, C.c_int]
+        L.orc_alloc_blank.restype = P
+        L.orc_state_digest.argtypes = [P, C.c_void_p]
+        L.orc_state_digest.restype = None
         L.orc_nucleated_fraction_area.argtypes = [P]
         L.orc_nucleated_fraction_area.restype = C.c_double
         _lib = L
@@ -152,6 +156,30 @@ class Oracle:
             raise RuntimeError("orc_load_arrays failed: %d" % rc)
         return cls(p)
 
+    @classmethod
+    def from_state(cls, opt, st, n=0, allow_nucleation=0, vrt_id_candidate=0):
+        """An oracle holding a mesh taken in the middle of a run: st is a
+        dict of arrays in the engine's sevc_get_state layout; the polling
+        buffer starts as the candidate flags, the random stream at its
+        beginning.  Used to time the reference's algorithm on a given
+        state; the run from here is the reference's step logic, but not
+        bit-identical to the run that produced st (its polling buffer and
+        random streams are not carried over)."""
+        nv, nb, ng = len(st["px"]), len(st["bini"]), len(st["gvlen"])
+        o = cls(lib().orc_alloc_blank(C.byref(opt), nv, nb, ng))
+        for f in ("px", "py", "vx", "vy", "venergy", "vel_bnd_x", "vel_grn_x", "vel_bnd_y", "vel_grn_y", "ven", "vb",
+                  "vg", "bini", "bend", "benergy", "blen", "btext", "ben", "bcand", "glist", "gvlen", "garea", "gdadt",
+                  "gori", "gse", "gen", "gtype"):
+            o.field(f)[:] = st[f]
+        o.field("cand_buf")[:] = st["bcand"] * st["ben"]
+        s = o.s
+        s.n = n
+        s.t = n * opt.dt
+        s.curr_n_grains = int(st["gen"].sum())
+        s.allow_nucleation = allow_nucleation
+        s.vrt_id_candidate = vrt_id_candidate
+        return o
+
     def __del__(self):
         if getattr(self, "_p", None) and _lib is not None:
             _lib.orc_free(self._p)
@@ -173,6 +201,12 @@ class Oracle:
             return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_int32)), shape=(n.value * 4,)).reshape(-1, 4)
         ct = {0: C.c_double, 1: C.c_int32, 2: C.c_uint8, 3: C.c_int64}[k.value]
         return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), shape=(n.value,))
+
+    def state_digest(self):
+        """Per-field digests (the definition of the engine's sevc_state_digest)."""
+        out = (C.c_uint64 * 20)()
+        lib().orc_state_digest(self._p, out)
+        return tuple(int(x) for x in out)
 
     def rng_synthetic(self, seed):
         lib().orc_rng_synthetic(self._p, seed)

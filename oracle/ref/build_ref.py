@@ -1,8 +1,9 @@
 #!/usr/bin/env python3
 """Build the reference's own sources for the CPU (test infrastructure only).
 
-Recipe: read the reference sources where they lie (default
-``/root/reference/src``), rewrite each CUDA launch ``k<<<g, b>>>(args)`` into
+Recipe: read the reference sources where they lie (``<checkout>/src``, the
+checkout being $SEVC_REFERENCE or a directory named ``reference`` next to
+this repository), rewrite each CUDA launch ``k<<<g, b>>>(args)`` into
 ``SEVC_LAUNCH(k, g, b, args)`` and the constant of ``src/main.cu:49``
 (``min_grains = 5000;``) into a call that reads SEVC_REF_MIN_GRAINS (default
 5000), write the rewritten files to a temporary directory, compile them with
@@ -25,7 +26,10 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
-DEFAULT_SRC = "/root/reference/src"
+# the reference checkout: $SEVC_REFERENCE, else a directory named "reference"
+# next to this repository
+DEFAULT_SRC = os.path.join(os.environ.get("SEVC_REFERENCE") or
+                           os.path.join(os.path.dirname(os.path.dirname(ORACLE)), "reference"), "src")
 
 
 def _comment_mask(text):

@@ -551,6 +551,26 @@ int orc_load_arrays(const orc_options *opt, int nv, const double *xy, int nb, co
     return load_core(opt, nv, xy, nb, ridges, ng, oris, ng, se, out);
 }
 
+/* A state of nv vertices, nb boundaries and ng grains with every entity
+ * in its initial (init_vertex / init_boundary / init_grain) condition and
+ * no connectivity, for the caller to fill field by field (orc_field) with
+ * a mesh taken in the middle of a run; curr_n_grains = ng. */
+orc_state *orc_alloc_blank(const orc_options *opt, int nv, int nb, int ng)
+{
+    orc_state *st = alloc_state(opt, nv, nb, ng);
+    v2 z = { 0.0, 0.0 };
+    for (int i = 0; i < nv; i++) init_vertex(st, i, z);
+    for (int b = 0; b < nb; b++) {
+        st->bini[b] = st->bend[b] = -1;
+        st->btext[b] = ORC_MAX_T_EXT;
+        st->ben[b] = 1;
+        st->bconf[b] = -1;
+    }
+    for (int g = 0; g < ng; g++) init_grain(st, g);
+    st->curr_n_grains = ng;
+    return st;
+}
+
 static int read_doubles(const char *path, int per_line, double **out, int *n)
 {
     FILE *f = fopen(path, "r");
@@ -840,6 +860,7 @@ static void check_conflictive_boundaries(orc_state *st)  /* topological.h:83 */
         if (bi >= 0 && be >= 0) {
             if (st->btext[bi] == st->btext[be]) st->bconf[b] = bi < be ? bi : be;
             else st->bconf[b] = st->btext[bi] < st->btext[be] ? bi : be;
+            st->ev_conflicts++;
         }
     }
 }
@@ -1342,7 +1363,7 @@ int orc_should_export(const orc_state *st)
 int orc_step(orc_state *st)
 {
     orc_options *o = &st->opt;
-    st->ev_flips = st->ev_removals = st->ev_two_three = st->ev_nucleations = 0;
+    st->ev_flips = st->ev_removals = st->ev_two_three = st->ev_nucleations = st->ev_conflicts = 0;
     st->n_two_three_iters = 0;
     orc_compute_boundary_arclengths(st);                  /* :124 */
     orc_compute_grain_areas(st);                          /* :127 */
@@ -1573,4 +1594,37 @@ orc_state *orc_clone(const orc_state *src)
         memcpy(d, s, (size_t)c1 * ksz[k1]);
     }
     return st;
+}
+
+/* Digests of the state in the definition of sevc_state_digest (the
+ * engine's include/sevc.h): per field, the sum mod 2^64 over its elements
+ * i of splitmix64_finaliser((f << 56) + i * 0x9E3779B97F4A7C15 + bits_i),
+ * bits_i = the double's bit pattern, the int32 as unsigned 32-bit, or the
+ * byte.  Lets the tests compare a run with the engine's every step. */
+static uint64_t dg_mix(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+void orc_state_digest(orc_state *st, uint64_t *out)
+{
+    static const char *names[20] = { "px", "py", "vx", "vy", "ven", "vb", "vg", "bini", "bend", "benergy", "blen",
+                                     "ben", "bcand", "glist", "gvlen", "garea", "gori", "gse", "gen", "gtype" };
+    for (int f = 0; f < 20; f++) {
+        int64_t n;
+        int kind;
+        void *p = orc_field(st, names[f], &n, &kind);
+        uint64_t salt = (uint64_t)f << 56, acc = 0;
+        int nt = st->nthreads_omp > 1 && n > 65536 ? st->nthreads_omp : 1;
+#pragma omp parallel for reduction(+ : acc) schedule(static) num_threads(nt)
+        for (int64_t i = 0; i < n; i++) {
+            uint64_t b;
+            if (kind == 0) memcpy(&b, (const double *)p + i, 8);
+            else if (kind == 1) b = (uint32_t)((const int32_t *)p)[i];
+            else b = ((const uint8_t *)p)[i];
+            acc += dg_mix(salt + (uint64_t)i * 0x9E3779B97F4A7C15ULL + b);
+        }
+        out[f] = acc;
+    }
 }

@@ -124,6 +124,8 @@ typedef struct orc_state {
     int ev_flips, ev_removals, ev_two_three, ev_nucleations;
     int status;                 /* sticky error */
     int nthreads_omp;           /* >1: OpenMP for race-free loops */
+    int ev_conflicts;           /* boundaries marked by check_conflictive_boundaries this step
+                                   (one device printf each, src/topological.h:116) */
 } orc_state;
 
 /* options.h:69-206 restated.  Returns ORC_OK or ORC_ERR_IO. */
@@ -177,7 +179,13 @@ void orc_compute_t_ext(orc_state *st);
 int  orc_current_n_grains(const orc_state *st);
 double orc_nucleated_fraction_area(const orc_state *st);
 
+/* a blank state of the given sizes, to be filled through orc_field */
+orc_state *orc_alloc_blank(const orc_options *opt, int nv, int nb, int ng);
+/* per-field digests of the state, as the engine's sevc_state_digest */
+void orc_state_digest(orc_state *st, uint64_t *out);
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif

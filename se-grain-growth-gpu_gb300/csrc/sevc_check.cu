@@ -130,6 +130,65 @@ __global__ void k_fp64_rate(int iters, double a, double b, double *sink)
     if (s == 12345.678) *sink = s;   /* keeps the chains live */
 }
 
+
+/* ---- state digests (sevc_state_digest) ---- */
+__device__ __forceinline__ unsigned long long digest_mix(unsigned long long z)   /* splitmix64 finaliser */
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ unsigned long long ubits(int v) { return (unsigned long long)(unsigned)v; }
+__device__ __forceinline__ unsigned long long ubits(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+/* elements of field f in the layout of sevc_get_state */
+__device__ long long digest_len(const DevMesh &m, int f)
+{
+    if (f < 5) return m.nv;
+    if (f < 7) return 3LL * m.nv;
+    if (f < 13) return m.nb;
+    if (f == 13) return (long long)SEVC_MAXV * m.ng;
+    return m.ng;
+}
+__device__ unsigned long long digest_bits(const DevMesh &m, int f, long long i)
+{
+    switch (f) {
+    case 0: return ubits(m.pos[i].x);
+    case 1: return ubits(m.pos[i].y);
+    case 2: return ubits(m.vel[i].x);
+    case 3: return ubits(m.vel[i].y);
+    case 4: return m.ven[i];
+    case 5: return ubits(slot3(m.vb[i / 3], (int)(i % 3)));
+    case 6: return ubits(slot3(m.vg[i / 3], (int)(i % 3)));
+    case 7: return ubits(m.bv[i].x);
+    case 8: return ubits(m.bv[i].y);
+    case 9: return ubits(m.benergy[i]);
+    case 10: return ubits(m.blen[i]);
+    case 11: return m.ben[i];
+    case 12: return m.bcand[i];
+    case 13: return ubits(m.glist[i]);
+    case 14: return ubits(m.gvlen[i]);
+    case 15: return ubits(m.garea[i]);
+    case 16: return ubits(m.gori[i]);
+    case 17: return ubits(m.gse[i]);
+    case 18: return m.gen[i];
+    default: return m.gtype[i];
+    }
+}
+/* blockIdx.y = field; the sum is order-independent, so the result does
+ * not depend on the launch shape */
+__global__ void k_digest(DevMesh m, unsigned long long *out)
+{
+    const int f = blockIdx.y;
+    const long long n = digest_len(m, f);
+    const unsigned long long salt = (unsigned long long)f << 56;
+    unsigned long long acc = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        acc += digest_mix(salt + (unsigned long long)i * 0x9E3779B97F4A7C15ULL + digest_bits(m, f, i));
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out + f, acc);
+}
+
 } // namespace
 
 /* FP64 multiply-add instructions (thread operations) per second on the
@@ -254,4 +313,13 @@ void launch_check(const DevMesh &m, int *out, cudaStream_t s)
     COUNT_LAUNCHES(1), k_check_boundaries<<<(m.nb + TPB - 1) / TPB, TPB, 0, s>>>(m, out);
     COUNT_LAUNCHES(1), k_check_vertices<<<(m.nv + TPB - 1) / TPB, TPB, 0, s>>>(m, out);
     COUNT_LAUNCHES(1), k_check_grains<<<(m.ng + TPB - 1) / TPB, TPB, 0, s>>>(m, out);
+}
+
+void launch_digest(const DevMesh &m, unsigned long long *out, cudaStream_t s)
+{
+    long long n = (long long)SEVC_MAXV * m.ng;
+    long long gx = (n + TPB - 1) / TPB;
+    if (gx > 4 * 152) gx = 4 * 152;
+    if (gx < 1) gx = 1;
+    COUNT_LAUNCHES(1), k_digest<<<dim3((unsigned)gx, SEVC_DIGEST_FIELDS), TPB, 0, s>>>(m, out);
 }

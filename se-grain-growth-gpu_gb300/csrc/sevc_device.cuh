@@ -61,9 +61,11 @@ struct DevMesh {
     int *glist, *gvlen;
     double *garea, *gdadt, *gori, *gse, *gq;
     uint8_t *gen, *gcand, *gfix, *gtype;
-    /* worklists of the grain-list fix-up (src/topological.h:1209) */
+    /* worklists of the grain-list fix-up (src/topological.h:1209); the
+     * capacities are the array sizes unless sevc_set_limits lowers them */
     int *fixlist, *nfix;
     int *modlist, *nmod;
+    int fixcap, modcap;
     int *err;            /* ERRB_* bits */
     int *evt;            /* event counters, EVT_COUNT per instance */
     /* Instances.  A batched handle holds several independent meshes one
@@ -104,7 +106,10 @@ struct DevMesh {
     int *lastblk;        /* arrival counters of last_block, zero between launches */
 };
 
-enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_COUNT = 4 };
+/* per-instance event counters of a step; EVT_CONFLICTS counts the
+ * boundaries check_conflictive_boundaries marks (src/topological.h:116
+ * prints one line for each) */
+enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, EVT_CONFLICTS = 4, EVT_COUNT = 5 };
 
 /* one position-moving event: a T1 flip (vertices a, b move to their
  * midpoint) or a 3-sided grain removal (a moves to the length-weighted

@@ -196,6 +196,9 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.vstamp, V * 4 },
         { (void **)&m.bstamp, B * 4 }, { (void **)&m.stamp, 4 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
         { (void **)&m.bmark, B }, { (void **)&m.lastblk, 8 * 4 },
+        { (void **)&x.digest, SEVC_DIGEST_FIELDS * 8 },
+        { (void **)&x.vown, V * 8 }, { (void **)&x.bown, B * 8 }, { (void **)&x.ehits, maxn * 4 },
+        { (void **)&x.n_ehits, 4 }, { (void **)&x.edefer, maxn }, { (void **)&x.ndefer, I * 4 },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -205,8 +208,14 @@ bool alloc_device(sevc_handle *h)
     h->dblock = base;
     h->dbytes = total;
     for (auto &q : r) { *q.p = base; base += align256(q.bytes); }
+    /* reservation keys start above every key an event writes */
+    if (!cuda_ok(cudaMemsetAsync(x.vown, 0xFF, V * 8, h->stream), "memset") ||
+        !cuda_ok(cudaMemsetAsync(x.bown, 0xFF, B * 8, h->stream), "memset"))
+        return false;
     m.nv = h->nv; m.nb = h->nb; m.ng = h->ng; m.D = h->opt.domain_bound;
     m.ninst = h->ninst;
+    m.fixcap = h->ng;
+    m.modcap = h->nv;
     return true;
 }
 
@@ -532,7 +541,7 @@ void enqueue_tail(sevc_handle *h, bool lists_unchanged)
     DevScratch &x = h->x;
     { Prof pr(h, "label_3sided"); launch_label_3sided(m, x, o.dt, lists_unchanged, s); }        /* :252-255 */
     { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
-    { Prof pr(h, "remove_grains"); launch_remove_grains(m, x.list_c, x.n_c, s); }                 /* :259 */
+    { Prof pr(h, "remove_grains"); launch_remove_grains(m, x, x.list_c, x.n_c, s); }              /* :259 */
     launch_clear_grain_cand(m, x.list_c, x.n_c, s);
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
     { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
@@ -851,6 +860,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         ii.n_removals = ev[EVT_REMOVALS];
         ii.n_flips = ev[EVT_FLIPS];
         ii.n_nucleations = ev[EVT_NUCLEATIONS];
+        ii.n_conflicts = ev[EVT_CONFLICTS];
         ii.nucleation_attempted = h->h_on[i];
         /* reported in the instance's own vertex indices */
         ii.nucleation_candidate = (h->h_on[i] && ctr[CTR_CANDIDATE] >= 0) ? ctr[CTR_CANDIDATE] - h->voff[i] : -1;
@@ -862,6 +872,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         loc.n_removals += ii.n_removals;
         loc.n_flips += ii.n_flips;
         loc.n_nucleations += ii.n_nucleations;
+        loc.n_conflicts += ii.n_conflicts;
     }
     h->curr_n_grains = total;
     h->nucleated_area = batch ? area_sum / I : area_sum;
@@ -1026,6 +1037,18 @@ sevc_status sevc_check_data(sevc_handle *h, int *n_bad)
     return SEVC_OK;
 }
 
+sevc_status sevc_state_digest(sevc_handle *h, uint64_t *out)
+{
+    if (!h || !out) return SEVC_ERR_ARG;
+    cudaStream_t s = h->stream;
+    if (!cuda_ok(cudaMemsetAsync(h->x.digest, 0, SEVC_DIGEST_FIELDS * 8, s), "memset")) return SEVC_ERR_CUDA;
+    launch_digest(h->m, h->x.digest, s);
+    if (!cuda_ok(cudaMemcpyAsync(out, h->x.digest, SEVC_DIGEST_FIELDS * 8, cudaMemcpyDeviceToHost, s), "readback") ||
+        !cuda_ok(cudaStreamSynchronize(s), "sync"))
+        return SEVC_ERR_CUDA;
+    return SEVC_OK;
+}
+
 sevc_status sevc_check_data_host(sevc_handle *h, int *n_bad)
 {
     if (!h || !n_bad) return SEVC_ERR_ARG;
@@ -1155,6 +1178,18 @@ sevc_status sevc_autotune(sevc_handle *h, int steps, int *chosen)
     if (st) return st;
     if (!ok) return SEVC_ERR_CUDA;
     if (chosen) { chosen[0] = sh.tpb_vertex; chosen[1] = sh.tpb_boundary; chosen[2] = sh.wide_sides; chosen[3] = sh.grain_occ; }
+    return SEVC_OK;
+}
+
+sevc_status sevc_set_limits(sevc_handle *h, int polling_cap, int worklist_cap)
+{
+    if (!h || polling_cap < 0 || worklist_cap < 0) return SEVC_ERR_ARG;
+    if (polling_cap > 0) h->polling_cap = polling_cap;
+    if (worklist_cap > 0) {
+        h->m.fixcap = worklist_cap < h->ng ? worklist_cap : h->ng;
+        h->m.modcap = worklist_cap < h->nv ? worklist_cap : h->nv;
+        drop_graphs(h);   /* captured launches carry the mesh view by value */
+    }
     return SEVC_OK;
 }
 

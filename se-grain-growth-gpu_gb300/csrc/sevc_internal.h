@@ -30,6 +30,14 @@ struct DevScratch {
     int *flags;                      /* 4 ints: the step's output decision, see launch_full_flag */
     int *summary;                    /* the step's summary packed for one readback */
     int *perm, *n_perm;              /* enabled grains ordered by side count */
+    unsigned long long *digest;      /* SEVC_DIGEST_FIELDS sums of sevc_state_digest */
+    /* events applied in parallel (removals, flips): reservation keys of
+     * every vertex and boundary, the events of the phase (list positions),
+     * the deferred ones (flag per list position, count per instance) */
+    unsigned long long *vown, *bown;
+    int *ehits, *n_ehits;
+    uint8_t *edefer;
+    int *ndefer;
 };
 constexpr int EXTRA_CAP = 1024;
 constexpr int TWO_THREE_PASSES = 20;  /* src/main.cu:227 */
@@ -108,7 +116,7 @@ void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *l
 /* bucket: no grain list changed since this step's side-count order, so
  * only its 3-sided bucket is visited */
 void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool bucket, cudaStream_t s);
-void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s);
+void launch_remove_grains(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s);
 /* clears the candidate flag of every listed grain (after the removals) */
 void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cudaStream_t s);
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s);
@@ -119,6 +127,8 @@ void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s);
 
 /* check_data on the device (sevc_check.cu): violations counted into *out */
 void launch_check(const DevMesh &m, int *out, cudaStream_t s);
+/* per-field digests of the state (sevc_state_digest) into out[SEVC_DIGEST_FIELDS] */
+void launch_digest(const DevMesh &m, unsigned long long *out, cudaStream_t s);
 
 /* nucleation (sevc_nucleation.cu) */
 void launch_rng_init(curandState *st, int n, cudaStream_t s);

@@ -73,15 +73,22 @@ __device__ void glist_replace(const DevMesh &m, int g, int oldv, int newv) /* :6
         if (L[i] == oldv) { L[i] = newv; return; }
 }
 
+/* Set flags[i] (a 0/1 byte) to 1; true for the one caller that changed
+ * it.  Events that run concurrently may queue the same grain. */
+__device__ __forceinline__ bool claim_byte(uint8_t *flags, int i)
+{
+    uintptr_t a = (uintptr_t)(flags + i);
+    unsigned bit = 1u << (8 * (unsigned)(a & 3));
+    return !(atomicOr((unsigned *)(a & ~(uintptr_t)3), bit) & bit);
+}
 /* queue a grain for the fix-up pass (grain.fix = true); its list is
  * about to change, so its dA/dt for this step is settled first */
 __device__ void mark_fix(const DevMesh &m, int g)
 {
     finalize_grain(m, g);
-    if (m.gfix[g]) return;
-    m.gfix[g] = 1;
+    if (!claim_byte(m.gfix, g)) return;
     int i = atomicAdd(m.nfix, 1);
-    if (i < m.ng) m.fixlist[i] = g; else raise_err(m, ERRB_WORKLIST);
+    if (i < m.fixcap) m.fixlist[i] = g; else raise_err(m, ERRB_WORKLIST);
 }
 /* write a deferred edit into vertex v's mod slot (mod_t, src/geometry.h:26);
  * prev < -1 keeps the slot's previous vrt_prev_id, as the reference does
@@ -95,7 +102,7 @@ __device__ void set_mod(const DevMesh &m, int v, int slot, int fix, int grn, int
     if (!m.vmodmark[v]) {
         m.vmodmark[v] = 1;
         int i = atomicAdd(m.nmod, 1);
-        if (i < m.nv) m.modlist[i] = v; else raise_err(m, ERRB_WORKLIST);
+        if (i < m.modcap) m.modlist[i] = v; else raise_err(m, ERRB_WORKLIST);
     }
 }
 
@@ -415,7 +422,9 @@ __device__ void conflict_check_one(const DevMesh &m, int b)
         int w;
         if (ti == te) w = bi < be ? bi : be;
         else w = ti < te ? bi : be;
-        m.bconf[b] = w;
+        /* b is reached from each candidate next to it and every visit writes
+         * the same w; the first writer (bconf was -1) counts the mark */
+        if (atomicExch(&m.bconf[b], w) == -1) atomicAdd(&m.evt[EVT_COUNT * m.binst[b] + EVT_CONFLICTS], 1);
     }
 }
 /* check_conflictive_boundaries for every non-candidate boundary adjacent
@@ -733,31 +742,126 @@ __device__ void remove_grain_dev(const DevMesh &m, int grn)
     m.vg[A] = ga;
 }
 
-/* remove_grains (:994), launched <<<1,1>>> by the reference: grains in
- * ascending index order */
-/* one warp per instance: a removal disables only its own grain, so the
- * listed grains that will be removed are known up front; lane 0 applies
- * them in list order */
-__global__ void k_remove_grains(DevMesh m, const int *list, const int *n)
+/* ------------------------------------------------------------------ */
+/* Events in parallel with the serial order's result                    */
+/* ------------------------------------------------------------------ */
+/* The reference applies the 3-sided removals one at a time in ascending
+ * grain order (remove_grains <<<1,1>>>, :994) and defines no order for the
+ * flips; here both phases follow ascending list order.  An event reads and
+ * writes only its footprint (its vertices and the boundaries in their
+ * slots) plus grain-level records that commute: queueing a grain for the
+ * fix-up (an atomic claim of its flag), its mod slots (per vertex) and the
+ * dA/dt settled from the step's starting values (settled before any event
+ * of the phase runs).  Two events with disjoint footprints therefore
+ * commute, and the serial result is obtained by deterministic reservation:
+ *   reserve  every event writes its key into each footprint record
+ *            (atomicMin); the key orders events by list position;
+ *   apply    an event that holds every one of its records shares none
+ *            with an earlier event: it runs at once, all such in parallel;
+ *            any other is deferred;
+ *   deferred the deferred events run one at a time in list order, after
+ *            the parallel ones; each shares records only with earlier
+ *            events, which have all run (in parallel or before it here),
+ *            and commutes with every later parallel one.
+ * Keys carry a per-phase epoch in their high half that grows every step,
+ * so records never need clearing: an earlier step's key is larger and is
+ * replaced by the first reservation of a later step. */
+__device__ __forceinline__ unsigned long long resv_key(unsigned epoch, int pos)
+{
+    return ((unsigned long long)(0xFFFFFFFFu - epoch) << 32) | (unsigned)pos;
+}
+__device__ __forceinline__ bool valid_v(const DevMesh &m, int v) { return (unsigned)v < (unsigned)m.nv; }
+__device__ __forceinline__ bool valid_b(const DevMesh &m, int b) { return (unsigned)b < (unsigned)m.nb; }
+__device__ __forceinline__ bool valid_g(const DevMesh &m, int g) { return (unsigned)g < (unsigned)m.ng; }
+
+/* reserve vertex v and the boundaries in its slots; settle the dA/dt of
+ * its grains */
+__device__ void reserve_vertex(const DevMesh &m, const DevScratch &x, int v, unsigned long long key)
+{
+    atomicMin(x.vown + v, key);
+    int4 s = m.vb[v], g = m.vg[v];
+    for (int j = 0; j < 3; j++) {
+        int b = slot3(s, j);
+        if (valid_b(m, b)) atomicMin(x.bown + b, key);
+        int h = slot3(g, j);
+        if (valid_g(m, h)) finalize_grain(m, h);
+    }
+}
+/* whether v and every boundary in its slots hold key; nothing but the
+ * event holding v writes its slots, so they are the reserved ones */
+__device__ bool holds_vertex(const DevMesh &m, const DevScratch &x, int v, unsigned long long key)
+{
+    if (x.vown[v] != key) return false;
+    int4 s = m.vb[v];
+    for (int j = 0; j < 3; j++) {
+        int b = slot3(s, j);
+        if (!valid_b(m, b) || x.bown[b] != key) return false;
+    }
+    return true;
+}
+
+/* 3-sided removals (remove_grains, :994): a listed grain that is enabled
+ * and a candidate is removed; a removal disables only its own grain, so
+ * the set is known up front */
+__global__ void k_remove_reserve(DevMesh m, DevScratch x, const int *list, const int *n)
+{
+    griddep_wait();
+    const unsigned ep = 2u * *m.stamp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int g = list[i];
+        if (!(m.gen[g] && m.gcand[g])) continue;
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        unsigned long long key = resv_key(ep, i);
+        for (int k = 0; k < 3; k++)
+            if (valid_v(m, L[k])) reserve_vertex(m, x, L[k], key);
+        int p = atomicAdd(x.n_ehits, 1);
+        x.ehits[p] = i;
+    }
+}
+__global__ void k_remove_apply(DevMesh m, DevScratch x, const int *list)
+{
+    griddep_wait();
+    const unsigned ep = 2u * *m.stamp;
+    const int nh = *x.n_ehits;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nh; t += gridDim.x * blockDim.x) {
+        int i = x.ehits[t], g = list[i];
+        const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        unsigned long long key = resv_key(ep, i);
+        bool own = true;
+        for (int k = 0; k < 3 && own; k++) own = valid_v(m, L[k]) && holds_vertex(m, x, L[k], key);
+        if (own) {
+            remove_grain_dev(m, g);
+            atomicAdd(&m.evt[EVT_COUNT * m.ginst[g] + EVT_REMOVALS], 1);
+        } else {
+            x.edefer[i] = 1;
+            atomicAdd(&x.ndefer[m.ginst[g]], 1);
+        }
+    }
+}
+/* one warp per instance: its deferred removals in list order */
+__global__ void k_remove_deferred(DevMesh m, DevScratch x, const int *list, const int *n)
 {
     griddep_wait();
     int inst = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (inst >= m.ninst) return;
+    if (inst == 0 && lane == 0) *x.n_ehits = 0;
+    if (inst >= m.ninst || x.ndefer[inst] == 0) return;
     int lo = lower_bound_i(list, *n, m.goff[inst]);
     int hi = lower_bound_i(list, *n, m.goff[inst + 1]);
     for (int base = lo; base < hi; base += 32) {
         int i = base + lane;
-        bool f = i < hi && m.gen[list[i]] && m.gcand[list[i]];
+        bool f = i < hi && x.edefer[i];
         unsigned hits = __ballot_sync(0xffffffffu, f);
         if (lane == 0)
             while (hits) {
                 int j = __ffs(hits) - 1;
                 hits &= hits - 1;
+                x.edefer[base + j] = 0;
                 remove_grain_dev(m, list[base + j]);
                 m.evt[EVT_COUNT * inst + EVT_REMOVALS]++;
             }
         __syncwarp();
     }
+    if (lane == 0) x.ndefer[inst] = 0;
 }
 
 /* unlabel_boundaries_st2 (:588-606) */
@@ -933,8 +1037,8 @@ __device__ bool flip_plan(const DevMesh &m, int bnd, int lane, FlipPlan &P)
  * the same values, but every record the flip reads is loaded up front in
  * one round trip instead of behind the writes that precede it, and the
  * work-list appends of the mod slots and of the fix-up grains take one
- * atomic each (the appended entries and their order are the ones the
- * one-at-a-time appends give). */
+ * atomic each (the fix-up pass edits each queued grain on its own, so the
+ * order of the entries does not matter). */
 __device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPlan &P)
 {
     const int A = P.A, B = P.B, AC = P.AC, BE = P.BE;
@@ -944,9 +1048,6 @@ __device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPl
     int2 eAC = m.bv[AC], eBE = m.bv[BE];
     int4 mA0 = m.vmod[4 * (size_t)A], mB0 = m.vmod[4 * (size_t)B];
     uint8_t mkA = m.vmodmark[A], mkB = m.vmodmark[B];
-    uint8_t fx[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) fx[k] = m.gfix[G[k]];
     double2 pa = m.pos[A], pb = m.pos[B], va = m.vel[A], vb = m.vel[B];
     log_event(m, EV_FLIP, A, B, -1, pa, pb, pb);
     /* boundary slots, then vertex_invert_boundary_order */
@@ -975,22 +1076,21 @@ __device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPl
         int i0 = atomicAdd(m.nmod, nm);
         if (!mkA) {
             m.vmodmark[A] = 1;
-            if (i0 < m.nv) m.modlist[i0] = A; else raise_err(m, ERRB_WORKLIST);
+            if (i0 < m.modcap) m.modlist[i0] = A; else raise_err(m, ERRB_WORKLIST);
             i0++;
         }
         if (!mkB) {
             m.vmodmark[B] = 1;
-            if (i0 < m.nv) m.modlist[i0] = B; else raise_err(m, ERRB_WORKLIST);
+            if (i0 < m.modcap) m.modlist[i0] = B; else raise_err(m, ERRB_WORKLIST);
         }
     }
-    /* mark_fix of the four grains (their dA/dt is settled) */
+    /* mark_fix of the four grains (their dA/dt is settled); flips running
+     * at the same time may queue the same grain, the claim decides */
     bool nf[4];
     int nfix = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        bool dup = false;
-        for (int q = 0; q < k; q++) dup |= G[q] == G[k];
-        nf[k] = !fx[k] && !dup;
+        nf[k] = claim_byte(m.gfix, G[k]);
         nfix += nf[k];
     }
     if (nfix) {
@@ -998,8 +1098,7 @@ __device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPl
 #pragma unroll
         for (int k = 0; k < 4; k++)
             if (nf[k]) {
-                m.gfix[G[k]] = 1;
-                if (i0 < m.ng) m.fixlist[i0] = G[k]; else raise_err(m, ERRB_WORKLIST);
+                if (i0 < m.fixcap) m.fixlist[i0] = G[k]; else raise_err(m, ERRB_WORKLIST);
                 i0++;
             }
     }
@@ -1030,19 +1129,73 @@ __device__ void flip_planned(const DevMesh &m, int bnd, double eps, const FlipPl
     m.vel[B] = make_double2(0, 0);
 }
 
-/* apply_flippings (:1016-1026); flips that share no vertex commute, the
- * rest are applied in ascending boundary order */
-/* One block per instance.  A flip changes no boundary's enabled or
- * candidate flag, so which listed boundaries flip is known up front: the
- * block tests FLIP_TPB entries at a time (the list is long and hits are
- * few, so the scan's dependent loads are the cost) and warp 0 applies the
- * hits in list order, its lanes prefetching each flip's records. */
+/* apply_flippings (:1016-1026): the reference flips every remaining
+ * candidate in parallel, with unsynchronised writes when two share
+ * records; here flips follow ascending list (boundary) order, which is
+ * every race-free outcome.  A flip changes no boundary's enabled or
+ * candidate flag, so the flips are known up front.  Reservation, parallel
+ * application and the deferred pass as for the removals (epoch 2 * stamp
+ * + 1); the footprint is both ends with their slots. */
+__global__ void k_flip_reserve(DevMesh m, DevScratch x, const int *list, const int *n)
+{
+    griddep_wait();
+    const unsigned ep = 2u * *m.stamp + 1u;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+        int b = list[i];
+        if (!(m.ben[b] && m.bcand[b])) continue;
+        int2 e = m.bv[b];
+        unsigned long long key = resv_key(ep, i);
+        if (valid_v(m, e.x)) reserve_vertex(m, x, e.x, key);
+        if (valid_v(m, e.y)) reserve_vertex(m, x, e.y, key);
+        int p = atomicAdd(x.n_ehits, 1);
+        x.ehits[p] = i;
+    }
+}
+/* one warp per flip: lanes prefetch its neighbourhood and derive the
+ * plan, lane 0 applies it */
+__global__ void k_flip_apply(DevMesh m, DevScratch x, double eps, const int *list)
+{
+    griddep_wait();
+    const unsigned ep = 2u * *m.stamp + 1u;
+    const int nh = *x.n_ehits;
+    const int lane = threadIdx.x & 31, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nh; t += nw) {
+        int i = x.ehits[t], b = list[i];
+        int2 e = m.bv[b];
+        unsigned long long key = resv_key(ep, i);
+        bool own = false;
+        if (lane == 0)
+            own = valid_v(m, e.x) && valid_v(m, e.y) && holds_vertex(m, x, e.x, key) && holds_vertex(m, x, e.y, key);
+        own = __shfl_sync(0xffffffffu, own, 0);
+        if (own) {
+            prefetch_flip(m, b, lane);
+            FlipPlan P;
+            bool planned = flip_plan(m, b, lane, P) && P.AC != P.BE;
+            __syncwarp();
+            if (lane == 0) {
+                if (planned) flip_planned(m, b, eps, P);
+                else flip_dev(m, b, eps);
+                atomicAdd(&m.evt[EVT_COUNT * m.binst[b] + EVT_FLIPS], 1);
+            }
+        } else if (lane == 0) {
+            x.edefer[i] = 1;
+            atomicAdd(&x.ndefer[m.binst[b]], 1);
+        }
+        __syncwarp();
+    }
+}
+/* One block per instance: its deferred flips in list order.  The block
+ * tests FLIP_TPB entries at a time and warp 0 applies the deferred ones,
+ * its lanes prefetching each flip's records. */
 constexpr int FLIP_TPB = 512;
-__global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const int *list, const int *n)
+__global__ void __launch_bounds__(FLIP_TPB) k_flip_deferred(DevMesh m, DevScratch x, double eps, const int *list,
+                                                            const int *n)
 {
     griddep_wait();
     __shared__ unsigned hitmask[FLIP_TPB / 32];
     int inst = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (inst == 0 && threadIdx.x == 0) *x.n_ehits = 0;
+    if (x.ndefer[inst] == 0) return;
     int lo = 0, hi = *n;
     if (m.ninst > 1) {
         lo = lower_bound_i(list, hi, m.boff[inst]);
@@ -1050,12 +1203,7 @@ __global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const
     }
     for (int base = lo; base < hi; base += FLIP_TPB) {
         int i = base + (int)threadIdx.x;
-        bool f = false;
-        if (i < hi) {
-            int b = list[i];
-            uint8_t en = m.ben[b], ca = m.bcand[b];   /* both loads in flight together */
-            f = en && ca;
-        }
+        bool f = i < hi && x.edefer[i];
         unsigned w = __ballot_sync(0xffffffffu, f);
         if (lane == 0) hitmask[warp] = w;
         if (!__syncthreads_or(f)) continue;           /* the barrier also publishes hitmask */
@@ -1071,6 +1219,7 @@ __global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const
                     bool planned = flip_plan(m, b, lane, P) && P.AC != P.BE;
                     __syncwarp();
                     if (lane == 0) {
+                        x.edefer[base + 32 * k + j] = 0;
                         if (planned) flip_planned(m, b, eps, P);
                         else flip_dev(m, b, eps);
                         m.evt[EVT_COUNT * inst + EVT_FLIPS]++;
@@ -1081,6 +1230,7 @@ __global__ void __launch_bounds__(FLIP_TPB) k_flips(DevMesh m, double eps, const
         }
         __syncthreads();
     }
+    if (threadIdx.x == 0) x.ndefer[inst] = 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1122,7 +1272,7 @@ __device__ void fix_grain(const DevMesh &m, int g)
 __global__ void k_fix_edit(DevMesh m)
 {
     griddep_wait();
-    int nf = *m.nfix;
+    int nf = min(*m.nfix, m.fixcap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
         int g = m.fixlist[w];
         if (m.gen[g] && m.gfix[g]) fix_grain(m, g);
@@ -1134,7 +1284,7 @@ __global__ void k_fix_edit(DevMesh m)
 __global__ void k_fix_clear(DevMesh m)
 {
     griddep_wait();
-    int nf = *m.nfix, nm = *m.nmod;
+    int nf = min(*m.nfix, m.fixcap), nm = min(*m.nmod, m.modcap);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
         int g = m.fixlist[w];
         if (m.gen[g]) {
@@ -1267,9 +1417,12 @@ void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cu
     launch_dep(k_clear_grain_cand, 32, TPB, s, m, list, n);
 }
 
-void launch_remove_grains(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
+void launch_remove_grains(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s)
 {
-    launch_dep(k_remove_grains, m.ninst, 32, s, m, list, n);
+    int g = listgrid(m.ng);
+    launch_dep(k_remove_reserve, g, TPB, s, m, x, list, n);
+    launch_dep(k_remove_apply, g, TPB, s, m, x, list);
+    launch_dep(k_remove_deferred, (m.ninst + 3) / 4, 128, s, m, x, list, n);
 }
 
 void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
@@ -1280,8 +1433,10 @@ void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cud
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s)
 {
-    (void)x;
-    launch_dep(k_flips, m.ninst, FLIP_TPB, s, m, eps, cand, ncand);
+    int g = listgrid(m.nb);
+    launch_dep(k_flip_reserve, g, TPB, s, m, x, cand, ncand);
+    launch_dep(k_flip_apply, 4 * WL_BLOCKS, TPB, s, m, x, eps, cand);
+    launch_dep(k_flip_deferred, m.ninst, FLIP_TPB, s, m, x, eps, cand, ncand);
 }
 
 void launch_fix_lists(const DevMesh &m, cudaStream_t s)

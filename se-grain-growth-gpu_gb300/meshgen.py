@@ -23,11 +23,13 @@ import numpy as np
 RES = 2 ** 32
 
 
-def periodic_voronoi(n, rng, max_attempts=20):
+def periodic_voronoi(n, rng, max_attempts=20, points=None):
+    """points: the n seeds (in [0, 1)^2) instead of uniform draws; a mesh
+    that is not made of triple junctions then raises instead of redrawing."""
     from scipy.spatial import Voronoi
 
-    for _ in range(max_attempts):
-        pts = rng.random((n, 2))
+    for _ in range(1 if points is not None else max_attempts):
+        pts = rng.random((n, 2)) if points is None else np.asarray(points, np.float64)
         margin = min(0.5, 8.0 / np.sqrt(n))
         imgs = [pts]
         for dx in (-1.0, 0.0, 1.0):

@@ -78,7 +78,7 @@ class StepInfo(C.Structure):
         ("n_two_three_iters", C.c_int), ("two_three_counts", C.c_int * 20), ("n_flips", C.c_int),
         ("n_removals", C.c_int), ("n_two_three", C.c_int), ("n_nucleations", C.c_int),
         ("nucleation_attempted", C.c_int), ("nucleation_candidate", C.c_int), ("gpu_ms", C.c_double),
-        ("outputs_complete", C.c_int), ("kernel_launches", C.c_int),
+        ("outputs_complete", C.c_int), ("kernel_launches", C.c_int), ("n_conflicts", C.c_int),
     ]
 
     def as_dict(self):
@@ -236,6 +236,11 @@ def rng_record_noalloc(nstreams, ndraws, d_out, stream=None):
     _check(L.sevc_rng_record_noalloc(nstreams, ndraws, C.c_void_p(d_out), C.c_void_p(stream)))
 
 
+# fields of sevc_state_digest, in order (include/sevc.h)
+DIGEST_FIELDS = ("px", "py", "vx", "vy", "ven", "vb", "vg", "bini", "bend", "benergy", "blen", "ben", "bcand",
+                 "glist", "gvlen", "garea", "gori", "gse", "gen", "gtype")
+
+
 class Engine:
     """One simulation on the GPU (an sevc_handle)."""
 
@@ -369,6 +374,14 @@ class Engine:
         _check(lib().sevc_get_state(self._h, C.byref(mh)))
         return arrs
 
+    def state_digest(self):
+        """Per-field digests of the state computed on the device
+        (sevc_state_digest), as a tuple of DIGEST_FIELDS Python ints."""
+        out = (C.c_uint64 * len(DIGEST_FIELDS))()
+        lib().sevc_state_digest.argtypes = [C.c_void_p, C.c_void_p]
+        _check(lib().sevc_state_digest(self._h, out))
+        return tuple(int(x) for x in out)
+
     # ---- checkpoint files, statistics ----
     def checkpoint_save(self, path):
         lib().sevc_checkpoint_save.argtypes = [C.c_void_p, C.c_char_p]
@@ -424,6 +437,10 @@ class Engine:
         _check(lib().sevc_adjoint_histogram(self._h, nbins, float(amax), d.ctypes.data, gse.ctypes.data,
                                             C.byref(ggb), C.byref(gmu)))
         return gse, ggb.value, gmu.value
+
+    def set_limits(self, polling_cap=0, worklist_cap=0):
+        lib().sevc_set_limits.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        _check(lib().sevc_set_limits(self._h, polling_cap, worklist_cap))
 
     def set_exact_all(self, on):
         lib().sevc_set_exact_all.argtypes = [C.c_void_p, C.c_int]

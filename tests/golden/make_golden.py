@@ -1,15 +1,23 @@
 #!/usr/bin/env python3
-"""Regenerate the golden fixtures (run in a container that has the reference).
+"""Regenerate the golden fixtures (run where a checkout of the reference is).
 
-1. Meshes: the reference's own generator, /root/reference/voronoi/voronoi.py,
-   run with fixed seeds (m300: N=300 seed 11, m1000: N=1000 seed 12), with
-   both its uniform and triangular stored-energy files.
+    python tests/golden/make_golden.py [--reference DIR] [--only NAME ...]
+
+DIR is the reference checkout (default: $SEVC_REFERENCE, else a directory
+named "reference" next to this repository).
+
+1. Meshes: the reference's own generator, voronoi/voronoi.py, run with
+   fixed seeds (m300: N=300 seed 11, m1000: N=1000 seed 12, m2000: N=2000
+   seed 1), with both its uniform and triangular stored-energy files; and
+   ref2k, a copy of the reference's shipped 2,000-grain input
+   (voronoi/2K/{vertices,ridges,oris}.txt, SE/uniform.txt, SE/triangular.txt).
 2. Runs: each configuration of configs.py executed by the reference's own
    sources built for the CPU (oracle/_ref/sevc_ref, see oracle/ref), with the
    synthetic random stream seeded as listed.  For every snapshot the full and
    integer-only digests are stored, plus the per-step numbers of the
    reference's log (2x3 counts, grain count, nucleated area, nucleation
-   site).
+   site); for the long runs (configs.LONG_CONFIGS) the same for their first
+   configs.FIRST_STEPS steps.
 
 Output: tests/golden/meshes/*, tests/golden/golden.json.
 """
@@ -29,12 +37,27 @@ sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
 import configs  # noqa: E402
 import snapshot  # noqa: E402
 
-REF = "/root/reference"
-MESHES = {"m300": (300, 11), "m1000": (1000, 12)}
+MESHES = {"m300": (300, 11), "m1000": (1000, 12), "m2000": (2000, 1)}
+REF_MESHES = {"ref2k": "2K"}   # copies of the reference's shipped inputs (voronoi/<dir>)
 
 
-def make_meshes():
-    gen = os.path.join(REF, "voronoi", "voronoi.py")
+def reference_dir(arg=None):
+    return arg or os.environ.get("SEVC_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
+def copy_reference_meshes(ref):
+    for name, sub in REF_MESHES.items():
+        src, d = os.path.join(ref, "voronoi", sub), os.path.join(configs.MESH_DIR, name)
+        os.makedirs(d, exist_ok=True)
+        for a, b in (("vertices.txt", "vertices.txt"), ("ridges.txt", "ridges.txt"), ("oris.txt", "oris.txt"),
+                     (os.path.join("SE", "uniform.txt"), "se_uniform.txt"),
+                     (os.path.join("SE", "triangular.txt"), "se_triangular.txt")):
+            shutil.copyfile(os.path.join(src, a), os.path.join(d, b))
+
+
+def make_meshes(ref):
+    copy_reference_meshes(ref)
+    gen = os.path.join(ref, "voronoi", "voronoi.py")
     for name, (n, seed) in MESHES.items():
         d = os.path.join(configs.MESH_DIR, name)
         os.makedirs(d, exist_ok=True)
@@ -76,34 +99,47 @@ def parse_log(text):
 
 
 def run_config(name, exe):
-    _, _, _, seed, min_grains = configs.CONFIGS[name]
+    _, _, _, seed, min_grains = configs.ALL_CONFIGS[name]
     tmp = tempfile.mkdtemp(prefix="golden_")
     try:
         folder = os.path.join(tmp, "out")
-        ini = configs.write_ini(os.path.join(tmp, "run.ini"), name, folder)
+        nmax = configs.golden_nmax(name)
+        ini = configs.write_ini(os.path.join(tmp, "run.ini"), name, folder, nmax=nmax)
         env = dict(os.environ, SEVC_REF_MIN_GRAINS=str(min_grains), SEVC_REF_RNG_SEED=str(seed))
         r = subprocess.run([exe, "-c", ini], capture_output=True, text=True, env=env, check=True)
         data = os.path.join(folder, "DATA")
         snaps = [list(snapshot.digests(os.path.join(data, f))) for f in sorted(os.listdir(data))]
-        return {"snapshots": snaps, "steps": parse_log(r.stdout), "rng_seed": seed, "min_grains": min_grains}
+        return {"snapshots": snaps, "steps": parse_log(r.stdout), "rng_seed": seed, "min_grains": min_grains,
+                "nmax": nmax}
     finally:
         shutil.rmtree(tmp)
 
 
 def main():
+    import argparse
     import build_ref
-    exe = build_ref.build(verbose=True)
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help="reference checkout (default $SEVC_REFERENCE or ../reference)")
+    ap.add_argument("--only", nargs="*", default=None, help="regenerate these configurations only (meshes are kept)")
+    args = ap.parse_args()
+    ref = reference_dir(args.reference)
+    exe = build_ref.build(os.path.join(ref, "src"), verbose=True)
     if exe is None:
-        raise SystemExit("the reference sources are needed to regenerate the fixtures")
-    make_meshes()
+        raise SystemExit("the reference sources are needed to regenerate the fixtures (%s)" % ref)
+    path = os.path.join(HERE, "golden.json")
     out = {}
-    for name in configs.CONFIGS:
+    if args.only:
+        out = json.load(open(path))
+    else:
+        make_meshes(ref)
+    for name in (args.only or configs.ALL_CONFIGS):
         out[name] = run_config(name, exe)
-        s = out[name]["steps"]
-        print("%-14s %4d steps, %3d snapshots, grains %d -> %s, nucleations %d" % (
-            name, len(s), len(out[name]["snapshots"]), s[0]["n_grains"], s[-1]["n_grains"],
-            sum(1 for x in s if x["nucleated_at"] >= 0)))
-    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        g = out[name]
+        s = g["steps"]
+        print("%-14s %4d steps, %3d snapshots, grains %d -> %s, nucleations %d, 2x3 steps %d" % (
+            name, len(s), len(g["snapshots"]), s[0]["n_grains"], s[-1]["n_grains"],
+            sum(1 for x in s if x["nucleated_at"] >= 0), sum(1 for x in s if any(x["two_three"]))), flush=True)
+    with open(path, "w") as f:
         json.dump(out, f, indent=0)
 
 

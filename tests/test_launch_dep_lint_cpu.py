@@ -54,13 +54,23 @@ def _kernel_bodies(text):
 
 
 def test_kernels_with_last_block_never_return_early():
-    """last_block counts the blocks that reach it: a thread that returns
-    before it would leave the count short and the list counts it resets
-    would never be reset."""
+    """last_block counts the blocks that reach it and holds a block
+    barrier: every thread must call it.  So a kernel that uses it returns
+    nowhere early, and the call sits at the top level of the kernel body
+    (no enclosing block that could depend on the thread) as the first
+    operand of its expression (no short-circuit operator or conditional
+    before it that some threads could stop at)."""
     found = 0
     for f, text in _sources().items():
         for name, body in _kernel_bodies(text):
-            if "last_block(" in body:
+            if "last_block(" not in body:
+                continue
+            assert not re.search(r"\breturn\b", body), name
+            for mo in re.finditer(r"last_block\(", body):
                 found += 1
-                assert not re.search(r"\breturn\b", body), name
+                head = body[:mo.start()]
+                depth = head.count("{") - head.count("}")
+                assert depth == 0, "%s: last_block inside a nested block" % name
+                stmt = re.split(r"[;{}]", head)[-1]
+                assert not re.search(r"&&|\|\||\?", stmt), "%s: last_block after a short-circuit operand" % name
     assert found >= 2

@@ -3,8 +3,10 @@
 tests/golden/golden.json holds, for each configuration in
 tests/golden/configs.py, the digests of every snapshot and the per-step log
 numbers that the reference's own sources produced (built for the CPU by
-oracle/ref, run by tests/golden/make_golden.py).  The oracle must reproduce
-them: integer state (topology, flags, candidates, lists) bit for bit
+oracle/ref, run by tests/golden/make_golden.py); for the long runs
+(configs.LONG_CONFIGS, among them the reference's shipped input with its
+example.ini) those of the first configs.FIRST_STEPS steps.  The oracle must
+reproduce them: integer state (topology, flags, candidates, lists) bit for bit
 everywhere, and the full snapshot text byte for byte on x86-64, where the
 fixtures were made (libm's last bit can differ on other CPUs).
 """
@@ -21,8 +23,9 @@ GOLDEN = json.load(open(os.path.join(configs.HERE, "golden.json")))
 
 
 def run_oracle(O, name, tmp):
-    _, _, _, seed, mg = configs.CONFIGS[name]
-    ini = configs.write_ini(os.path.join(tmp, "run.ini"), name, os.path.join(tmp, "unused"))
+    _, _, _, seed, mg = configs.ALL_CONFIGS[name]
+    nmax = configs.golden_nmax(name)
+    ini = configs.write_ini(os.path.join(tmp, "run.ini"), name, os.path.join(tmp, "unused"), nmax=nmax)
     opt = O.parse_ini(ini)
     opt.min_grains = mg
     o = O.Oracle.from_files(opt)
@@ -41,7 +44,7 @@ def run_oracle(O, name, tmp):
     return log, [snapshot.digests(os.path.join(snaps, f)) for f in sorted(os.listdir(snaps))]
 
 
-@pytest.mark.parametrize("name", sorted(configs.CONFIGS))
+@pytest.mark.parametrize("name", sorted(configs.ALL_CONFIGS))
 def test_oracle_reproduces_reference(oracle_mod, name, tmp_path):
     log, snaps = run_oracle(oracle_mod, name, str(tmp_path))
     g = GOLDEN[name]
@@ -58,7 +61,8 @@ def test_oracle_reproduces_reference(oracle_mod, name, tmp_path):
 
 def test_golden_covers_every_event_kind():
     steps = [s for g in GOLDEN.values() for s in g["steps"]]
+    assert any(any(s["two_three"]) for s in GOLDEN["example_ref2k"]["steps"] + GOLDEN["events_m1000"]["steps"])
     assert any(any(s["two_three"]) for s in steps), "no 2x3 removal in the fixtures"
     assert sum(s["nucleated_at"] >= 0 for s in steps) >= 10
-    removed = [g["steps"][0]["n_grains"] - g["steps"][-1]["n_grains"] for g in GOLDEN.values()]
+    removed = [GOLDEN[k]["steps"][0]["n_grains"] - GOLDEN[k]["steps"][-1]["n_grains"] for k in configs.CONFIGS]
     assert min(removed) > 0

@@ -49,6 +49,15 @@ def test_noalloc_record_matches_allocating_record(gpu):
         out = np.empty((100, 3), np.float64)
         assert rt.cudaMemcpy(out.ctypes.data, dptr, 100 * 3 * 8, 2) == 0
         assert np.array_equal(out, small)
+        # after the first call (which commits the fixed array), further
+        # calls take no device memory
+        free0, free1, total = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        assert rt.cudaMemGetInfo(ctypes.byref(free0), ctypes.byref(total)) == 0
+        for _ in range(3):
+            gpu.rng_record_noalloc(nstreams, ndraws, dptr.value)
+        assert rt.cudaDeviceSynchronize() == 0
+        assert rt.cudaMemGetInfo(ctypes.byref(free1), ctypes.byref(total)) == 0
+        assert free1.value == free0.value
     finally:
         rt.cudaFree(dptr)
     with pytest.raises(gpu.SevcError) as e:
