@@ -129,7 +129,7 @@ def make_mesh(n, seed, cache=None):
         if int(z["n_grains"]) == n:
             return {k: z[k] for k in z.files}
     import meshgen
-    mesh = meshgen.make_inputs(n, seed, se="lognormal", se_params=(-1.0, 0.5))
+    mesh = meshgen.make_inputs(n, seed, se="lognormal", se_params=(-1.0, 0.5), generator="c")
     if cache:
         np.savez(cache, **mesh)
     return mesh
@@ -148,7 +148,7 @@ def make_ensemble(n_inst, lo, hi, seed, cache=None):
     import meshgen
     rng = np.random.default_rng(seed)
     sizes = rng.integers(lo, hi + 1, n_inst)
-    meshes = [meshgen.make_inputs(int(n), seed * 100003 + i) for i, n in enumerate(sizes)]
+    meshes = [meshgen.make_inputs(int(n), seed * 100003 + i, generator="c") for i, n in enumerate(sizes)]
     if cache:
         np.savez(cache, key=key, **{"%s%d" % (f, i): m[f] for i, m in enumerate(meshes)
                                     for f in ("xy", "ridges", "oris", "se")})
@@ -214,11 +214,13 @@ def run_ensemble(n_inst, lo, hi, steps, warmup, seed=7, cache=None):
             "timing": "wall clock around the steps, inputs resident on the device"}
 
 
-def run_adjoint(n=10000, steps=2000, every=100, dt=1e-6, seed=17, nbins=20, amax=3.0):
+def run_adjoint(n=10000, steps=2000, every=100, dt=4e-6, seed=17, nbins=20, amax=3.0):
     """Forward + adjoint of the 10,000-grain differentiable workload: unit
     square, SE U[0, 0.5], gamma = mu = 1, histogram loss after `steps`
-    steps, checkpoints every `every` steps.  Wall-clock times of the steps
-    (forward, with the tape) and of the adjoint call (replay + backward)."""
+    steps, checkpoints every `every` steps; dt = 4e-6 so that the window
+    holds flips and removals (about 190 of each).  Wall-clock times of the
+    steps (forward, with the tape) and of the adjoint call (replay +
+    backward)."""
     import numpy as np
     import sevc
     import meshgen
@@ -263,6 +265,46 @@ def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=2e-3, s
     meshes = [meshgen.make_inputs(int(n), 100 + i) for i, n in enumerate(sizes)]
     return calibrate.run(meshes, dt=dt, steps=steps, iters=iters, checkpoint_every=50,
                          domain=float(np.sqrt(sizes.mean())))
+
+
+def run_window(args):
+    """The main workload's mesh at --grains, run to W steps past the 5/6
+    nucleation gate and saved to --ckpt (or loaded from it when it exists),
+    then K steps: a short launch sequence from the event-heavy phase, for
+    profilers (the first call makes the checkpoint, the profiled call only
+    loads it and steps)."""
+    import sevc
+    n = args.grains
+    mesh = make_mesh(n, args.seed, args.mesh_cache)
+    opt = workload_options(sevc, n, args.steps)
+    opt.domain_bound = float(n) ** 0.5
+    eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    made = False
+    if args.ckpt and os.path.exists(args.ckpt):
+        eng.checkpoint_load(args.ckpt)
+    else:
+        g, k, gate = n, 0, None
+        while gate is None or k < gate + args.warmup:
+            g = eng.step().curr_n_grains
+            k += 1
+            if gate is None and g <= 5 * n // 6:
+                gate = k
+            if k > FULL_STEPS:
+                raise RuntimeError("no gate within %d steps" % FULL_STEPS)
+        if args.ckpt:
+            eng.checkpoint_save(args.ckpt)
+        made = True
+    g0 = eng.grain_stats(-1)["n_grains"]
+    ms, vs, g, ev = 0.0, 0, g0, [0, 0, 0]
+    for _ in range(args.steps):
+        vs += 2 * g
+        i = eng.step()
+        ms += i.gpu_ms
+        g = i.curr_n_grains
+        ev = [ev[0] + i.n_flips, ev[1] + i.n_removals, ev[2] + i.nucleation_attempted]
+    eng.close()
+    return {"grains": n, "value": vs / (ms / 1e3), "ms_per_step": ms / args.steps, "checkpoint_made": made,
+            "grains_at_window": g0, "flips": ev[0], "removals": ev[1], "nucleation_attempts": ev[2]}
 
 
 def run_small(steps, seed=1, n=2000):
@@ -400,8 +442,6 @@ def run_engine(args):
         k += 1
         if gate is None and g <= 5 * n // 6:
             gate = k
-        if not info.keep_going:
-            break
     st_final = eng.get_state()
     e_wall = time.time() - e0 - ck_s
     eng.close()
@@ -595,12 +635,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate", "small"],
+    ap.add_argument("--ckpt", default=None, help="--workload window: checkpoint file past the gate (made if absent)")
+    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate", "small", "window"],
                     help="ensemble: batched ensemble against sequential plain runs; calibrate: 64 x 20,000-grain "
                          "batched calibration, 50 iterations; each prints its own JSON line")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--ensemble-grains", type=int, nargs=2, default=[500, 20000])
-    ap.add_argument("--ensemble-sample", type=int, default=64,
+    ap.add_argument("--ensemble-sample", type=int, default=512,
                     help="instances of the ensemble measurement added to the single-run line (0: none)")
     ap.add_argument("--ensemble-cache", default=None, help="npz file to reuse the generated ensemble")
     ap.add_argument("--no-adjoint-sample", dest="adjoint_sample", action="store_false",
@@ -621,6 +662,14 @@ def main():
                           "ms_per_step": r["batch_ms_per_step"], "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded periodic Voronoi)",
                           "config": {"workload": "batched ensemble", **r}}))
+        return
+    if args.workload == "window":
+        r = run_window(args)
+        print(json.dumps({"metric": METRIC.replace("1M", "%d" % args.grains), "value": r["value"], "unit": UNIT,
+                          "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded periodic Voronoi, lognormal stored energy)",
+                          "config": {"workload": "steps past the nucleation gate", **r}}))
         return
     if args.workload == "small":
         r = run_small(args.steps)

@@ -326,6 +326,25 @@ sevc_status sevc_set_profiling(sevc_handle *h, int on);
 sevc_status sevc_get_profile(sevc_handle *h, int max_entries, char (*names)[48], double *ms,
                              int64_t *launches, int *n_entries);
 
+/* Initial microstructure: the job of the reference's generator
+ * voronoi/voronoi.py:12-169 (a periodic Voronoi diagram of n seeds drawn
+ * uniformly in the unit square, vertices on the 2^-32 grid of [0, 1), only
+ * triple junctions; a degenerate sample is drawn again, up to 20 times),
+ * in C on every host core.  Outputs: xy 2n vertices (interleaved), ridges
+ * 3n pairs of vertex indices, oris n orientations U[0,1) and se n stored
+ * energies (se_dist 0: U[0,1), 1: triangular(3, 6, 6) as voronoi.py
+ * --sedist triangular); oris and se may be NULL.  The random stream is
+ * this library's (xoshiro256** seeded by `seed`), not numpy's: meshes
+ * agree with voronoi.py's in distribution.  n >= 64.  SEVC_ERR_TOPOLOGY if
+ * no sample gave a triple-junction mesh. */
+sevc_status sevc_voronoi_generate(int n, uint64_t seed, int se_dist, double *xy, int32_t *ridges, double *oris,
+                                  double *se);
+/* The four input files of voronoi.py:141-164 (vertices "%.16f %.16f",
+ * ridges "%d %d", orientations and stored energies "%.16f"). */
+sevc_status sevc_voronoi_write(int n, const double *xy, const int32_t *ridges, const double *oris, const double *se,
+                               const char *vertex_file, const char *ridge_file, const char *ori_file,
+                               const char *se_file);
+
 /* The number formatting of the snapshots: writes x as printf("%.16f")
  * does (correctly rounded, ties to even) into out (at least 48 bytes),
  * returns the length.  Integer arithmetic only, several times faster

@@ -1,4 +1,5 @@
-"""Build the engine: libsevc.so (CUDA kernels + C ABI + host C) and the sevc CLI.
+"""Build the engine: libsevc.so (CUDA kernels + C ABI + host C), the sevc CLI
+and the sevc-voronoi input generator.
 
 Every .cu file is compiled for sm_103a only, with -fmad=false (no fused
 multiply-add, the arithmetic contract of the kernels) and -lineinfo; host C
@@ -16,6 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libsevc.so")
 CLI = os.path.join(PKG, "sevc")
+VORONOI_CLI = os.path.join(PKG, "sevc-voronoi")
 
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -26,7 +28,7 @@ CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-W
 
 CU = ["sevc_geometry.cu", "sevc_topology.cu", "sevc_nucleation.cu", "sevc_adjoint.cu", "sevc_check.cu",
       "sevc_engine.cu"]
-C = ["sevc_host.c"]
+C = ["sevc_host.c", "sevc_voronoi.c"]
 HDRS = ["sevc_device.cuh", "sevc_internal.h", "sevc_host.h"]
 
 
@@ -67,9 +69,10 @@ def build(force=False, verbose=False, ptxas_info=False):
         tmp = LIB + ".tmp%d" % os.getpid()
         _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lgomp"])
         os.replace(tmp, LIB)
-    cli_src = os.path.join(PKG, "cli", "sevc_main.c")
-    if force or _stale(CLI, [cli_src, LIB]):
-        _run(["gcc"] + CFLAGS + [cli_src, "-o", CLI, "-L", PKG, "-lsevc", "-lm", "-Wl,-rpath,$ORIGIN"])
+    for src, exe in ((os.path.join(PKG, "cli", "sevc_main.c"), CLI),
+                     (os.path.join(PKG, "cli", "sevc_voronoi_main.c"), VORONOI_CLI)):
+        if force or _stale(exe, [src, LIB]):
+            _run(["gcc"] + CFLAGS + [src, "-o", exe, "-L", PKG, "-lsevc", "-lm", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("".join(logs))
     return LIB

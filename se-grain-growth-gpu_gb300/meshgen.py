@@ -1,8 +1,10 @@
 """Periodic Voronoi initial microstructures in the reference's input format.
 
 The reference ships voronoi/voronoi.py, a pure-Python generator (3x3 tiling,
-Python loops; about 3-4 minutes at 1M grains).  This module produces the
-same kind of input, vectorised with numpy and scipy.spatial.Voronoi:
+Python loops; about 3-4 minutes at 1M grains).  Two generators produce the
+same kind of input: the library's C generator (sevc_voronoi_generate,
+OpenMP cell clipping; a few seconds at 1M grains), and this module's
+numpy/scipy version:
 
 * N seeds uniform in the unit square; only seeds within a margin of the
   border are replicated into the eight periodic images (the Voronoi cells
@@ -72,14 +74,24 @@ def periodic_voronoi(n, rng, max_attempts=20, points=None):
     raise RuntimeError("could not build a periodic Voronoi mesh of %d grains" % n)
 
 
-def make_inputs(n, seed, se="uniform", se_params=None):
+def make_inputs(n, seed, se="uniform", se_params=None, generator="scipy"):
     """Mesh, orientations and stored energies for `n` grains.
 
     se: "uniform" U[0,1) (rescaled by SE_min/SE_max in the options),
         "lognormal" with se_params=(mu, sigma), "triangular" (3, 6, 6) like
         voronoi.py --sedist triangular.
+    generator: "scipy" (this module, numpy + scipy.spatial.Voronoi) or "c"
+        (the library's OpenMP generator sevc_voronoi_generate, several
+        times faster; same distribution, different sample for a seed).
     """
     rng = np.random.default_rng(seed)
+    if generator == "c":
+        import sevc
+        m = sevc.voronoi(n, seed, "triangular" if se == "triangular" else "uniform")
+        if se == "lognormal":
+            mu, sigma = se_params or (-1.0, 0.5)
+            m["se"] = rng.lognormal(mu, sigma, n)
+        return m
     xy, ridges = periodic_voronoi(n, rng)
     oris = rng.random(n)
     if se == "lognormal":

@@ -26,7 +26,8 @@ EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_
            "sevc_tape_start", "sevc_tape_stop", "sevc_area_histogram", "sevc_adjoint_histogram",
            "sevc_checkpoint_save", "sevc_checkpoint_load", "sevc_grain_stats", "sevc_format_fixed16",
            "sevc_check_data_host", "sevc_check_mesh", "sevc_set_graphs", "sevc_measure_fp64_rate",
-           "sevc_autotune", "sevc_selftest_arith", "sevc_write_snapshot"]
+           "sevc_autotune", "sevc_selftest_arith", "sevc_write_snapshot", "sevc_state_digest", "sevc_set_limits",
+           "sevc_voronoi_generate", "sevc_voronoi_write"]
 
 
 class SevcError(RuntimeError):
@@ -188,6 +189,29 @@ def write_snapshot(arrs, opt, path, time):
     L = lib()
     L.sevc_write_snapshot.argtypes = [C.POINTER(MeshHost), C.POINTER(Options), C.c_char_p, C.c_double]
     _check(L.sevc_write_snapshot(C.byref(mh), C.byref(opt), path.encode(), float(time)))
+
+
+def voronoi(n, seed, se_dist="uniform"):
+    """Periodic Voronoi input of n grains from the library's C generator
+    (sevc_voronoi_generate, voronoi.py's job): dict with xy (2n x 2),
+    ridges (3n x 2), oris and se (n each; se U[0,1) or triangular(3,6,6))."""
+    L = lib()
+    L.sevc_voronoi_generate.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
+    xy, ridges = np.empty((2 * n, 2)), np.empty((3 * n, 2), np.int32)
+    oris, se = np.empty(n), np.empty(n)
+    _check(L.sevc_voronoi_generate(n, seed, 1 if se_dist == "triangular" else 0, xy.ctypes.data, ridges.ctypes.data,
+                                   oris.ctypes.data, se.ctypes.data))
+    return {"xy": xy, "ridges": ridges, "oris": oris, "se": se, "n_grains": n}
+
+
+def voronoi_write(inp, vertices, ridges, oris, se):
+    """The four input files (voronoi.py's formats) of a voronoi() result."""
+    L = lib()
+    L.sevc_voronoi_write.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_char_p] * 4
+    a = {k: np.ascontiguousarray(inp[k]) for k in ("xy", "ridges", "oris", "se")}
+    _check(L.sevc_voronoi_write(len(a["oris"]), a["xy"].ctypes.data, a["ridges"].ctypes.data, a["oris"].ctypes.data,
+                                a["se"].ctypes.data, vertices.encode(), ridges.encode(), oris.encode(), se.encode()))
 
 
 def measure_fp64_rate():
