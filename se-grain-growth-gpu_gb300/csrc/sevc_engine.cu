@@ -27,6 +27,7 @@
 #include <vector>
 
 long long sevc_kernel_launches = 0;
+thread_local bool sevc_pdl_off = false;
 
 struct ProfEntry { double ms = 0; int64_t launches = 0; };
 
@@ -92,12 +93,17 @@ struct sevc_handle {
      * without / with a nucleation attempt, one polling iteration, and the
      * second half of a step without 2x3 pairs */
     StepGraph g_pre[2], g_poll, g_post;
+    /* the whole step as one graph (without / with a nucleation attempt):
+     * the polling and 2x3 loops are conditional WHILE nodes driven by the
+     * device, so a step is one graph launch and one readback */
+    StepGraph g_step[2];
+    bool device_loops = true;
     bool use_graphs = true;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     /* side streams of the step (branches that do not depend on each other
      * run concurrently; captured as graph branches) and the fork / join
      * events between them: 0-5 in the first half, 6-7 in the tail */
-    cudaStream_t side[2] = { nullptr, nullptr };
+    cudaStream_t side[3] = { nullptr, nullptr, nullptr };   /* [2]: capture of loop bodies */
     cudaEvent_t evfork[8] = {};
     bool profiling = false;
     std::map<std::string, ProfEntry> prof;
@@ -199,6 +205,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.digest, SEVC_DIGEST_FIELDS * 8 },
         { (void **)&x.vown, V * 8 }, { (void **)&x.bown, B * 8 }, { (void **)&x.ehits, maxn * 4 },
         { (void **)&x.n_ehits, 4 }, { (void **)&x.edefer, maxn }, { (void **)&x.ndefer, I * 4 },
+        { (void **)&x.ptot, 4 }, { (void **)&x.tt_first, 4 }, { (void **)&x.tt_pass, 4 },
     };
     size_t total = 0;
     for (auto &q : r) total += align256(q.bytes);
@@ -332,7 +339,7 @@ sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handl
     /* readback: counters, events, polling iterations, 2x3 counts per instance */
     h->h_big_ints = (size_t)ninst * (CTR_COUNT + EVT_COUNT + 1 + TWO_THREE_PASSES) + 64;
     bool streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
-    for (int k = 0; streams_ok && k < 2; k++)
+    for (int k = 0; streams_ok && k < 3; k++)
         streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking), "stream");
     for (int k = 0; streams_ok && k < 8; k++)
         streams_ok = cuda_ok(cudaEventCreateWithFlags(&h->evfork[k], cudaEventDisableTiming), "event");
@@ -415,7 +422,7 @@ void tape_free(sevc_handle *h)
 
 void drop_graphs(sevc_handle *h)
 {
-    StepGraph *gs[] = { &h->g_pre[0], &h->g_pre[1], &h->g_poll, &h->g_post };
+    StepGraph *gs[] = { &h->g_pre[0], &h->g_pre[1], &h->g_poll, &h->g_post, &h->g_step[0], &h->g_step[1] };
     for (StepGraph *g : gs) {
         if (g->exec) cudaGraphExecDestroy(g->exec);
         *g = StepGraph();
@@ -532,14 +539,23 @@ void enqueue_poll(sevc_handle *h)
 }
 
 /* from the 3-sided labels to the end of the step (src/main.cu:252-325);
- * lists_unchanged: no 2x3 removal edited a list since the side-count order */
-void enqueue_tail(sevc_handle *h, bool lists_unchanged)
+ * lists_unchanged: no 2x3 removal edited a list since the side-count order
+ * (1), some did (0), the device knows (-1: the step's first 2x3 count
+ * recorded by the whole-step graph decides) */
+void enqueue_tail(sevc_handle *h, int lists_unchanged)
 {
     cudaStream_t s = h->stream;
     const sevc_options &o = h->opt;
     DevMesh &m = h->m;
     DevScratch &x = h->x;
-    { Prof pr(h, "label_3sided"); launch_label_3sided(m, x, o.dt, lists_unchanged, s); }        /* :252-255 */
+    if (lists_unchanged < 0) {                                                                    /* :252-255 */
+        sevc_pdl_off = true;     /* the first kernel after a conditional node */
+        launch_label_3sided_auto(m, x, o.dt, s);
+        sevc_pdl_off = false;
+    } else {
+        Prof pr(h, "label_3sided");
+        launch_label_3sided(m, x, o.dt, lists_unchanged != 0, s);
+    }
     { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
     { Prof pr(h, "remove_grains"); launch_remove_grains(m, x, x.list_c, x.n_c, s); }              /* :259 */
     launch_clear_grain_cand(m, x.list_c, x.n_c, s);
@@ -568,7 +584,83 @@ void enqueue_tail(sevc_handle *h, bool lists_unchanged)
 void enqueue_post(sevc_handle *h)
 {
     { Prof pr(h, "conflicts"); launch_conflicts(h->m, h->x.list_a, h->x.n_a, h->stream); }         /* :222-225 */
-    enqueue_tail(h, true);
+    enqueue_tail(h, 1);
+}
+
+/* Add a WHILE conditional node at the current point of the capture on the
+ * handle's stream.  pre(handle) enqueues on that stream what runs just
+ * before the node (it may set the condition); body(stream, handle)
+ * enqueues the loop body onto the given stream, captured into the node's
+ * body graph.  Launches in the body go without programmatic serialisation
+ * (a body holds kernels, memsets and copies with plain dependencies). */
+template <class Pre, class Body>
+bool capture_while(sevc_handle *h, unsigned dflt, unsigned flags, Pre &&pre, Body &&body)
+{
+    cudaStream_t s = h->stream;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *ed = nullptr;
+    size_t nd = 0;
+    if (!cuda_ok(cudaStreamGetCaptureInfo(s, &st, nullptr, &cg, &deps, &ed, &nd), "capture info")) return false;
+    cudaGraphConditionalHandle hnd;
+    if (!cuda_ok(cudaGraphConditionalHandleCreate(&hnd, cg, dflt, flags), "conditional handle")) return false;
+    pre(hnd);
+    if (!cuda_ok(cudaStreamGetCaptureInfo(s, &st, nullptr, &cg, &deps, &ed, &nd), "capture info")) return false;
+    std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+    cudaGraphNodeParams np = { cudaGraphNodeTypeConditional };
+    np.conditional.handle = hnd;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (!cuda_ok(cudaGraphAddNode(&node, cg, dv.data(), nullptr, dv.size(), &np), "conditional node")) return false;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    if (!cuda_ok(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                 "capture dependencies"))
+        return false;
+    cudaStream_t bs = h->side[2];
+    bool ok = cuda_ok(cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                      "body capture");
+    if (ok) {
+        sevc_pdl_off = true;
+        body(bs, hnd);
+        sevc_pdl_off = false;
+        cudaGraph_t out = nullptr;
+        ok = cuda_ok(cudaStreamEndCapture(bs, &out), "body capture");
+    }
+    return ok;
+}
+
+/* The whole step as one launch sequence for a graph (src/main.cu:121-325):
+ * the first half, the polling loop and the 2x3 loop as device-driven
+ * WHILE nodes with the conflicts in between, then the tail.  Only while
+ * capturing. */
+bool enqueue_step_graph(sevc_handle *h, bool nucleation)
+{
+    cudaStream_t s = h->stream;
+    DevMesh &m = h->m;
+    DevScratch &x = h->x;
+    enqueue_pre(h, nucleation);
+    cudaMemsetAsync(x.ptot, 0, sizeof(int), s);
+    bool ok = capture_while(h, 1u, cudaGraphCondAssignDefault, [](cudaGraphConditionalHandle) {},   /* :219 */
+                            [&](cudaStream_t bs, cudaGraphConditionalHandle hnd) {
+                                launch_poll_iteration(m, x, x.list_a, x.n_a, h->p, bs);
+                                launch_poll_cond(m, x, hnd, h->polling_cap, bs);
+                            });
+    if (!ok) return false;
+    sevc_pdl_off = true;         /* the first kernels after a conditional node */
+    launch_conflicts(m, x.list_a, x.n_a, s);                                                        /* :222-225 */
+    sevc_pdl_off = false;
+    ok = capture_while(h, 0u, 0u, [&](cudaGraphConditionalHandle hnd) { launch_tt_init(x, hnd, s); },  /* :227-250 */
+                       [&](cudaStream_t bs, cudaGraphConditionalHandle hnd) {
+                           launch_remove_two_three_dev(m, x, x.list_b, x.n_b, bs);
+                           launch_fix_lists(m, bs);
+                           launch_compact(m, x, CK_TWO_THREE, x.list_b, x.n_b, bs);
+                           launch_tt_cond(x, hnd, bs);
+                       });
+    if (!ok) return false;
+    enqueue_tail(h, -1);
+    return true;
 }
 
 sevc_status err_bits_to_status(int bits)
@@ -577,6 +669,7 @@ sevc_status err_bits_to_status(int bits)
     if (bits & ERRB_TOPOLOGY) { sevc_set_error("inconsistent mesh met by an event kernel"); return SEVC_ERR_TOPOLOGY; }
     if (bits & ERRB_RNG) { sevc_set_error("nucleation picked no valid vertex (the reference reads stale data here)"); return SEVC_ERR_TOPOLOGY; }
     if (bits & ERRB_WORKLIST) { sevc_set_error("internal worklist overflow"); return SEVC_ERR_CAPACITY; }
+    if (bits & ERRB_NONCONVERGED) { sevc_set_error("polling did not converge"); return SEVC_ERR_NONCONVERGED; }
     return SEVC_OK;
 }
 
@@ -779,6 +872,14 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     h->h_flags[3] = h->curr_n_grains;
     if (!cuda_ok(cudaMemcpyAsync(x.flags + 1, h->h_flags + 1, 3 * sizeof(int), cudaMemcpyHostToDevice, s), "upload"))
         return SEVC_ERR_CUDA;
+    const bool whole = graphs_on(h) && h->device_loops;
+    if (whole) {
+        /* one graph: the loops run on the device, their counts come back
+         * with the step summary */
+        bool cap_ok = true;
+        if (!run_seq(h, h->g_step[n_on ? 1 : 0], [&] { cap_ok = enqueue_step_graph(h, n_on > 0); }) || !cap_ok)
+            return SEVC_ERR_CUDA;
+    } else {
     if (!run_seq(h, h->g_pre[n_on ? 1 : 0], [&] { enqueue_pre(h, n_on > 0); })) return SEVC_ERR_CUDA;
 
     /* polling (:219); the first readback also brings the 2x3 count */
@@ -814,7 +915,8 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
             { Prof pr(h, "two_three_remove"); launch_remove_two_three(m, x, x.list_b, x.n_b, k, s); }
             { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }
         }
-        enqueue_tail(h, false);
+        enqueue_tail(h, 0);
+    }
     }
     cudaEventRecord(h->ev1, s);
 
@@ -873,6 +975,17 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
         loc.n_flips += ii.n_flips;
         loc.n_nucleations += ii.n_nucleations;
         loc.n_conflicts += ii.n_conflicts;
+    }
+    if (whole) {        /* the loops' counts, as the host loops report them */
+        loc.polling_iters = 0;
+        for (int i = 0; i < I; i++) loc.polling_iters = std::max(loc.polling_iters, h->iinfo[i].polling_iters);
+        for (int k = 0; k < TWO_THREE_PASSES; k++) {
+            int c = 0;
+            for (int i = 0; i < I; i++) c += hb[o_seg + (size_t)k * I + i];
+            loc.two_three_counts[k] = c;
+            loc.n_two_three_iters = k + 1;
+            if (c == 0) break;
+        }
     }
     h->curr_n_grains = total;
     h->nucleated_area = batch ? area_sum / I : area_sum;
@@ -1188,8 +1301,8 @@ sevc_status sevc_set_limits(sevc_handle *h, int polling_cap, int worklist_cap)
     if (worklist_cap > 0) {
         h->m.fixcap = worklist_cap < h->ng ? worklist_cap : h->ng;
         h->m.modcap = worklist_cap < h->nv ? worklist_cap : h->nv;
-        drop_graphs(h);   /* captured launches carry the mesh view by value */
     }
+    drop_graphs(h);   /* captured launches carry both by value */
     return SEVC_OK;
 }
 
@@ -1505,8 +1618,8 @@ static bool make_folders(sevc_options *o, int verbose)
         if (verbose) printf("rm -rf %s\n", o->output_folder);
     }
     mkdir(o->output_folder, 0775);
-    char data[300];
-    snprintf(data, sizeof data, "%s/DATA", o->output_folder);
+    char data[sizeof o->output_folder];
+    snprintf(data, sizeof data, "%.250s/DATA", o->output_folder);
     mkdir(data, 0775);
     snprintf(o->output_folder, sizeof o->output_folder, "%s", data);
     if (verbose) printf("mkdir %s\n", o->output_folder);

@@ -38,6 +38,9 @@ struct DevScratch {
     int *ehits, *n_ehits;
     uint8_t *edefer;
     int *ndefer;
+    /* device-driven loops of a whole-step graph: polling iterations taken
+     * (all instances), the first 2x3 count and the 2x3 pass index */
+    int *ptot, *tt_first, *tt_pass;
 };
 constexpr int EXTRA_CAP = 1024;
 constexpr int TWO_THREE_PASSES = 20;  /* src/main.cu:227 */
@@ -113,6 +116,20 @@ void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaS
 /* pass `pass` of the 2x3 loop (per-instance counts go to x.segcnt) */
 void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *list, const int *n, int pass,
                              cudaStream_t s);
+/* the same with the pass index read from x.tt_pass on the device */
+void launch_remove_two_three_dev(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s);
+/* Loop control of the whole-step graph (conditional WHILE nodes):
+ * poll_cond after each polling iteration: continue while an instance has
+ * not converged, up to `cap` iterations (past it: ERRB_NONCONVERGED);
+ * tt_init before the 2x3 loop: record the first count, start while it is
+ * nonzero; tt_cond after each pass: the next pass runs while the count
+ * just compacted is nonzero and fewer than TWO_THREE_PASSES ran. */
+void launch_poll_cond(const DevMesh &m, const DevScratch &x, cudaGraphConditionalHandle hnd, int cap, cudaStream_t s);
+void launch_tt_init(const DevScratch &x, cudaGraphConditionalHandle hnd, cudaStream_t s);
+void launch_tt_cond(const DevScratch &x, cudaGraphConditionalHandle hnd, cudaStream_t s);
+/* the 3-sided labels, bucket or full as x.tt_first says (no 2x3 removal:
+ * the bucket) */
+void launch_label_3sided_auto(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s);
 /* bucket: no grain list changed since this step's side-count order, so
  * only its 3-sided bucket is visited */
 void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool bucket, cudaStream_t s);
@@ -167,6 +184,10 @@ void launch_grain_stats(const DevMesh &m, int lo, int hi, double *out, cudaStrea
 
 /* kernels launched by this process (reported per step) */
 extern long long sevc_kernel_launches;
+/* set while the body of a conditional graph node, or the first kernels
+ * after one, are captured: launches then go without the
+ * programmatic-serialisation attribute */
+extern thread_local bool sevc_pdl_off;
 #define COUNT_LAUNCHES(k) (sevc_kernel_launches += (k))
 
 /* Launch with programmatic dependent launch allowed: the grid may be
@@ -187,7 +208,7 @@ inline void launch_dep(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s, A
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = sevc_pdl_off ? 0 : 1;
     COUNT_LAUNCHES(1);
     cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(args)...);
 }

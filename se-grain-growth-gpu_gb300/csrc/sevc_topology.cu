@@ -561,10 +561,12 @@ __device__ bool sorted_contains(const int *a, int lo, int hi, int x)
  * count) and boundaries re-wired during the scan (CE) can qualify, so the
  * scan visits exactly those, in index order, re-testing each on visit. */
 /* One thread per instance, each over its own part of the ascending list. */
-__global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int *extra, int *segcnt)
+__global__ void k_remove_two_three(DevMesh m, const int *list, const int *n, int *extra, int *segcnt,
+                                   const int *pass_dev)
 {
     int inst = blockIdx.x * blockDim.x + threadIdx.x;
     if (inst >= m.ninst) return;
+    if (pass_dev) segcnt += (size_t)*pass_dev * m.ninst;
     int i = lower_bound_i(list, *n, m.boff[inst]);
     int N = lower_bound_i(list, *n, m.boff[inst + 1]);
     segcnt[inst] = N - i;
@@ -660,6 +662,47 @@ __global__ void k_label_3sided_bucket(DevMesh m, double dt, const int *perm, con
         int g = perm[start + i];
         m.gcand[g] = label3_cand(m, g, dt);
     }
+}
+/* either of the two above, as the step's first 2x3 count says: no 2x3
+ * removal (count 0) leaves every list as the side-count order saw it */
+__global__ void k_label_3sided_auto(DevMesh m, double dt, const int *perm, const int *vbucket, const int *tt_first)
+{
+    griddep_wait();
+    if (*tt_first == 0) {
+        int n3 = vbucket[VB_COUNT(3)], start = vbucket[VB_START(3)];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x) {
+            int g = perm[start + i];
+            m.gcand[g] = label3_cand(m, g, dt);
+        }
+    } else {
+        for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < m.ng; g += gridDim.x * blockDim.x)
+            if (m.gen[g]) m.gcand[g] = m.gvlen[g] == 3 ? label3_cand(m, g, dt) : 0;
+    }
+}
+/* loop control of the whole-step graph (one thread) */
+__global__ void k_poll_cond(cudaGraphConditionalHandle hnd, const int *nrun, int *ptot, int cap, int *err)
+{
+    if (threadIdx.x) return;
+    int it = ++*ptot;
+    bool run = *nrun > 0;
+    if (run && it >= cap) {
+        atomicOr(err, ERRB_NONCONVERGED);
+        run = false;
+    }
+    cudaGraphSetConditional(hnd, run ? 1u : 0u);
+}
+__global__ void k_tt_init(cudaGraphConditionalHandle hnd, const int *n, int *first, int *pass)
+{
+    if (threadIdx.x) return;
+    *first = *n;
+    *pass = 0;
+    cudaGraphSetConditional(hnd, *n > 0 ? 1u : 0u);
+}
+__global__ void k_tt_cond(cudaGraphConditionalHandle hnd, const int *n, int *pass)
+{
+    if (threadIdx.x) return;
+    int p = ++*pass;
+    cudaGraphSetConditional(hnd, (*n > 0 && p < TWO_THREE_PASSES) ? 1u : 0u);
 }
 __global__ void k_clear_grain_cand(DevMesh m, const int *list, const int *n)
 {
@@ -1400,7 +1443,28 @@ void launch_remove_two_three(const DevMesh &m, const DevScratch &x, const int *l
                              cudaStream_t s)
 {
     COUNT_LAUNCHES(1), k_remove_two_three<<<instgrid(m), 32, 0, s>>>(m, list, n, x.extra,
-                                                                     x.segcnt + (size_t)pass * m.ninst);
+                                                                     x.segcnt + (size_t)pass * m.ninst, nullptr);
+}
+void launch_remove_two_three_dev(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_remove_two_three<<<instgrid(m), 32, 0, s>>>(m, list, n, x.extra, x.segcnt, x.tt_pass);
+}
+void launch_poll_cond(const DevMesh &m, const DevScratch &x, cudaGraphConditionalHandle hnd, int cap, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_poll_cond<<<1, 32, 0, s>>>(hnd, x.nrun, x.ptot, cap, m.err);
+}
+void launch_tt_init(const DevScratch &x, cudaGraphConditionalHandle hnd, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_tt_init<<<1, 32, 0, s>>>(hnd, x.n_b, x.tt_first, x.tt_pass);
+}
+void launch_tt_cond(const DevScratch &x, cudaGraphConditionalHandle hnd, cudaStream_t s)
+{
+    COUNT_LAUNCHES(1), k_tt_cond<<<1, 32, 0, s>>>(hnd, x.n_b, x.tt_pass);
+}
+void launch_label_3sided_auto(const DevMesh &m, const DevScratch &x, double dt, cudaStream_t s)
+{
+    int g = (m.ng + TPB - 1) / TPB;
+    launch_dep(k_label_3sided_auto, g < 4 * 152 ? g : 4 * 152, TPB, s, m, dt, x.perm, x.vbucket, x.tt_first);
 }
 
 void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool bucket, cudaStream_t s)

@@ -297,3 +297,31 @@ def test_program_loop_snapshots_match_reference(gpu, tmp_path):
             assert open(path, "rb").read() == open(os.path.join(out, "DATA", files[prog]), "rb").read()
             prog += 1
     eng.close()
+
+
+@pytest.mark.parametrize("name", ["plain_unit", "example_ref2k"])
+def test_cli_log_lines_match_reference(gpu, name, tmp_path):
+    """The drop-in executable prints the reference's per-step log lines
+    (src/main.cu:122, 231, 324-325): `sevc -c run.ini` parsed as the
+    reference's own log is parsed for the golden record (make_golden.
+    parse_log) gives the same numbers at every step; its snapshots have the
+    reference's integer digests."""
+    import subprocess
+    import make_golden
+    _, _, keys, _, mg = configs.ALL_CONFIGS[name]
+    out = os.path.join(str(tmp_path), "out")
+    ini = configs.write_ini(os.path.join(str(tmp_path), "run.ini"), name, out, nmax=configs.golden_nmax(name))
+    if "leave_percent" not in keys:
+        with open(ini, "a") as f:
+            f.write("[Temporal]\nleave_percent=%r\n" % (mg / int(keys["n_grains"])))
+    exe = os.path.join(os.path.dirname(gpu.LIB_PATH), "sevc")
+    r = subprocess.run([exe, "-c", ini, "--honor-leave-percent"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    mine, ref = make_golden.parse_log(r.stdout), GOLDEN[name]["steps"]
+    assert len(mine) == len(ref)
+    for a, b in zip(mine, ref):
+        assert a == b, (a, b)
+    files = sorted(os.listdir(os.path.join(out, "DATA")))
+    assert len(files) == len(GOLDEN[name]["snapshots"])
+    for f, (_, topo) in zip(files, GOLDEN[name]["snapshots"]):
+        assert snapshot.digests(os.path.join(out, "DATA", f))[1] == topo, f
