@@ -252,19 +252,23 @@ def run_adjoint(n=10000, steps=2000, every=100, dt=4e-6, seed=17, nbins=20, amax
             "timing": "wall clock; forward = the taped steps, backward = sevc_adjoint_histogram"}
 
 
-def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=2e-3, seed=5):
+def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=2e-3, seed=5, nucleation=None):
     """Batched calibration of (gamma, mu, stored-energy scale) by Adam steps
     through the adjoint, against the histogram of the same batch run with
     the generating values (1, 1, 1); grains about one unit across (domain
-    sqrt of the mean grain count), SE U[0,1)."""
+    sqrt of the mean grain count), SE U[0,1).  nucleation (gap, MC_k): the
+    window starts once every instance has passed its 5/6 gate, with stored
+    energies triangular(3, 6, 6) (voronoi.py's, where the Metropolis test
+    accepts nucleations at this grain size)."""
     import numpy as np
     import meshgen
     import calibrate
     rng = np.random.default_rng(seed)
     sizes = rng.integers(lo, hi + 1, n_inst)
-    meshes = [meshgen.make_inputs(int(n), 100 + i) for i, n in enumerate(sizes)]
+    se = "triangular" if nucleation else "uniform"
+    meshes = [meshgen.make_inputs(int(n), 100 + i, se=se, generator="c") for i, n in enumerate(sizes)]
     return calibrate.run(meshes, dt=dt, steps=steps, iters=iters, checkpoint_every=50,
-                         domain=float(np.sqrt(sizes.mean())))
+                         domain=float(np.sqrt(sizes.mean())), nucleation=nucleation)
 
 
 def run_window(args):
@@ -280,6 +284,8 @@ def run_window(args):
     opt.domain_bound = float(n) ** 0.5
     eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
     made = False
+    if args.direct:
+        eng.set_graphs(False)
     if args.ckpt and os.path.exists(args.ckpt):
         eng.checkpoint_load(args.ckpt)
     else:
@@ -635,10 +641,14 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--direct", action="store_true",
+                    help="--workload window: launch every kernel directly (no CUDA graphs), for profilers")
+    ap.add_argument("--cal-dt", type=float, default=1e-3, help="--workload calibrate: time step")
     ap.add_argument("--ckpt", default=None, help="--workload window: checkpoint file past the gate (made if absent)")
     ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate", "small", "window"],
                     help="ensemble: batched ensemble against sequential plain runs; calibrate: 64 x 20,000-grain "
-                         "batched calibration, 50 iterations; each prints its own JSON line")
+                         "batched calibration with nucleation, 50 iterations of a --steps window past the "
+                         "gate; each prints its own JSON line")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--ensemble-grains", type=int, nargs=2, default=[500, 20000])
     ap.add_argument("--ensemble-sample", type=int, default=512,
@@ -680,7 +690,8 @@ def main():
                           "config": {"workload": "2,000-grain plain run, SE U[0,0.5], dt 1e-6", **r}}))
         return
     if args.workload == "calibrate":
-        r = run_calibration(n_inst=64, lo=20000, hi=20000, steps=args.steps, iters=50, dt=2e-3)
+        r = run_calibration(n_inst=64, lo=20000, hi=20000, steps=args.steps, iters=50, dt=args.cal_dt,
+                            nucleation=(5, 3.0))
         print(json.dumps({"metric": "backward/forward time ratio of batched calibration",
                           "value": r["backward_forward_ratio"], "unit": "x", "n_gpus": 1, "steps": args.steps,
                           "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,

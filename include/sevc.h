@@ -266,8 +266,10 @@ sevc_status sevc_set_stored_energy(sevc_handle *h, const double *se /* ng values
  * adjoint replays one segment at a time from its checkpoint, recording the
  * mesh and the position-moving events of each step, and runs the steps
  * backward.  Topology changes are followed (flips, 2x3 and 3-sided
- * removals move or disable vertices; their discrete decisions carry no
- * gradient).  Runs with nucleation are not covered (SEVC_ERR_ARG).
+ * removals move or disable vertices; a nucleation moves its vertex and
+ * places the new triangle by a map of the neighbours' positions, with the
+ * replayed random draws).  Discrete decisions carry no gradient, and a
+ * nucleated grain's stored energy (0) is not a parameter.
  * Memory: one copy of the device state per checkpoint plus about 600 bytes
  * per grain per step of one segment. */
 sevc_status sevc_tape_start(sevc_handle *h, int checkpoint_every);

@@ -61,7 +61,7 @@ def events(args):
                 f.write("[Temporal]\nleave_percent=%r\n" % (mg / n_grains))
         dirs[side] = (ini, os.path.join(tmp, side, "DATA"))
     env = dict(os.environ, SEVC_REF_MIN_GRAINS=str(mg))
-    r, ref_s = run([os.path.join(OUT, args.exe), "-c", dirs["ref"][0]], env=env)
+    r, ref_s = run([os.path.join(OUT, args.exe), "-c", dirs["ref"][0]], env=env, timeout=args.timeout)
     out["ref_rc"], out["ref_wall_s"] = r.returncode, ref_s
     t = marks(r.stderr)
     if len(t) > 2:
@@ -70,7 +70,7 @@ def events(args):
     ref_log = make_golden.parse_log(r.stdout)
     out["ref_tail"] = r.stdout[-400:]
     e, eng_s = run([os.path.join(ROOT, "se-grain-growth-gpu_gb300", "sevc"), "-c", dirs["eng"][0],
-                    "--honor-leave-percent"])
+                    "--honor-leave-percent"], timeout=args.timeout)
     out["eng_rc"], out["eng_wall_s"] = e.returncode, eng_s
     eng_log = make_golden.parse_log(e.stdout)
     out["steps"] = [len(ref_log), len(eng_log)]
@@ -82,6 +82,7 @@ def events(args):
     if first is None and len(ref_log) != len(eng_log):
         first = {"step": min(len(ref_log), len(eng_log)), "note": "runs of different length"}
     out["first_log_difference"] = first
+    out["log_steps_differing"] = sum(1 for a, b in zip(ref_log, eng_log) if a != b)
     out["two_three_steps"] = sum(1 for s in ref_log if any(s["two_three"]))
     fr = sorted(os.listdir(dirs["ref"][1])) if os.path.isdir(dirs["ref"][1]) else []
     fe = sorted(os.listdir(dirs["eng"][1])) if os.path.isdir(dirs["eng"][1]) else []
@@ -148,7 +149,8 @@ def timing(args):
                 "[System]\nn_blocks=32\nn_threads=256\ndebug_lvl=0\n[Output]\nfolder=%s\n"
                 % (opt.dt, opt.dtau, args.nmax, n, paths["vertices"], paths["ridges"], paths["oris"], paths["se"],
                    opt.domain_bound, os.path.join(tmp, "out")))
-    env = dict(os.environ, SEVC_REF_MIN_GRAINS="-1", SEVC_REF_SNAPSHOTS="0")
+    # the loop runs only while min_grains > 0 (src/main.cu:120): 1 never stops it here
+    env = dict(os.environ, SEVC_REF_MIN_GRAINS="1", SEVC_REF_SNAPSHOTS="0")
     r, ref_s = run([os.path.join(OUT, args.exe), "-c", ini], env=env, timeout=args.timeout)
     t = marks(r.stderr)
     ks = sorted(t)
@@ -180,7 +182,7 @@ def main():
     ap.add_argument("--config", default="example_ref2k")
     ap.add_argument("--nmax", type=int, default=None)
     ap.add_argument("--grains", type=int, default=1000000)
-    ap.add_argument("--timeout", type=float, default=1800)
+    ap.add_argument("--timeout", type=float, default=900)
     ap.add_argument("--json", default=None)
     a = ap.parse_args()
     res = events(a) if a.mode == "events" else timing(a)

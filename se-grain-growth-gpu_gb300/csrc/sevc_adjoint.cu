@@ -13,6 +13,13 @@
  *           velocities of the vertices they move; disabled vertices stop
  *   x_{n+1} = x' + dt * v'                 (src/calculus.h:391-404)
  * with gamma_j = s * f_j (s = GB_scaling, f_j = 1 for GB_eps = 0).
+ * A step with a nucleation first maps the positions by the inserted
+ * triangle (src/nucleation2.cu:116-212 with the factor 0.99): with
+ * A's boundaries ending at D, E, F, d_X = X - A (wrapped), u_X = d_X/|d_X|
+ * and r = k * |d_X*| + 0.1 (X* the end of the shortest boundary, k = 0.8
+ * times the replayed draw), the new A, B, C are A + 0.99 r u_D, u_E, u_F;
+ * the rest of the step acts on that mesh.  The nucleated grain's stored
+ * energy is 0, not a parameter.
  *
  * The adjoint below is the exact derivative of that map in real
  * arithmetic.  Two identities keep it cheap: the shoelace area is linear in
@@ -146,6 +153,7 @@ __global__ void k_adj_mark_events(uint8_t *mark, const EventRec *log, const int 
     int n = *nlog;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         EventRec r = log[i];
+        if (r.type != EV_FLIP && r.type != EV_REMOVE) continue;
         mark[r.a] = 1;
         mark[r.b] = 1;
         if (r.type == EV_REMOVE) mark[r.c] = 1;
@@ -179,6 +187,7 @@ __global__ void k_adj_events(double D, const EventRec *log, const int *nlog, dou
             lx[r.b] = s;
             continue;
         }
+        if (r.type != EV_REMOVE) continue;            /* nucleations: k_adj_nucleation */
         /* A' = A + F(u, w), u = B - A, w = C - A,
          * F = (|w| u + |u| w) / (|u| + |w - u| + |w|) */
         double2 lp = lx[r.a];
@@ -217,8 +226,53 @@ __device__ __forceinline__ double gb_weight(const DevMesh &m, int b, double eps)
     return gb_energy(m.gori[gic[0]] - m.gori[gic[1]], eps);
 }
 
+/* the nucleations of the step, last first: lambda of the positions
+ * before it from lambda after it (one thread).  For each new position
+ * Y = A + c u_X (c = 0.99 r):
+ *   dY/dX = c (I - u u^T) / |d_X|,  dY/dA = I - dY/dX + u (dc/dA)^T,
+ *   dc/dX* = 0.99 k u_X* = -dc/dA;
+ * the new vertices B and C had no position before. */
+__global__ void k_adj_nucleation(double D, const EventRec *log, const int *nlog, double2 *lam)
+{
+    for (int e = *nlog - 1; e >= 1; e--) {
+        EventRec r = log[e - 1], x = log[e];
+        if (r.type != EV_NUCL || x.type != EV_NUCL_AUX) continue;
+        int Y[3] = { r.a, r.b, r.c }, X[3] = { x.a, x.b, x.c };
+        double2 pa = r.pa, px[3] = { r.pb, r.pc, x.pa };
+        double k = x.pb.x, c = 0.99 * x.pb.y;
+        int is = (int)x.pc.x;
+        double2 ly[3] = { lam[Y[0]], lam[Y[1]], lam[Y[2]] };
+        double usx = wrapd(px[is].x, pa.x, D), usy = wrapd(px[is].y, pa.y, D);
+        double ns = sqrt(usx * usx + usy * usy);
+        usx = ns > 0 ? usx / ns : 0.0;
+        usy = ns > 0 ? usy / ns : 0.0;
+        double2 la = make_double2(0, 0);
+        double2 lstar = make_double2(0, 0);
+        for (int i = 0; i < 3; i++) {
+            double dx = wrapd(px[i].x, pa.x, D), dy = wrapd(px[i].y, pa.y, D), n = sqrt(dx * dx + dy * dy);
+            if (!(n > 0)) continue;
+            double ux = dx / n, uy = dy / n, l_u = ux * ly[i].x + uy * ly[i].y;
+            double gx = c / n * (ly[i].x - ux * l_u), gy = c / n * (ly[i].y - uy * l_u);
+            double t = 0.99 * k * l_u;
+            la.x += ly[i].x - gx - t * usx;
+            la.y += ly[i].y - gy - t * usy;
+            lam[X[i]].x += gx;
+            lam[X[i]].y += gy;
+            lstar.x += t * usx;
+            lstar.y += t * usy;
+        }
+        lam[X[is]].x += lstar.x;
+        lam[X[is]].y += lstar.y;
+        lam[Y[0]] = la;
+        lam[Y[1]] = make_double2(0, 0);
+        lam[Y[2]] = make_double2(0, 0);
+        e--;
+    }
+}
+
 /* per grain: sign of the area at the step's start, and
- * dL/dSE_g += sum_p lambda_v(p) . (-mu sign(A) dA/dx_p) */
+ * dL/dSE_g += sum_p lambda_v(p) . (-mu sign(A) dA/dx_p) (not for a
+ * nucleated grain, whose stored energy is 0, not a parameter) */
 __global__ void k_adj_grains(DevMesh m, double mu, const double2 *lv, double *sgn, double *gse)
 {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -238,7 +292,7 @@ __global__ void k_adj_grains(DevMesh m, double mu, const double2 *lv, double *sg
         double2 l = lv[v];
         acc += l.x * (0.5 * (yn - yp)) + l.y * (0.5 * (xp - xn));
     }
-    gse[g] += -mu * s * acc;
+    if (m.gtype[g] != GT_NUCLEATED) gse[g] += -mu * s * acc;
 }
 
 /* For the edge vector d (length L) and its end moved by eps along axis c,
@@ -352,7 +406,8 @@ __global__ void k_adj_vertices(DevMesh m, double mu, double eps, double s_gb, co
         if (g < 0 || !m.gen[g]) continue;
         int pv, nx;
         if (list_pos(m, g, k, &pv, &nx) < 0) continue;
-        double c = 0.5 * mu * m.gse[g] * sgn[g];
+        double se = m.gtype[g] == GT_NUCLEATED ? 0.0 : m.gse[g];
+        double c = 0.5 * mu * se * sgn[g];
         double2 a = lv[pv], b = lv[nx];
         out.x += c * (a.y - b.y);
         out.y += c * (b.x - a.x);
@@ -436,6 +491,7 @@ void launch_adjoint_step(const DevMesh &rec, const AdjointBuffers &a, double dt,
     COUNT_LAUNCHES(1), k_adj_grains<<<nblk(rec.ng), TPB, 0, s>>>(rec, mu, a.lv, a.sgn, a.gse);
     COUNT_LAUNCHES(1), k_adj_vertices<<<nblk(rec.nv), TPB, 0, s>>>(rec, mu, eps, s_gb, a.lx, a.lv, a.sgn, a.lam,
                                                                    a.ggam);
+    COUNT_LAUNCHES(1), k_adj_nucleation<<<1, 1, 0, s>>>(rec.D, log, nlog, a.lam);
 }
 
 void launch_grain_stats(const DevMesh &m, int lo, int hi, double *out, cudaStream_t s)

@@ -113,8 +113,13 @@ enum { EVT_TWO_THREE = 0, EVT_REMOVALS = 1, EVT_FLIPS = 2, EVT_NUCLEATIONS = 3, 
 
 /* one position-moving event: a T1 flip (vertices a, b move to their
  * midpoint) or a 3-sided grain removal (a moves to the length-weighted
- * point of a, b, c; b and c are disabled), with the positions it read */
-enum { EV_FLIP = 1, EV_REMOVE = 2 };
+ * point of a, b, c; b and c are disabled), with the positions it read.
+ * A nucleation takes two records in a row: EV_NUCL {a = A, b = B, c = C
+ * (the new vertices), pa, pb, pc = A, D, E before it} and EV_NUCL_AUX
+ * {a, b, c = D, E, F (the far ends of A's boundaries), pa = F,
+ * pb = (k, r) with r = k * min length + 0.1 the triangle's radius,
+ * pc.x = the slot (0..2) of the shortest boundary}. */
+enum { EV_FLIP = 1, EV_REMOVE = 2, EV_NUCL = 3, EV_NUCL_AUX = 4 };
 struct EventRec {
     int type, a, b, c;
     double2 pa, pb, pc;
@@ -136,6 +141,16 @@ __device__ __forceinline__ void log_event(const DevMesh &m, int type, int a, int
     EventRec r;
     r.type = type; r.a = a; r.b = b; r.c = c; r.pa = pa; r.pb = pb; r.pc = pc;
     L.buf[i] = r;
+}
+/* two records in consecutive slots (an event that takes two) */
+__device__ __forceinline__ void log_event_pair(const DevMesh &m, const EventRec &r0, const EventRec &r1)
+{
+    EventLog L = *m.elog;
+    if (!L.buf) return;
+    int i = atomicAdd(L.n, 2);
+    if (i + 1 >= L.cap) { atomicOr(m.err, ERRB_WORKLIST); return; }
+    L.buf[i] = r0;
+    L.buf[i + 1] = r1;
 }
 
 /* first statement of a kernel launched with launch_dep: wait until the

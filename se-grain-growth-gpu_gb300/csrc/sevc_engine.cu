@@ -19,6 +19,7 @@
 #include <cstring>
 #include <ctime>
 #include <ftw.h>
+#include <functional>
 #include <map>
 #include <string>
 #include <thread>
@@ -58,6 +59,11 @@ struct Tape {
     int rec_steps = 0, log_cap = 0;
     void *adj = nullptr;           /* AdjointBuffers storage */
     size_t adj_bytes = 0;
+    double *separam = nullptr;     /* the stored energies when the tape started */
+    /* set while a segment is replayed: after a step's nucleation kernels,
+     * copies the mesh (as the velocities will see it) into that step's
+     * record */
+    std::function<void(cudaStream_t)> after_nucleation;
 };
 
 struct sevc_handle {
@@ -99,6 +105,7 @@ struct sevc_handle {
     StepGraph g_step[2];
     bool device_loops = true;
     bool use_graphs = true;
+    bool force_direct = false;   /* this step launches directly (an adjoint replay records inside it) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     /* side streams of the step (branches that do not depend on each other
      * run concurrently; captured as graph branches) and the fork / join
@@ -417,6 +424,7 @@ void tape_free(sevc_handle *h)
     for (void *p : tp.ckpt) cudaFree(p);
     if (tp.rec) cudaFree(tp.rec);
     if (tp.adj) cudaFree(tp.adj);
+    if (tp.separam) cudaFree(tp.separam);
     tp = Tape();
 }
 
@@ -434,7 +442,7 @@ void drop_graphs(sevc_handle *h)
  * (the log pointers are arguments). */
 bool graphs_on(const sevc_handle *h)
 {
-    return h->use_graphs && !h->profiling;
+    return h->use_graphs && !h->profiling && !h->force_direct;
 }
 
 /* Run a fixed launch sequence: replay its graph (captured on first use) or
@@ -470,10 +478,10 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     cudaMemsetAsync(m.evt, 0, I * EVT_COUNT * sizeof(int), s);
     cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
     cudaMemsetAsync(m.gexact, 0, (size_t)h->ng, s);
-    launch_area_dirty(m, 0, s);   /* drop the previous step's post-area marks */
     if (nucleation) {
         { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :124-130 */
         { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
+        if (h->tape.after_nucleation) h->tape.after_nucleation(s);
     }
     /* From here three branches that share no written data run concurrently
      * (side streams, graph branches when captured):
@@ -558,7 +566,6 @@ void enqueue_tail(sevc_handle *h, int lists_unchanged)
     }
     { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
     { Prof pr(h, "remove_grains"); launch_remove_grains(m, x, x.list_c, x.n_c, s); }              /* :259 */
-    launch_clear_grain_cand(m, x.list_c, x.n_c, s);
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
     { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
     /* The counts (:317-325) read only grain flags, types and areas, which
@@ -571,9 +578,8 @@ void enqueue_tail(sevc_handle *h, int lists_unchanged)
         launch_counts(m, x, h->p, h->side[0]);
         cudaEventRecord(h->evfork[7], h->side[0]);
     }
-    { Prof pr(h, "unlabel_st2"); launch_unlabel_st2(m, x.list_a, x.n_a, s); }                     /* :282 */
-    { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }                     /* :289 */
-    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :294 */
+    { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }             /* :282, :289 */
+    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s, false); }                                   /* :294 */
     { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                                /* :314 */
     if (h->profiling) { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }
     else cudaStreamWaitEvent(s, h->evfork[7], 0);
@@ -872,6 +878,7 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     h->h_flags[3] = h->curr_n_grains;
     if (!cuda_ok(cudaMemcpyAsync(x.flags + 1, h->h_flags + 1, 3 * sizeof(int), cudaMemcpyHostToDevice, s), "upload"))
         return SEVC_ERR_CUDA;
+    h->force_direct = n_on > 0 && (bool)h->tape.after_nucleation;
     const bool whole = graphs_on(h) && h->device_loops;
     if (whole) {
         /* one graph: the loops run on the device, their counts come back
@@ -1326,12 +1333,12 @@ sevc_status sevc_set_stored_energy(sevc_handle *h, const double *se)
 sevc_status sevc_tape_start(sevc_handle *h, int checkpoint_every)
 {
     if (!h || checkpoint_every < 1) return SEVC_ERR_ARG;
-    if (h->opt.do_nucleation) {
-        sevc_set_error("the adjoint covers runs without nucleation (do_nucleation = 0)");
-        return SEVC_ERR_ARG;
-    }
     tape_free(h);
     h->tape.every = checkpoint_every;
+    if (!cuda_ok(cudaMalloc(&h->tape.separam, (size_t)h->ng * 8), "cudaMalloc tape") ||
+        !cuda_ok(cudaMemcpyAsync(h->tape.separam, h->m.gse, (size_t)h->ng * 8, cudaMemcpyDeviceToDevice, h->stream),
+                 "tape copy"))
+        return SEVC_ERR_CUDA;
     return tape_checkpoint(h) ? SEVC_OK : SEVC_ERR_CUDA;
 }
 
@@ -1388,8 +1395,8 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
            off_vel1 = off_vg + align256(V * 16), off_ven = off_vel1 + align256(V * 16), off_ven1 = off_ven + align256(V),
            off_bv = off_ven1 + align256(V), off_ben = off_bv + align256(B * 8), off_gl = off_ben + align256(B),
            off_gvl = off_gl + align256(G * SEVC_MAXV * 4), off_gen = off_gvl + align256(G * 4),
-           off_log = off_gen + align256(G), off_nlog = off_log + align256((size_t)tp.log_cap * sizeof(EventRec)),
-           step_bytes = off_nlog + 256;
+           off_gty = off_gen + align256(G), off_log = off_gty + align256(G),
+           off_nlog = off_log + align256((size_t)tp.log_cap * sizeof(EventRec)), step_bytes = off_nlog + 256;
     if (!tp.rec || tp.rec_step_bytes != step_bytes || tp.rec_steps < tp.every) {
         if (tp.rec) cudaFree(tp.rec);
         tp.rec = nullptr;
@@ -1422,19 +1429,28 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
         int K = (int)std::min<long long>(tp.every, tp.nsteps - seg * tp.every);
         for (int k = 0; k < K && !st; k++) {
             DevMesh &m = h->m;
-            bool ok = d2d(rec(k, off_pos), m.pos, V * 16) && d2d(rec(k, off_vb), m.vb, V * 16) &&
-                      d2d(rec(k, off_vg), m.vg, V * 16) && d2d(rec(k, off_ven), m.ven, V) &&
-                      d2d(rec(k, off_bv), m.bv, B * 8) && d2d(rec(k, off_ben), m.ben, B) &&
-                      d2d(rec(k, off_gl), m.glist, G * SEVC_MAXV * 4) && d2d(rec(k, off_gvl), m.gvlen, G * 4) &&
-                      d2d(rec(k, off_gen), m.gen, G) &&
-                      cuda_ok(cudaMemsetAsync(rec(k, off_nlog), 0, 4, s), "memset");
+            /* the mesh the step's velocities are computed on: at its start,
+             * or after its nucleation (recorded again from inside the step) */
+            auto record = [&, k](cudaStream_t rs) {
+                auto cp = [&](size_t off, const void *src, size_t n) {
+                    return cudaMemcpyAsync(rec(k, off), src, n, cudaMemcpyDeviceToDevice, rs) == cudaSuccess;
+                };
+                return cp(off_pos, m.pos, V * 16) && cp(off_vb, m.vb, V * 16) && cp(off_vg, m.vg, V * 16) &&
+                       cp(off_ven, m.ven, V) && cp(off_bv, m.bv, B * 8) && cp(off_ben, m.ben, B) &&
+                       cp(off_gl, m.glist, G * SEVC_MAXV * 4) && cp(off_gvl, m.gvlen, G * 4) &&
+                       cp(off_gen, m.gen, G) && cp(off_gty, m.gtype, G);
+            };
+            bool ok = record(s) && cuda_ok(cudaMemsetAsync(rec(k, off_nlog), 0, 4, s), "memset");
             if (!ok) { st = SEVC_ERR_CUDA; break; }
+            tp.after_nucleation = [&, record](cudaStream_t rs) { if (!record(rs)) sevc_set_error("tape copy"); };
             EventLog on = { (EventRec *)rec(k, off_log), (int *)rec(k, off_nlog), tp.log_cap }, off = { nullptr, nullptr, 0 };
             if (!cuda_ok(cudaMemcpyAsync(m.elog, &on, sizeof on, cudaMemcpyHostToDevice, s), "upload")) {
                 st = SEVC_ERR_CUDA;
                 break;
             }
             st = sevc_step(h, nullptr);
+            tp.after_nucleation = nullptr;
+            h->force_direct = false;
             if (!cuda_ok(cudaMemcpyAsync(m.elog, &off, sizeof off, cudaMemcpyHostToDevice, s), "upload"))
                 st = SEVC_ERR_CUDA;
             if (!st && !(d2d(rec(k, off_vel1), m.vel, V * 16) && d2d(rec(k, off_ven1), m.ven, V))) st = SEVC_ERR_CUDA;
@@ -1450,12 +1466,16 @@ sevc_status sevc_adjoint_histogram(sevc_handle *h, int nbins, double amax, const
             view.glist = (int *)rec(k, off_gl);
             view.gvlen = (int *)rec(k, off_gvl);
             view.gen = (uint8_t *)rec(k, off_gen);
+            view.gtype = (uint8_t *)rec(k, off_gty);
+            view.gse = tp.separam;           /* a nucleated grain's 0 is applied by its type */
             launch_adjoint_step(view, a, h->opt.dt, h->p.mu, h->opt.GB_eps, h->opt.GB_scaling,
                                 (const EventRec *)rec(k, off_log), (const int *)rec(k, off_nlog),
                                 (const uint8_t *)rec(k, off_ven1), (const double2 *)rec(k, off_vel1), s);
         }
     }
     tp.replaying = false;
+    tp.after_nucleation = nullptr;
+    h->force_direct = false;
     if (!d2d(h->dblock, fin, h->dbytes)) st = SEVC_ERR_CUDA;
     load_run(h, rfin);
     launch_sum_ordered(a.gmu, (int)V, a.scalars, s);

@@ -135,11 +135,9 @@ void launch_label_3sided_auto(const DevMesh &m, const DevScratch &x, double dt, 
 void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool bucket, cudaStream_t s);
 void launch_remove_grains(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s);
 /* clears the candidate flag of every listed grain (after the removals) */
-void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cudaStream_t s);
-void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s);
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s);
-void launch_fix_lists(const DevMesh &m, cudaStream_t s);
+void launch_fix_lists(const DevMesh &m, cudaStream_t s, bool queue_areas = true);
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s);
 
 /* check_data on the device (sevc_check.cu): violations counted into *out */

@@ -278,7 +278,8 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     int4 sb = m.vb[v];
     double AL[3] = { m.blen[sb.x], m.blen[sb.y], m.blen[sb.z] };
     double mn = AL[0];
-    for (int i = 0; i < 3; i++) if (mn > AL[i]) mn = AL[i];   /* min(), src/geometry.h:116 */
+    int imin = 0;
+    for (int i = 0; i < 3; i++) if (mn > AL[i]) { mn = AL[i]; imin = i; }   /* min(), src/geometry.h:116 */
     double nucl_r = 0.8 * mn * u1 + 0.1;
     double nucl_ori = 2 * M_PI * u2;
     NuclGeo o0, o1;
@@ -317,6 +318,14 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
      * energy changes */
     NuclGeo o;
     if (gen_triangle(m, A, nucl_r, nucl_ori, scaling, eps, true, o)) { raise_err(m, ERRB_TOPOLOGY); return; }
+    {   /* the triangle's position map, for an adjoint replay */
+        EventRec r0, r1;
+        r0.type = EV_NUCL; r0.a = A; r0.b = B; r0.c = C;
+        r0.pa = m.pos[A]; r0.pb = m.pos[o.D]; r0.pc = m.pos[o.E];
+        r1.type = EV_NUCL_AUX; r1.a = o.D; r1.b = o.E; r1.c = o.F;
+        r1.pa = m.pos[o.F]; r1.pb = make_double2(0.8 * u1, nucl_r); r1.pc = make_double2(imin, 0.0);
+        log_event_pair(m, r0, r1);
+    }
     init_vertex_dev(m, B, o.Bpos);
     init_vertex_dev(m, C, o.Cpos);
     m.pos[A] = o.Apos;

@@ -428,21 +428,20 @@ __device__ void conflict_check_one(const DevMesh &m, int b)
     }
 }
 /* check_conflictive_boundaries for every non-candidate boundary adjacent
- * to a candidate (the only ones it can mark) */
+ * to a candidate (the only ones it can mark); one thread per candidate and
+ * slot of its ends, so the six neighbours' load chains run side by side
+ * (every visit of a boundary writes the same winner) */
 __global__ void k_conflict_check(DevMesh m, const int *list, const int *n)
 {
     griddep_wait();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+    const int total = 6 * *n;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        int i = t / 6, r = t - 6 * i;
         int c = list[i];
         if (!(m.ben[c] && m.bcand[c])) continue;
         int2 e = m.bv[c];
-        for (int k = 0; k < 2; k++) {
-            int4 s = m.vb[k == 0 ? e.x : e.y];
-            for (int j = 0; j < 3; j++) {
-                int b = slot3(s, j);
-                if (b != c) conflict_check_one(m, b);
-            }
-        }
+        int b = slot3(m.vb[r < 3 ? e.x : e.y], r < 3 ? r : r - 3);
+        if (b != c) conflict_check_one(m, b);
     }
 }
 __global__ void k_conflict_unlabel(DevMesh m, const int *list, const int *n)
@@ -653,7 +652,7 @@ __global__ void k_label_3sided(DevMesh m, double dt)
 /* The same when no list changed since this step's side-count order: only
  * the grains of its 3-sided bucket are visited.  Every other enabled grain
  * already has gcand = 0, because each step clears the flag of every grain
- * it listed as a candidate (k_clear_grain_cand). */
+ * it listed as a candidate (k_remove_reserve). */
 __global__ void k_label_3sided_bucket(DevMesh m, double dt, const int *perm, const int *vbucket)
 {
     griddep_wait();
@@ -703,11 +702,6 @@ __global__ void k_tt_cond(cudaGraphConditionalHandle hnd, const int *n, int *pas
     if (threadIdx.x) return;
     int p = ++*pass;
     cudaGraphSetConditional(hnd, (*n > 0 && p < TWO_THREE_PASSES) ? 1u : 0u);
-}
-__global__ void k_clear_grain_cand(DevMesh m, const int *list, const int *n)
-{
-    griddep_wait();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) m.gcand[list[i]] = 0;
 }
 
 /* remove_grain (:687-822) */
@@ -817,18 +811,63 @@ __device__ __forceinline__ bool valid_v(const DevMesh &m, int v) { return (unsig
 __device__ __forceinline__ bool valid_b(const DevMesh &m, int b) { return (unsigned)b < (unsigned)m.nb; }
 __device__ __forceinline__ bool valid_g(const DevMesh &m, int g) { return (unsigned)g < (unsigned)m.ng; }
 
-/* reserve vertex v and the boundaries in its slots; settle the dA/dt of
- * its grains */
-__device__ void reserve_vertex(const DevMesh &m, const DevScratch &x, int v, unsigned long long key)
+/* An event's warp reserves its vertices and the boundaries in their slots
+ * (lane 3j + k: vertex j, slot k) and settles the dA/dt of every grain
+ * around them, one grain per lane (a grain an earlier lane also sees is
+ * left to that lane), so the settling runs side by side instead of one
+ * grain after another.  With `internal`, the extinction times of the
+ * boundaries joining two of the event's vertices (the ones a 3-sided
+ * removal disables) are settled too, each by the lane at its first end.
+ * Settling reads only the step's starting values, which nothing changes
+ * before the events apply, and is idempotent (an event that defers and
+ * then finds other boundaries settles those itself).  Warp-uniform
+ * arguments; every lane calls it. */
+__device__ void reserve_warp(const DevMesh &m, const DevScratch &x, const int *verts, int nverts,
+                             unsigned long long key, int lane, bool internal)
 {
-    atomicMin(x.vown + v, key);
-    int4 s = m.vb[v], g = m.vg[v];
-    for (int j = 0; j < 3; j++) {
-        int b = slot3(s, j);
-        if (valid_b(m, b)) atomicMin(x.bown + b, key);
-        int h = slot3(g, j);
-        if (valid_g(m, h)) finalize_grain(m, h);
+    int j = lane / 3, k = lane - 3 * j, h = -1;
+    if (lane < 3 * nverts) {
+        int v = verts[j];
+        if (valid_v(m, v)) {
+            if (k == 0) atomicMin(x.vown + v, key);
+            int b = slot3(m.vb[v], k);
+            if (valid_b(m, b)) {
+                atomicMin(x.bown + b, key);
+                if (internal) {
+                    int2 e = m.bv[b];
+                    bool in = false;
+                    for (int q = 0; q < nverts; q++) in |= verts[q] != v && (verts[q] == e.x || verts[q] == e.y);
+                    if (in && e.x == v) finalize_boundary(m, b);
+                }
+            }
+            h = slot3(m.vg[v], k);
+            if (!valid_g(m, h)) h = -1;
+        }
     }
+    bool first = h >= 0;
+    for (int q = 0; q < 9; q++) {
+        int hq = __shfl_sync(0xffffffffu, h, q);
+        if (q < lane && hq == h) first = false;
+    }
+    if (first) finalize_grain(m, h);
+}
+/* the records an event's single-thread code reads, brought into L1 by
+ * the warp in two parallel rounds: the vertices' own records, then the
+ * boundaries in their slots and the grains around them */
+__device__ __forceinline__ void l1_touch(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ void prefetch_event(const DevMesh &m, const int *verts, int nverts, int lane)
+{
+    int j = lane / 3, k = lane - 3 * j;
+    if (lane >= 3 * nverts) return;
+    int v = verts[j];
+    if (!valid_v(m, v)) return;
+    if (k == 0) {
+        l1_touch(m.pos + v); l1_touch(m.vel + v); l1_touch(m.vstamp + v); l1_touch(m.pos0 + v);
+        l1_touch(m.vmod + 4 * (size_t)v); l1_touch(m.vmodmark + v);
+    }
+    int b = slot3(m.vb[v], k), h = slot3(m.vg[v], k);
+    if (valid_b(m, b)) { l1_touch(m.bv + b); l1_touch(m.bstamp + b); l1_touch(m.bexact + b); l1_touch(m.ben + b); }
+    if (valid_g(m, h)) { l1_touch(m.gfix + h); l1_touch(m.gexact + h); l1_touch(m.gvlen + h); }
 }
 /* whether v and every boundary in its slots hold key; nothing but the
  * event holding v writes its slots, so they are the reserved ones */
@@ -845,40 +884,58 @@ __device__ bool holds_vertex(const DevMesh &m, const DevScratch &x, int v, unsig
 
 /* 3-sided removals (remove_grains, :994): a listed grain that is enabled
  * and a candidate is removed; a removal disables only its own grain, so
- * the set is known up front */
+ * the set is known up front.  One warp per listed grain, which also
+ * clears the grain's candidate flag (src/main.cu:260; nothing after this
+ * test reads it this step). */
 __global__ void k_remove_reserve(DevMesh m, DevScratch x, const int *list, const int *n)
 {
     griddep_wait();
     const unsigned ep = 2u * *m.stamp;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < *n; i += nw) {
         int g = list[i];
-        if (!(m.gen[g] && m.gcand[g])) continue;
+        bool rm = m.gen[g] && m.gcand[g];
+        __syncwarp();
+        if (lane == 0) m.gcand[g] = 0;
+        if (!rm) continue;
         const int *L = m.glist + (size_t)SEVC_MAXV * g;
-        unsigned long long key = resv_key(ep, i);
-        for (int k = 0; k < 3; k++)
-            if (valid_v(m, L[k])) reserve_vertex(m, x, L[k], key);
-        int p = atomicAdd(x.n_ehits, 1);
-        x.ehits[p] = i;
+        int verts[3] = { L[0], L[1], L[2] };
+        reserve_warp(m, x, verts, 3, resv_key(ep, i), lane, true);
+        if (lane == 0) {
+            int p = atomicAdd(x.n_ehits, 1);
+            x.ehits[p] = i;
+        }
     }
 }
+/* one warp per removal: its records are brought into L1, then lane 0
+ * applies it (or defers it when an earlier removal holds a record) */
 __global__ void k_remove_apply(DevMesh m, DevScratch x, const int *list)
 {
     griddep_wait();
     const unsigned ep = 2u * *m.stamp;
     const int nh = *x.n_ehits;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nh; t += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nh; t += nw) {
         int i = x.ehits[t], g = list[i];
         const int *L = m.glist + (size_t)SEVC_MAXV * g;
+        int verts[3] = { L[0], L[1], L[2] };
         unsigned long long key = resv_key(ep, i);
         bool own = true;
-        for (int k = 0; k < 3 && own; k++) own = valid_v(m, L[k]) && holds_vertex(m, x, L[k], key);
-        if (own) {
-            remove_grain_dev(m, g);
-            atomicAdd(&m.evt[EVT_COUNT * m.ginst[g] + EVT_REMOVALS], 1);
-        } else {
-            x.edefer[i] = 1;
-            atomicAdd(&x.ndefer[m.ginst[g]], 1);
+        if (lane == 0)
+            for (int k = 0; k < 3 && own; k++) own = valid_v(m, verts[k]) && holds_vertex(m, x, verts[k], key);
+        own = __shfl_sync(0xffffffffu, own, 0);
+        if (own) prefetch_event(m, verts, 3, lane);
+        __syncwarp();
+        if (lane == 0) {
+            if (own) {
+                remove_grain_dev(m, g);
+                atomicAdd(&m.evt[EVT_COUNT * m.ginst[g] + EVT_REMOVALS], 1);
+            } else {
+                x.edefer[i] = 1;
+                atomicAdd(&x.ndefer[m.ginst[g]], 1);
+            }
         }
+        __syncwarp();
     }
 }
 /* one warp per instance: its deferred removals in list order */
@@ -907,18 +964,22 @@ __global__ void k_remove_deferred(DevMesh m, DevScratch x, const int *list, cons
     if (lane == 0) x.ndefer[inst] = 0;
 }
 
-/* unlabel_boundaries_st2 (:588-606) */
-__global__ void k_unlabel_st2(DevMesh m, const int *list, const int *n)
+/* unlabel_boundaries_st2 (:588-606) for an enabled candidate b: it stays
+ * a candidate unless a grain on either side has 3 sides.  It reads and
+ * writes only b's own flags, so it runs inside the flip reservation (one
+ * warp per candidate, warp-uniform result). */
+__device__ bool unlabel_st2_keeps(const DevMesh &m, int b)
 {
-    griddep_wait();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
-        int b = list[i];
-        if (!(m.ben[b] && m.bcand[b])) continue;
-        int2 e = m.bv[b];
-        int gic[2];
-        if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) { raise_err(m, ERRB_TOPOLOGY); continue; }
-        if (m.gvlen[gic[0]] == 3 || m.gvlen[gic[1]] == 3) m.bcand[b] = 0;
+    int2 e = m.bv[b];
+    int gic[2];
+    if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) {       /* the step fails */
+        if ((threadIdx.x & 31) == 0) raise_err(m, ERRB_TOPOLOGY);
+        return false;
     }
+    bool keep = !(m.gvlen[gic[0]] == 3 || m.gvlen[gic[1]] == 3);
+    __syncwarp();
+    if (!keep && (threadIdx.x & 31) == 0) m.bcand[b] = 0;
+    return keep;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1183,15 +1244,18 @@ __global__ void k_flip_reserve(DevMesh m, DevScratch x, const int *list, const i
 {
     griddep_wait();
     const unsigned ep = 2u * *m.stamp + 1u;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < *n; i += nw) {
         int b = list[i];
         if (!(m.ben[b] && m.bcand[b])) continue;
+        if (!unlabel_st2_keeps(m, b)) continue;
         int2 e = m.bv[b];
-        unsigned long long key = resv_key(ep, i);
-        if (valid_v(m, e.x)) reserve_vertex(m, x, e.x, key);
-        if (valid_v(m, e.y)) reserve_vertex(m, x, e.y, key);
-        int p = atomicAdd(x.n_ehits, 1);
-        x.ehits[p] = i;
+        int verts[2] = { e.x, e.y };
+        reserve_warp(m, x, verts, 2, resv_key(ep, i), lane, false);
+        if (lane == 0) {
+            int p = atomicAdd(x.n_ehits, 1);
+            x.ehits[p] = i;
+        }
     }
 }
 /* one warp per flip: lanes prefetch its neighbourhood and derive the
@@ -1283,48 +1347,124 @@ __global__ void __launch_bounds__(FLIP_TPB) k_flip_deferred(DevMesh m, DevScratc
  * (src/topological.h:1035-1148) for one queued grain.  The reference runs
  * each over all grains before the next; an edit only touches its own
  * grain's list and only reads the mods, which nothing writes meanwhile, so
- * running the three for one grain back to back gives the same lists. */
-__device__ void fix_grain(const DevMesh &m, int g)
+ * running the three for one grain back to back gives the same lists.
+ *
+ * One warp per grain.  The lanes copy the list to shared memory and read
+ * the four mod slots of every listed vertex at once, recording for each
+ * entry whether one of them is an ADD, REMOVE or REPLACE for this grain;
+ * lane 0 then runs the three passes exactly as written (same visiting
+ * order, same first-match searches, same shifts and -1 fills) on the
+ * shared copy, reading the mods again only for the entries that hold an
+ * edit (and the flags of a vertex an edit brings into the list), and the
+ * lanes write back every entry the passes touched.  The long chain of
+ * dependent global reads of one thread per grain becomes one parallel
+ * round and a few L1 hits. */
+constexpr int FIX_TPB = 256, FIX_WARPS = FIX_TPB / 32;
+__device__ __forceinline__ unsigned mod_ops_for(const DevMesh &m, int v, int g)
 {
-    int *L = m.glist + (size_t)SEVC_MAXV * g;
-    for (int i = 0; i < m.gvlen[g]; i++) {               /* ADD */
-        int v = L[i];
+    if ((unsigned)v >= (unsigned)m.nv) return 0;
+    const int4 *md = m.vmod + 4 * (size_t)v;
+    unsigned f = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        int4 x = md[j];
+        if (x.x == g) f |= x.w == FIX_ADD ? 1u : x.w == FIX_REMOVE ? 2u : x.w == FIX_REPLACE ? 4u : 0u;
+    }
+    return f;
+}
+__device__ void fix_grain_serial(const DevMesh &m, int g, int *Ls, unsigned char *Fs, int *Ss, unsigned char *SFs,
+                                 int &n, int &hi)
+{
+    for (int i = 0; i < n; i++) {                        /* ADD */
+        if (!(Fs[i] & 1u)) continue;
+        const int v = Ls[i];
         for (int j = 0; j < 4; j++) {
             int4 md = m.vmod[4 * (size_t)v + j];
-            if (md.w == FIX_ADD && md.x == g) glist_add_after(m, g, md.y, md.z);
+            if (!(md.w == FIX_ADD && md.x == g)) continue;
+            int pos = -1;                                /* glist_add_after(g, md.y, md.z) */
+            for (int k = 0; k < n; k++)
+                if (Ls[k] == md.z) { pos = k + 1; break; }
+            if (pos < 0) { raise_err(m, ERRB_TOPOLOGY); continue; }
+            if (n >= SEVC_MAXV) { raise_err(m, ERRB_CAPACITY); continue; }
+            for (int k = n; k > pos; k--) { Ls[k] = Ls[k - 1]; Fs[k] = Fs[k - 1]; }
+            Ls[pos] = md.y;
+            Fs[pos] = (unsigned char)mod_ops_for(m, md.y, g);
+            n++;
+            hi = n > hi ? n : hi;
         }
     }
-    {                                                    /* REMOVE */
-        int snap[SEVC_MAXV];   /* the list as it was when the mod buffer was filled (:1088-1097) */
-        int n0 = m.gvlen[g];
-        for (int i = 0; i < n0; i++) snap[i] = L[i];
-        for (int i = 0; i < n0; i++)
-            for (int j = 0; j < 4; j++) {
-                int4 md = m.vmod[4 * (size_t)snap[i] + j];
-                if (md.w == FIX_REMOVE && md.x == g) glist_remove(m, g, md.y);
-            }
-    }
-    for (int i = 0; i < m.gvlen[g]; i++) {               /* REPLACE */
-        int v = L[i];
+    const int n0 = n;                                    /* REMOVE over the list as it stood */
+    for (int i = 0; i < n0; i++) { Ss[i] = Ls[i]; SFs[i] = Fs[i]; }
+    for (int i = 0; i < n0; i++) {
+        if (!(SFs[i] & 2u)) continue;
+        const int v = Ss[i];
         for (int j = 0; j < 4; j++) {
             int4 md = m.vmod[4 * (size_t)v + j];
-            if (md.w == FIX_REPLACE && md.x == g) glist_replace(m, g, md.z, md.y);
+            if (!(md.w == FIX_REMOVE && md.x == g)) continue;
+            for (int k = 0; k < n; k++)                  /* glist_remove(g, md.y) */
+                if (Ls[k] == md.y) {
+                    for (int q = k; q < n - 1; q++) { Ls[q] = Ls[q + 1]; Fs[q] = Fs[q + 1]; }
+                    n--;
+                    Ls[n] = -1;
+                    Fs[n] = 0;
+                    break;
+                }
+        }
+    }
+    for (int i = 0; i < n; i++) {                        /* REPLACE */
+        if (!(Fs[i] & 4u)) continue;
+        const int v = Ls[i];
+        for (int j = 0; j < 4; j++) {
+            int4 md = m.vmod[4 * (size_t)v + j];
+            if (!(md.w == FIX_REPLACE && md.x == g)) continue;
+            for (int k = 0; k < n; k++)                  /* glist_replace(g, md.z, md.y) */
+                if (Ls[k] == md.z) {
+                    Ls[k] = md.y;
+                    Fs[k] = (unsigned char)mod_ops_for(m, md.y, g);
+                    break;
+                }
         }
     }
 }
-__global__ void k_fix_edit(DevMesh m)
+__global__ void __launch_bounds__(FIX_TPB) k_fix_edit(DevMesh m)
 {
     griddep_wait();
-    int nf = min(*m.nfix, m.fixcap);
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nf; w += gridDim.x * blockDim.x) {
-        int g = m.fixlist[w];
-        if (m.gen[g] && m.gfix[g]) fix_grain(m, g);
+    __shared__ int Ls[FIX_WARPS][SEVC_MAXV], Ss[FIX_WARPS][SEVC_MAXV];
+    __shared__ unsigned char Fs[FIX_WARPS][SEVC_MAXV], SFs[FIX_WARPS][SEVC_MAXV];
+    __shared__ int Nw[FIX_WARPS][2];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nf = min(*m.nfix, m.fixcap), nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nf; w += nw) {
+        const int g = m.fixlist[w];
+        if (!(m.gen[g] && m.gfix[g])) continue;
+        int *L = m.glist + (size_t)SEVC_MAXV * g;
+        const int n = m.gvlen[g];
+        for (int i = lane; i < n; i += 32) {
+            int v = L[i];
+            Ls[wib][i] = v;
+            Fs[wib][i] = (unsigned char)mod_ops_for(m, v, g);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int nn = n, hi = n;
+            fix_grain_serial(m, g, Ls[wib], Fs[wib], Ss[wib], SFs[wib], nn, hi);
+            Nw[wib][0] = nn;
+            Nw[wib][1] = hi;
+            if (nn != n) m.gvlen[g] = nn;
+        }
+        __syncwarp();
+        const int hi = Nw[wib][1];
+        for (int i = lane; i < hi; i += 32) L[i] = Ls[wib][i];
+        __syncwarp();
     }
 }
 /* clear_grains_fix_state (:1150-1163): fix = false for enabled grains and
  * reset the mods of every vertex listed by an enabled grain.  Only queued
- * grains can have fix set and only marked vertices can hold mods. */
-__global__ void k_fix_clear(DevMesh m)
+ * grains can have fix set and only marked vertices can hold mods.
+ * queue_areas: the edited grains' areas are recomputed before the step's
+ * counts (after the removals' fix-up; the flips' fix-up comes after the
+ * counts, and the next step's grain pass computes every area). */
+__global__ void k_fix_clear(DevMesh m, int queue_areas)
 {
     griddep_wait();
     int nf = min(*m.nfix, m.fixcap), nm = min(*m.nmod, m.modcap);
@@ -1332,7 +1472,7 @@ __global__ void k_fix_clear(DevMesh m)
         int g = m.fixlist[w];
         if (m.gen[g]) {
             m.gfix[g] = 0;
-            if (!m.gadirty[g]) {              /* its area must be recomputed */
+            if (queue_areas && !m.gadirty[g]) {   /* its area must be recomputed */
                 m.gadirty[g] = 1;
                 int i = atomicAdd(m.nadirty, 1);
                 if (i < m.ng) m.adirty[i] = g; else raise_err(m, ERRB_WORKLIST);
@@ -1476,37 +1616,27 @@ void launch_label_3sided(const DevMesh &m, const DevScratch &x, double dt, bool 
         launch_dep(k_label_3sided, (m.ng + TPB - 1) / TPB, TPB, s, m, dt);
     }
 }
-void launch_clear_grain_cand(const DevMesh &m, const int *list, const int *n, cudaStream_t s)
-{
-    launch_dep(k_clear_grain_cand, 32, TPB, s, m, list, n);
-}
 
 void launch_remove_grains(const DevMesh &m, const DevScratch &x, const int *list, const int *n, cudaStream_t s)
 {
-    int g = listgrid(m.ng);
-    launch_dep(k_remove_reserve, g, TPB, s, m, x, list, n);
-    launch_dep(k_remove_apply, g, TPB, s, m, x, list);
+    launch_dep(k_remove_reserve, 4 * WL_BLOCKS, TPB, s, m, x, list, n);
+    launch_dep(k_remove_apply, 4 * WL_BLOCKS, TPB, s, m, x, list);
     launch_dep(k_remove_deferred, (m.ninst + 3) / 4, 128, s, m, x, list, n);
 }
 
-void launch_unlabel_st2(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
-{
-    launch_dep(k_unlabel_st2, listgrid(m.nb), TPB, s, m, cand, ncand);
-}
 
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s)
 {
-    int g = listgrid(m.nb);
-    launch_dep(k_flip_reserve, g, TPB, s, m, x, cand, ncand);
+    launch_dep(k_flip_reserve, 4 * WL_BLOCKS, TPB, s, m, x, cand, ncand);
     launch_dep(k_flip_apply, 4 * WL_BLOCKS, TPB, s, m, x, eps, cand);
     launch_dep(k_flip_deferred, m.ninst, FLIP_TPB, s, m, x, eps, cand, ncand);
 }
 
-void launch_fix_lists(const DevMesh &m, cudaStream_t s)
+void launch_fix_lists(const DevMesh &m, cudaStream_t s, bool queue_areas)
 {
-    launch_dep(k_fix_edit, WL_BLOCKS, TPB, s, m);
-    launch_dep(k_fix_clear, WL_BLOCKS, TPB, s, m);
+    launch_dep(k_fix_edit, WL_BLOCKS, FIX_TPB, s, m);
+    launch_dep(k_fix_clear, WL_BLOCKS, TPB, s, m, (int)queue_areas);
 }
 
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s)

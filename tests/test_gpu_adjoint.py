@@ -157,3 +157,114 @@ def test_torch_function_gradients(gpu):
     e.close()
     assert np.allclose(se.grad.numpy(), gse, rtol=1e-12, atol=0)
     assert np.isclose(float(gam.grad), ggam, rtol=1e-12) and np.isclose(float(mu.grad), gmu, rtol=1e-12)
+
+
+def nucleation_window(gpu, tmp_path, dt_window=1e-3, before=1, after=2):
+    """The 300-grain fixture with its triangular stored energies (3..6;
+    grains about one unit across, where the Metropolis test accepts
+    nucleations), run at dt 4e-3 until 1/6 of the grains are gone (the gate
+    for nucleation attempts), then at dt_window with one attempt per step
+    until an attempt is accepted.  Returns the options, the mesh and a
+    checkpoint `before` + 1 steps ahead of the accepted one: a window of
+    before + 1 + after steps from it moves the vertices, nucleates, and
+    moves them again."""
+    import os
+    import configs
+    import meshgen
+    d = os.path.join(configs.MESH_DIR, "m300")
+    mesh = meshgen.read_files(*[os.path.join(d, f) for f in ("vertices.txt", "ridges.txt", "oris.txt",
+                                                              "se_triangular.txt")])
+    n = 300
+
+    def opts(dt):
+        o = gpu.default_options(n_grains=n, dt=dt, dtau=dt, domain_bound=17.0, GB_eps=0.0, GB_scaling=1.0,
+                                SE_eps=1.0, SE_min=999.0, SE_max=999.0, do_nucleation=1, MC_k=3.0,
+                                nmax=10 ** 8, tmax=-1, snap_gap=10 ** 8, n_blocks=32, n_threads=256)
+        o.min_grains = -1
+        return o
+    e = gpu.Engine.from_arrays(opts(4e-3), mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    for _ in range(2000):
+        if e.step().curr_n_grains <= 5 * n // 6:
+            break
+    gate = str(tmp_path / "gate.ckpt")
+    e.checkpoint_save(gate)
+    e.close()
+    o = opts(dt_window)
+    e = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    e.checkpoint_load(gate)
+    ring = [str(tmp_path / ("w%d.ckpt" % i)) for i in range(before + 2)]
+    for k in range(4000):
+        e.checkpoint_save(ring[k % len(ring)])
+        if e.step().n_nucleations > 0 and k > before:
+            e.close()
+            return o, mesh, ring[(k - before) % len(ring)], before + 1 + after
+    pytest.fail("no nucleation accepted within 4000 steps past the gate")
+
+
+def test_adjoint_matches_central_differences_through_nucleation(gpu, tmp_path):
+    """A window around an accepted nucleation (nucleation_window): the
+    adjoint follows the inserted triangle's position map (the new corners
+    A + 0.99 r u, r = 0.8 U |A - X*| + 0.1 with the replayed draw U) back to
+    the positions the step before moved.  Central differences of the GPU
+    forward over the same window (every run starts from the checkpoint; the
+    perturbed runs are checked to take the same events, the nucleation site
+    included) agree within 1e-6 relative for the mobility, the boundary
+    energy scale and a direction in the stored energies of the original
+    grains (a nucleated grain's stored energy is 0, not a parameter).
+    The forward's finite-difference velocity carries rounding noise of
+    ~1e-8 relative, so a difference quotient over a few steps is only good
+    to ~1e-8/h; h is 1e-2..1e-3, where the loss is still quadratic in the
+    parameters to far better than 1e-6 over so short a window."""
+    o, mesh, ckpt, window = nucleation_window(gpu, tmp_path)
+    probe = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    probe.checkpoint_load(ckpt)
+    st = probe.get_state()
+    probe.close()
+    n = len(st["gse"])
+    se0 = st["gse"].copy()
+    free = (st["gen"] > 0) & (st["gtype"] == 0)          # grains whose stored energy is a parameter
+
+    def run(se, gam, mu, every=None):
+        ee = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+        ee.checkpoint_load(ckpt)
+        ee.set_stored_energy(se)
+        ee.set_gb_scaling(gam)
+        ee.set_mobility(mu)
+        if every:
+            ee.tape_start(every)
+        ev = []
+        for _ in range(window):
+            i = ee.step()
+            ev.append((i.n_flips, i.n_removals, i.n_two_three, i.n_nucleations,
+                       i.nucleation_candidate if i.nucleation_attempted else -2))
+        return ee, ee.area_histogram(NB, AMAX), ev
+
+    e, h, events = run(se0, 1.0, 1.0, every=2)
+    assert [x[3] for x in events][1] == 1 and sum(x[3] for x in events) >= 1, events
+    e2, target, _ = run(np.where(free, se0 * 1.05, se0), 1.05, 0.95)
+    e2.close()
+    gse, ggam, gmu = e.adjoint_histogram(NB, AMAX, dloss(h, target))
+    e.close()
+    dirn = np.where(free, np.random.default_rng(4).standard_normal(n), 0.0)
+    for which, adj in (("mu", gmu), ("gamma", ggam), ("se", float(gse @ dirn))):
+        errs = []
+        for hstep in (1e-2, 3e-3, 1e-3):
+            out = []
+            for sgn in (1.0, -1.0):
+                s_, g, m = se0.copy(), 1.0, 1.0
+                if which == "se":
+                    s_ = se0 + sgn * hstep * dirn
+                elif which == "gamma":
+                    g += sgn * hstep
+                else:
+                    m += sgn * hstep
+                ee, hh, ev = run(s_, g, m)
+                ee.close()
+                if ev != events:
+                    break
+                out.append(loss_of(hh, target))
+            if len(out) == 2:
+                fd = (out[0] - out[1]) / (2 * hstep)
+                errs.append((abs(adj - fd) / abs(fd), hstep, fd))
+        assert errs, "%s: every perturbed run changed the event sequence" % which
+        assert min(errs)[0] <= 1e-6, (which, adj, errs)
