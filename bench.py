@@ -259,7 +259,10 @@ def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=2e-3, s
     sqrt of the mean grain count), SE U[0,1).  nucleation (gap, MC_k): the
     window starts once every instance has passed its 5/6 gate, with stored
     energies triangular(3, 6, 6) (voronoi.py's, where the Metropolis test
-    accepts nucleations at this grain size)."""
+    accepts nucleations at this grain size; the motion is then ~10x faster
+    than with U[0,1), so dt is smaller to keep the window's removals to a
+    few per thousand grains, where the loss is smooth enough between
+    discrete events for gradient steps)."""
     import numpy as np
     import meshgen
     import calibrate
@@ -568,7 +571,8 @@ def run_engine(args):
                                         10, 3, cache=args.ensemble_cache)
     if args.adjoint_sample:
         line["adjoint"] = run_adjoint()
-        line["calibration"] = run_calibration()
+        line["calibration"] = run_calibration(n_inst=64, lo=20000, hi=20000, steps=40, iters=50, dt=1e-4,
+                                              nucleation=(5, 3.0))
     print(json.dumps(line))
 
 
@@ -643,7 +647,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--direct", action="store_true",
                     help="--workload window: launch every kernel directly (no CUDA graphs), for profilers")
-    ap.add_argument("--cal-dt", type=float, default=1e-3, help="--workload calibrate: time step")
+    ap.add_argument("--cal-dt", type=float, default=1e-4, help="--workload calibrate: time step")
     ap.add_argument("--ckpt", default=None, help="--workload window: checkpoint file past the gate (made if absent)")
     ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate", "small", "window"],
                     help="ensemble: batched ensemble against sequential plain runs; calibrate: 64 x 20,000-grain "

@@ -135,3 +135,49 @@ def loss_and_grads(st, se0, gamma0, mu0, dt, steps, D, nbins, amax, target):
     loss = ((h - torch.as_tensor(target)) ** 2).mean()
     loss.backward()
     return float(loss.detach()), se.grad.numpy(), float(gamma.grad), float(mu.grad), h.detach().numpy()
+
+
+def nucleation_map(x, rec, D):
+    """Positions after a nucleation at vertex A (nucleation2.cu:116-212 with
+    the move of nucleate, :474-676): the new corners A, B, C sit at
+    A + 0.99 r (X - A)/|X - A| for A's far ends X = D, E, F, with
+    r = k |X* - A| + 0.1 (X* the end of A's shortest boundary, k = 0.8 U
+    for the recorded draw U).  rec: A, B, C, far (D, E, F), xstar, k."""
+    pa = x[rec["A"]]
+    ds = _wrap(x[rec["xstar"]] - pa, D)
+    r = rec["k"] * torch.sqrt((ds ** 2).sum()) + 0.1
+    out = []
+    for X in rec["far"]:
+        t = _wrap(x[X] - pa, D)
+        out.append(torch.remainder(pa + 0.99 * r * t / torch.sqrt((t ** 2).sum()), D))
+    x = x.clone()
+    x[rec["A"]], x[rec["B"]], x[rec["C"]] = out[0], out[1], out[2]
+    return x
+
+
+def loss_and_grads_nucleation(st, nucl, se0, gamma0, mu0, dt, steps, D, nbins, amax, target):
+    """loss_and_grads for a window whose only topology changes are
+    nucleations: nucl maps a step index to a record (nucleation_map's
+    fields plus "state", a get_state() dict holding the mesh right after
+    that nucleation), applied before the step's velocities.  A grain of
+    nonzero type (nucleated) has stored energy 0, not a parameter."""
+    se = torch.tensor(se0, dtype=torch.float64, requires_grad=True)
+    gamma = torch.tensor(float(gamma0), dtype=torch.float64, requires_grad=True)
+    mu = torch.tensor(float(mu0), dtype=torch.float64, requires_grad=True)
+    x = torch.tensor(np.stack([st["px"], st["py"]], 1), dtype=torch.float64)
+
+    def setup(s):
+        return Topology(s), torch.tensor((s["gtype"] == 0).astype(np.float64))
+    topo, free = setup(st)
+    for k in range(steps):
+        if k in nucl:
+            x = nucleation_map(x, nucl[k], D)
+            topo, free = setup(nucl[k]["state"])
+        v = velocities(x, topo, se * free, gamma, mu, D)
+        V = topo.verts
+        x = x.clone()
+        x[V] = torch.remainder(x[V] + dt * v[V], D)
+    h = histogram(x, topo, D, nbins, amax)
+    loss = ((h - torch.as_tensor(target)) ** 2).mean()
+    loss.backward()
+    return float(loss.detach()), se.grad.numpy(), float(gamma.grad), float(mu.grad), h.detach().numpy()

@@ -175,45 +175,86 @@ __global__ void k_adj_translate(int nv, double dt, double mu, const double2 *lam
     gmu[i] += dt * (l.x * w.x + l.y * w.y) / mu;
 }
 
-/* events in reverse order (one thread: events of a step may share vertices) */
-__global__ void k_adj_events(double D, const EventRec *log, const int *nlog, double2 *lx)
+/* one logged flip or 3-sided removal, backward */
+__device__ void adj_event_one(double D, const EventRec &r, double2 *lx)
 {
-    for (int e = *nlog - 1; e >= 0; e--) {
-        EventRec r = log[e];
-        if (r.type == EV_FLIP) {                      /* both ends -> midpoint */
-            double2 a = lx[r.a], b = lx[r.b];
-            double2 s = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
-            lx[r.a] = s;
-            lx[r.b] = s;
-            continue;
-        }
-        if (r.type != EV_REMOVE) continue;            /* nucleations: k_adj_nucleation */
-        /* A' = A + F(u, w), u = B - A, w = C - A,
-         * F = (|w| u + |u| w) / (|u| + |w - u| + |w|) */
-        double2 lp = lx[r.a];
-        double ux = wrapd(r.pb.x, r.pa.x, D), uy = wrapd(r.pb.y, r.pa.y, D);
-        double wx = ux + wrapd(r.pc.x, r.pb.x, D), wy = uy + wrapd(r.pc.y, r.pb.y, D);
-        double nu = sqrt(ux * ux + uy * uy), nw = sqrt(wx * wx + wy * wy);
-        double rx = wx - ux, ry = wy - uy, nr = sqrt(rx * rx + ry * ry);
-        double S = nu + nr + nw;
-        double Nx = nw * ux + nu * wx, Ny = nw * uy + nu * wy;
-        double lN = lp.x * Nx + lp.y * Ny, lw = lp.x * wx + lp.y * wy, lu = lp.x * ux + lp.y * uy;
-        double hux = ux / nu, huy = uy / nu, hwx = wx / nw, hwy = wy / nw, hrx = rx / nr, hry = ry / nr;
-        if (nu == 0) { hux = 0; huy = 0; }            /* coincident vertices: zero subgradient */
-        if (nw == 0) { hwx = 0; hwy = 0; }
-        if (nr == 0) { hrx = 0; hry = 0; }
-        if (!(S > 0)) continue;                       /* degenerate triangle: the map is not moved */
-        double S2 = S * S;
-        /* J_u^T lambda' and J_w^T lambda' */
-        double jux = (nw * lp.x + lw * hux) / S - lN * (hux - hrx) / S2;
-        double juy = (nw * lp.y + lw * huy) / S - lN * (huy - hry) / S2;
-        double jwx = (lu * hwx + nu * lp.x) / S - lN * (hrx + hwx) / S2;
-        double jwy = (lu * hwy + nu * lp.y) / S - lN * (hry + hwy) / S2;
-        lx[r.a] = make_double2(lp.x - jux - jwx, lp.y - juy - jwy);
-        double2 b = lx[r.b], c = lx[r.c];
-        lx[r.b] = make_double2(b.x + jux, b.y + juy);
-        lx[r.c] = make_double2(c.x + jwx, c.y + jwy);
+    if (r.type == EV_FLIP) {                          /* both ends -> midpoint */
+        double2 a = lx[r.a], b = lx[r.b];
+        double2 s = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+        lx[r.a] = s;
+        lx[r.b] = s;
+        return;
     }
+    if (r.type != EV_REMOVE) return;                  /* nucleations: k_adj_nucleation */
+    /* A' = A + F(u, w), u = B - A, w = C - A,
+     * F = (|w| u + |u| w) / (|u| + |w - u| + |w|) */
+    double2 lp = lx[r.a];
+    double ux = wrapd(r.pb.x, r.pa.x, D), uy = wrapd(r.pb.y, r.pa.y, D);
+    double wx = ux + wrapd(r.pc.x, r.pb.x, D), wy = uy + wrapd(r.pc.y, r.pb.y, D);
+    double nu = sqrt(ux * ux + uy * uy), nw = sqrt(wx * wx + wy * wy);
+    double rx = wx - ux, ry = wy - uy, nr = sqrt(rx * rx + ry * ry);
+    double S = nu + nr + nw;
+    double Nx = nw * ux + nu * wx, Ny = nw * uy + nu * wy;
+    double lN = lp.x * Nx + lp.y * Ny, lw = lp.x * wx + lp.y * wy, lu = lp.x * ux + lp.y * uy;
+    double hux = ux / nu, huy = uy / nu, hwx = wx / nw, hwy = wy / nw, hrx = rx / nr, hry = ry / nr;
+    if (nu == 0) { hux = 0; huy = 0; }                /* coincident vertices: zero subgradient */
+    if (nw == 0) { hwx = 0; hwy = 0; }
+    if (nr == 0) { hrx = 0; hry = 0; }
+    if (!(S > 0)) return;                             /* degenerate triangle: the map is not moved */
+    double S2 = S * S;
+    /* J_u^T lambda' and J_w^T lambda' */
+    double jux = (nw * lp.x + lw * hux) / S - lN * (hux - hrx) / S2;
+    double juy = (nw * lp.y + lw * huy) / S - lN * (huy - hry) / S2;
+    double jwx = (lu * hwx + nu * lp.x) / S - lN * (hrx + hwx) / S2;
+    double jwy = (lu * hwy + nu * lp.y) / S - lN * (hry + hwy) / S2;
+    lx[r.a] = make_double2(lp.x - jux - jwx, lp.y - juy - jwy);
+    double2 b = lx[r.b], c = lx[r.c];
+    lx[r.b] = make_double2(b.x + jux, b.y + juy);
+    lx[r.c] = make_double2(c.x + jwx, c.y + jwy);
+}
+
+/* Walk the step's log from its end in chunks of ADJ_TPB records, one block
+ * per instance: the threads test a chunk at once (record kind and the
+ * instance of its first vertex) and thread 0 takes the hits in descending
+ * log order.  Events of different instances touch disjoint vertices, so
+ * the instances run side by side; within an instance the events keep the
+ * reverse of the order they were applied in (the log order: the parallel
+ * events, which share no vertex, then the deferred ones). */
+constexpr int ADJ_TPB = 256;
+template <class Want, class Take>
+__device__ void walk_log_reverse(const EventRec *log, int n, Want want, Take take)
+{
+    __shared__ unsigned hit[ADJ_TPB / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int top = n; top > 0; top -= ADJ_TPB) {
+        int e = top - 1 - (int)threadIdx.x;
+        bool f = e >= 0 && want(e);
+        unsigned w = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) hit[warp] = w;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int k = 0; k < ADJ_TPB / 32; k++)
+                for (unsigned h = hit[k]; h; h &= h - 1) take(top - 1 - (32 * k + __ffs(h) - 1));
+        __syncthreads();
+    }
+}
+__device__ __forceinline__ bool in_instance(const int *voff, int ninst, int inst, int v)
+{
+    return ninst <= 1 || (v >= voff[inst] && v < voff[inst + 1]);
+}
+
+/* the step's flips and 3-sided removals in reverse order, per instance */
+__global__ void __launch_bounds__(ADJ_TPB) k_adj_events(double D, const EventRec *log, const int *nlog, double2 *lx,
+                                                        const int *voff, int ninst)
+{
+    const int inst = blockIdx.x;
+    walk_log_reverse(
+        log, *nlog,
+        [&](int e) {
+            EventRec r = log[e];
+            return (r.type == EV_FLIP || r.type == EV_REMOVE) && in_instance(voff, ninst, inst, r.a);
+        },
+        [&](int e) { adj_event_one(D, log[e], lx); });
 }
 
 /* boundary weight f_j = gamma_j / s (k_boundary_geometry's definition) */
@@ -227,47 +268,55 @@ __device__ __forceinline__ double gb_weight(const DevMesh &m, int b, double eps)
 }
 
 /* the nucleations of the step, last first: lambda of the positions
- * before it from lambda after it (one thread).  For each new position
- * Y = A + c u_X (c = 0.99 r):
+ * before it from lambda after it (one block per instance, as
+ * k_adj_events).  For each new position Y = A + c u_X (c = 0.99 r):
  *   dY/dX = c (I - u u^T) / |d_X|,  dY/dA = I - dY/dX + u (dc/dA)^T,
  *   dc/dX* = 0.99 k u_X* = -dc/dA;
  * the new vertices B and C had no position before. */
-__global__ void k_adj_nucleation(double D, const EventRec *log, const int *nlog, double2 *lam)
+__device__ void adj_nucleation_one(double D, const EventRec &r, const EventRec &x, double2 *lam)
 {
-    for (int e = *nlog - 1; e >= 1; e--) {
-        EventRec r = log[e - 1], x = log[e];
-        if (r.type != EV_NUCL || x.type != EV_NUCL_AUX) continue;
-        int Y[3] = { r.a, r.b, r.c }, X[3] = { x.a, x.b, x.c };
-        double2 pa = r.pa, px[3] = { r.pb, r.pc, x.pa };
-        double k = x.pb.x, c = 0.99 * x.pb.y;
-        int is = (int)x.pc.x;
-        double2 ly[3] = { lam[Y[0]], lam[Y[1]], lam[Y[2]] };
-        double usx = wrapd(px[is].x, pa.x, D), usy = wrapd(px[is].y, pa.y, D);
-        double ns = sqrt(usx * usx + usy * usy);
-        usx = ns > 0 ? usx / ns : 0.0;
-        usy = ns > 0 ? usy / ns : 0.0;
-        double2 la = make_double2(0, 0);
-        double2 lstar = make_double2(0, 0);
-        for (int i = 0; i < 3; i++) {
-            double dx = wrapd(px[i].x, pa.x, D), dy = wrapd(px[i].y, pa.y, D), n = sqrt(dx * dx + dy * dy);
-            if (!(n > 0)) continue;
-            double ux = dx / n, uy = dy / n, l_u = ux * ly[i].x + uy * ly[i].y;
-            double gx = c / n * (ly[i].x - ux * l_u), gy = c / n * (ly[i].y - uy * l_u);
-            double t = 0.99 * k * l_u;
-            la.x += ly[i].x - gx - t * usx;
-            la.y += ly[i].y - gy - t * usy;
-            lam[X[i]].x += gx;
-            lam[X[i]].y += gy;
-            lstar.x += t * usx;
-            lstar.y += t * usy;
-        }
-        lam[X[is]].x += lstar.x;
-        lam[X[is]].y += lstar.y;
-        lam[Y[0]] = la;
-        lam[Y[1]] = make_double2(0, 0);
-        lam[Y[2]] = make_double2(0, 0);
-        e--;
+    int Y[3] = { r.a, r.b, r.c }, X[3] = { x.a, x.b, x.c };
+    double2 pa = r.pa, px[3] = { r.pb, r.pc, x.pa };
+    double k = x.pb.x, c = 0.99 * x.pb.y;
+    int is = (int)x.pc.x;
+    double2 ly[3] = { lam[Y[0]], lam[Y[1]], lam[Y[2]] };
+    double usx = wrapd(px[is].x, pa.x, D), usy = wrapd(px[is].y, pa.y, D);
+    double ns = sqrt(usx * usx + usy * usy);
+    usx = ns > 0 ? usx / ns : 0.0;
+    usy = ns > 0 ? usy / ns : 0.0;
+    double2 la = make_double2(0, 0);
+    double2 lstar = make_double2(0, 0);
+    for (int i = 0; i < 3; i++) {
+        double dx = wrapd(px[i].x, pa.x, D), dy = wrapd(px[i].y, pa.y, D), n = sqrt(dx * dx + dy * dy);
+        if (!(n > 0)) continue;
+        double ux = dx / n, uy = dy / n, l_u = ux * ly[i].x + uy * ly[i].y;
+        double gx = c / n * (ly[i].x - ux * l_u), gy = c / n * (ly[i].y - uy * l_u);
+        double t = 0.99 * k * l_u;
+        la.x += ly[i].x - gx - t * usx;
+        la.y += ly[i].y - gy - t * usy;
+        lam[X[i]].x += gx;
+        lam[X[i]].y += gy;
+        lstar.x += t * usx;
+        lstar.y += t * usy;
     }
+    lam[X[is]].x += lstar.x;
+    lam[X[is]].y += lstar.y;
+    lam[Y[0]] = la;
+    lam[Y[1]] = make_double2(0, 0);
+    lam[Y[2]] = make_double2(0, 0);
+}
+__global__ void __launch_bounds__(ADJ_TPB) k_adj_nucleation(double D, const EventRec *log, const int *nlog,
+                                                            double2 *lam, const int *voff, int ninst)
+{
+    const int inst = blockIdx.x, n = *nlog;
+    walk_log_reverse(
+        log, n,
+        [&](int e) {
+            if (e + 1 >= n) return false;
+            EventRec r = log[e];
+            return r.type == EV_NUCL && log[e + 1].type == EV_NUCL_AUX && in_instance(voff, ninst, inst, r.a);
+        },
+        [&](int e) { adj_nucleation_one(D, log[e], log[e + 1], lam); });
 }
 
 /* per grain: sign of the area at the step's start, and
@@ -487,11 +536,11 @@ void launch_adjoint_step(const DevMesh &rec, const AdjointBuffers &a, double dt,
     COUNT_LAUNCHES(1), k_adj_mark_events<<<4, TPB, 0, s>>>(a.mark, log, nlog);
     COUNT_LAUNCHES(1), k_adj_translate<<<nblk(rec.nv), TPB, 0, s>>>(rec.nv, dt, mu, a.lam, ven1, vel1, a.mark, a.lx,
                                                                     a.lv, a.gmu);
-    COUNT_LAUNCHES(1), k_adj_events<<<1, 1, 0, s>>>(rec.D, log, nlog, a.lx);
+    COUNT_LAUNCHES(1), k_adj_events<<<rec.ninst, ADJ_TPB, 0, s>>>(rec.D, log, nlog, a.lx, rec.voff, rec.ninst);
     COUNT_LAUNCHES(1), k_adj_grains<<<nblk(rec.ng), TPB, 0, s>>>(rec, mu, a.lv, a.sgn, a.gse);
     COUNT_LAUNCHES(1), k_adj_vertices<<<nblk(rec.nv), TPB, 0, s>>>(rec, mu, eps, s_gb, a.lx, a.lv, a.sgn, a.lam,
                                                                    a.ggam);
-    COUNT_LAUNCHES(1), k_adj_nucleation<<<1, 1, 0, s>>>(rec.D, log, nlog, a.lam);
+    COUNT_LAUNCHES(1), k_adj_nucleation<<<rec.ninst, ADJ_TPB, 0, s>>>(rec.D, log, nlog, a.lam, rec.voff, rec.ninst);
 }
 
 void launch_grain_stats(const DevMesh &m, int lo, int hi, double *out, cudaStream_t s)

@@ -46,6 +46,7 @@ struct DevMesh {
     double2 *pos, *vel;
     struct alignas(16) FdTerms { double bx, gx, by, gy; } *terms; /* energy terms of src/calculus.h:59-69 */
     double2 *contrib;    /* 3 per vertex: stored-energy FD term per grain slot */
+    float *vspd;         /* upper bound of |vx| + |vy| from the step's vertex pass */
     double *venergy;
     uint8_t *ven;
     int4 *vb, *vg;
@@ -654,6 +655,18 @@ __device__ __forceinline__ float f32_cut(double x)
     mag = e <= 896u ? 0u : mag;
     mag = e >= 1151u ? 0x7fc00000u : mag;
     return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
+/* Upper bound of |vx| + |vy| in binary32, on the integer and FP32 pipes:
+ * f32_cut(x) is within a factor (1 - 2^-23) of x for normal binary32
+ * magnitudes, so scaling it up by 1 + 2^-21 (rounded up) and adding the
+ * largest magnitude it maps to 0 covers |x|; non-finite and huge x give
+ * NaN or infinity, which no comparison passes. */
+__device__ __forceinline__ float speed_bound(double vx, double vy)
+{
+    float ax = fabsf(f32_cut(vx)), ay = fabsf(f32_cut(vy));
+    const float up = 1.0f + 0x1p-21f;
+    return __fadd_ru(__fadd_ru(__fmul_ru(ax, up), __fmul_ru(ay, up)), 0x1p-125f);
 }
 
 /* True when compute_t_ext (src/topological.h:303-334) of the boundary

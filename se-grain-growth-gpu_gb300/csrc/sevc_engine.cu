@@ -188,6 +188,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.summary, h->h_big_ints * 4 }, { (void **)&m.elog, sizeof(EventLog) },
         { (void **)&m.pos, V * 16 }, { (void **)&m.vel, V * 16 }, { (void **)&m.terms, V * 32 },
         { (void **)&m.contrib, V * 48 }, { (void **)&m.venergy, V * 8 }, { (void **)&m.ven, V },
+        { (void **)&m.vspd, V * 4 },
         { (void **)&m.vb, V * 16 }, { (void **)&m.vg, V * 16 }, { (void **)&m.vmod, V * 64 },
         { (void **)&m.voted, V * 4 }, { (void **)&m.vmodmark, V }, { (void **)&m.modlist, V * 4 },
         { (void **)&m.bv, B * 8 }, { (void **)&m.benergy, B * 8 }, { (void **)&m.blen, B * 8 },
@@ -203,7 +204,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.extra, I * EXTRA_CAP * 4 }, { (void **)&x.threadfail, I * grid * 4 },
         { (void **)&x.block_area, I * h->p.n_blocks * 8 }, { (void **)&x.counters, I * CTR_COUNT * 4 },
         { (void **)&x.rng, nrng * sizeof(curandState) }, { (void **)&x.rng_saved, nrng * sizeof(curandState) },
-        { (void **)&x.nucl_buf, I * 64 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
+        { (void **)&x.nucl_buf, I * 96 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
         { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
         { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
         { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.vstamp, V * 4 },

@@ -15,6 +15,8 @@
  */
 #include "sevc_internal.h"
 
+#include <cmath>
+
 namespace {
 
 constexpr int TPB = 256;
@@ -450,6 +452,7 @@ __global__ void k_vertex_fd(DevMesh m, double mu)
     }
     m.terms[v] = t;
     m.vel[v] = make_double2(vel[0], vel[1]);
+    m.vspd[v] = speed_bound(vel[0], vel[1]);
     double e = 0.0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
@@ -537,9 +540,19 @@ __device__ __forceinline__ void text_label_one(const DevMesh &m, int b, uint8_t 
 }
 /* Two boundaries per thread (b and b + blockDim.x of the block's pair of
  * tiles), every load of both issued before either is labelled: the pass
- * waits on two rounds of gathers, and twice the loads in flight per thread
- * hide more of that latency than the registers they cost. */
-__global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, const int *flags)
+ * waits on rounds of gathers, and twice the loads in flight per thread
+ * hide more of that latency than the registers they cost.
+ *
+ * Speed bound.  A candidate has 0 <= t_ext = -|d| / (u.(ve - vi)) <= dt
+ * (u = d/|d| through atan2/cos/sin, |u| <= 1 + 1e-15), so
+ * |d| <= dt (|vi|_1 + |ve|_1) (1 + 1e-14).  The vertex pass leaves an upper
+ * bound of each |v|_1 in binary32 (speed_bound); a boundary whose
+ * arclength this step (blen, the same |d| up to 1e-15) cut down to binary32
+ * exceeds dt_up (s_i + s_e), dt_up >= dt (1 + 1e-6), rounded up, is no
+ * candidate, and is labelled as the certificate labels one (without
+ * reading its ends' positions and velocities).  The others take the
+ * certificate and, if undecided, the exact value. */
+__global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float inv_dt, float dt_up, const int *flags)
 {
     griddep_wait();
     int b0 = 2 * blockIdx.x * blockDim.x + threadIdx.x;
@@ -553,14 +566,31 @@ __global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float in
         en[k] = in ? m.ben[b] : 0;
         e[k] = in ? m.bv[b] : make_int2(0, 0);   /* loaded beside the flag: one round trip less */
     }
+    bool far[2] = { false, false };
+    if (!full) {
+        float bl[2] = { 0.f, 0.f }, si[2] = { 0.f, 0.f }, se[2] = { 0.f, 0.f };
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+            if (en[k]) { bl[k] = f32_cut(m.blen[b0 + k * blockDim.x]); si[k] = m.vspd[e[k].x]; se[k] = m.vspd[e[k].y]; }
+#pragma unroll
+        for (int k = 0; k < 2; k++) far[k] = en[k] && bl[k] > __fmul_ru(__fadd_ru(si[k], se[k]), dt_up);
+    }
     double2 z = make_double2(0, 0), pi[2] = { z, z }, pe[2] = { z, z }, vi[2] = { z, z }, ve[2] = { z, z };
 #pragma unroll
     for (int k = 0; k < 2; k++)
-        if (en[k]) { pi[k] = m.pos[e[k].x]; pe[k] = m.pos[e[k].y]; vi[k] = m.vel[e[k].x]; ve[k] = m.vel[e[k].y]; }
+        if (en[k] && !far[k]) { pi[k] = m.pos[e[k].x]; pe[k] = m.pos[e[k].y]; vi[k] = m.vel[e[k].x]; ve[k] = m.vel[e[k].y]; }
 #pragma unroll
     for (int k = 0; k < 2; k++) {
         int b = b0 + k * blockDim.x;
-        if (b < m.nb) text_label_one(m, b, en[k], pi[k], pe[k], vi[k], ve[k], dt, Df, hDf, inv_dt, full);
+        if (b >= m.nb) continue;
+        if (far[k]) {
+            m.btext[b] = SEVC_MAX_T_EXT_D;       /* as text_label_one's certified skip */
+            m.bexact[b] = 0;
+            m.bcand[b] = 0;
+            m.bconf[b] = -1;
+        } else {
+            text_label_one(m, b, en[k], pi[k], pe[k], vi[k], ve[k], dt, Df, hDf, inv_dt, full);
+        }
     }
 }
 
@@ -745,7 +775,11 @@ void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const L
     /* binary32 copies for the certificate (text_outside_dt): rounded to
      * nearest, within 2^-24 of the binary64 values */
     float Df = (float)m.D, hDf = (float)(m.D / 2.0), inv_dt = (float)(1.0 / dt);
-    if (m.nb > 0) launch_dep(k_text_label, (m.nb + 2 * t - 1) / (2 * t), t, s, m, dt, Df, hDf, inv_dt, x.flags);
+    /* dt (1 + 1e-6) rounded up to binary32, for the speed bound */
+    float dt_up = std::nextafter((float)(dt * (1.0 + 1e-6)), INFINITY);
+    if ((double)dt_up < dt * (1.0 + 1e-6)) dt_up = std::nextafter(dt_up, INFINITY);
+    if (m.nb > 0)
+        launch_dep(k_text_label, (m.nb + 2 * t - 1) / (2 * t), t, s, m, dt, Df, hDf, inv_dt, dt_up, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)

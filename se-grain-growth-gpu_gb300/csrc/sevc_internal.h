@@ -24,7 +24,7 @@ struct DevScratch {
     double *block_area;              /* nucleated-area partial per block, per instance */
     int *counters;                   /* CTR_COUNT device counters per instance, see CTR_* */
     curandState *rng, *rng_saved;    /* 8192 cuRAND states + pre-attempt copy, per instance */
-    int *nucl_buf;                   /* 64 ints per instance: per-block pick and alive count */
+    int *nucl_buf;                   /* 96 ints per instance: per-block pick, alive count, pick's rank */
     int *nucl_on;                    /* per instance: attempt a nucleation this step */
     int *vbucket;                    /* 64 ints: side-count histogram + cursors */
     int *flags;                      /* 4 ints: the step's output decision, see launch_full_flag */

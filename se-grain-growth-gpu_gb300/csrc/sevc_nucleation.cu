@@ -27,6 +27,7 @@
 namespace {
 
 constexpr int NBLK = 32, NTHR = 256, GRID = NBLK * NTHR;
+constexpr int NUCL_BUF = 3 * NBLK;   /* per instance: each block's pick, alive count, pick's rank */
 
 __global__ void k_rng_init(curandState *st, int n)
 {
@@ -49,13 +50,15 @@ __global__ void k_rng_draw(curandState *st, int n, int ndraws, double *out)
 __global__ void __launch_bounds__(NTHR) k_nucl_blocks(DevMesh m, curandState *rng, curandState *saved, int *buf,
                                                      const int *nucl_on)
 {
-    __shared__ int alive[NTHR], pick[NTHR];
+    __shared__ int alive[NTHR], pick[NTHR], nst[NTHR], stot;
+    __shared__ double share[NTHR];
     int inst = blockIdx.y;
     if (!nucl_on[inst]) return;
     int vo = m.voff[inst], nvi = m.voff[inst + 1] - vo;
     rng += (size_t)inst * GRID;
     saved += (size_t)inst * GRID;
-    buf += 64 * inst;
+    buf += NUCL_BUF * inst;
+    if (threadIdx.x == 0) stot = 0;
     int tid = blockIdx.x * NTHR + threadIdx.x;
     curandState s = rng[tid];
     saved[tid] = s;
@@ -63,36 +66,47 @@ __global__ void __launch_bounds__(NTHR) k_nucl_blocks(DevMesh m, curandState *rn
     for (int v = tid; v < nvi; v += GRID) n_alive += m.ven[vo + v] ? 1 : 0;
     for (int k = 0; k < 2 * n_alive; k++) (void)curand_uniform_double(&s);
     alive[threadIdx.x] = n_alive;
-    int rid = -1;
+    int rid = -1, rid_k = -1;   /* the pick and its rank among the stream's enabled vertices */
     if (n_alive > 0) {
         int n_steps = (int)(curand_uniform_double(&s) * (n_alive - 1));
         int k = 0;
         for (int v = tid; v < nvi; v += GRID)
             if (m.ven[vo + v]) {
-                if (k == n_steps) { rid = vo + v; break; }
+                if (k == n_steps) { rid = vo + v; rid_k = k; break; }
                 k++;
             }
     }
     pick[threadIdx.x] = rid;
+    nst[threadIdx.x] = rid_k;
+    __syncthreads();
+    atomicAdd(&stot, n_alive);                   /* integers: the same sum in any order */
+    __syncthreads();
+    const int tot = stot;
+    /* each thread's share alive[i] / tot, the quotient the selection below
+     * compares against (computed once per thread instead of one after
+     * another by thread 0) */
+    share[threadIdx.x] = tot > 0 ? alive[threadIdx.x] / (double)tot : 0.0;
     __syncthreads();
     if (threadIdx.x == 0) {
-        int tot = 0;
-        for (int i = 0; i < NTHR; i++) tot += alive[i];
         if (tot > 0) {
             double p = curand_uniform_double(&s);
             double pc = 0.0;
+            int kk = nst[0];
             for (int i = 0; i < NTHR; i++) {
-                if (pick[i] != -1 && pc <= p && p < (pc + (alive[i] / (double)tot))) {
+                if (pick[i] != -1 && pc <= p && p < (pc + share[i])) {
                     pick[0] = pick[i];
+                    kk = nst[i];
                     break;
                 }
-                pc += alive[i] / (double)tot;
+                pc += share[i];
             }
             buf[blockIdx.x] = pick[0];
             buf[NBLK + blockIdx.x] = tot;
+            buf[2 * NBLK + blockIdx.x] = kk;
         } else {
             buf[blockIdx.x] = -1;
             buf[NBLK + blockIdx.x] = 0;
+            buf[2 * NBLK + blockIdx.x] = -1;
         }
     }
     rng[tid] = s;
@@ -245,7 +259,7 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     int go = m.goff[inst], g_end = m.goff[inst + 1];
     rng += (size_t)inst * GRID;
     saved += (size_t)inst * GRID;
-    buf += 64 * inst;
+    buf += NUCL_BUF * inst;
     ctr += (size_t)inst * CTR_COUNT;
     int *nlist = m.nlist + go, *nnlist = m.nnlist + inst;
     int tot = 0;
@@ -253,10 +267,10 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     curandState s0 = rng[0];
     double p = curand_uniform_double(&s0);
     double pc = 0.0, pn = 0.0;
-    int cand = ctr[CTR_CANDIDATE];
+    int cand = ctr[CTR_CANDIDATE], kpick = -1;
     for (int i = 0; i < NBLK; i++) {
         pn = ((double)buf[NBLK + i]) / tot;
-        if (buf[i] != -1 && pc < p && p <= (pc + pn)) { cand = buf[i]; break; }
+        if (buf[i] != -1 && pc < p && p <= (pc + pn)) { cand = buf[i]; kpick = buf[2 * NBLK + i]; break; }
         pc += pn;
     }
     int v = cand;
@@ -268,9 +282,14 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
         return;
     }
     /* the two draws compute_nucleation_factor made for v: v is the k-th
-     * enabled vertex of stream ((v - vo) mod 8192) */
-    int t = (v - vo) % GRID, k = 0;
-    for (int u = vo + t; u < v; u += GRID) k += m.ven[u] ? 1 : 0;
+     * enabled vertex of stream ((v - vo) mod 8192); k_nucl_blocks recorded
+     * that rank with its pick (a candidate kept from an earlier attempt is
+     * counted here) */
+    int t = (v - vo) % GRID, k = kpick;
+    if (k < 0) {
+        k = 0;
+        for (int u = vo + t; u < v; u += GRID) k += m.ven[u] ? 1 : 0;
+    }
     curandState s = saved[t];
     for (int j = 0; j < 2 * k; j++) (void)curand_uniform_double(&s);
     double u1 = curand_uniform_double(&s);

@@ -159,15 +159,16 @@ def test_torch_function_gradients(gpu):
     assert np.isclose(float(gam.grad), ggam, rtol=1e-12) and np.isclose(float(mu.grad), gmu, rtol=1e-12)
 
 
-def nucleation_window(gpu, tmp_path, dt_window=1e-3, before=1, after=2):
+def nucleation_window(gpu, tmp_path, dt_window=1e-3, before=1, after=2, quiet=False):
     """The 300-grain fixture with its triangular stored energies (3..6;
     grains about one unit across, where the Metropolis test accepts
     nucleations), run at dt 4e-3 until 1/6 of the grains are gone (the gate
     for nucleation attempts), then at dt_window with one attempt per step
-    until an attempt is accepted.  Returns the options, the mesh and a
-    checkpoint `before` + 1 steps ahead of the accepted one: a window of
-    before + 1 + after steps from it moves the vertices, nucleates, and
-    moves them again."""
+    until an attempt is accepted with `before` steps ahead of it and
+    `after` steps behind it (quiet: none of them with a flip or a removal).
+    Returns the options, the mesh, a checkpoint at the window's start and
+    the window's length: it moves the vertices, nucleates, and moves them
+    again."""
     import os
     import configs
     import meshgen
@@ -192,79 +193,157 @@ def nucleation_window(gpu, tmp_path, dt_window=1e-3, before=1, after=2):
     o = opts(dt_window)
     e = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
     e.checkpoint_load(gate)
-    ring = [str(tmp_path / ("w%d.ckpt" % i)) for i in range(before + 2)]
-    for k in range(4000):
-        e.checkpoint_save(ring[k % len(ring)])
-        if e.step().n_nucleations > 0 and k > before:
+    R = before + after + 2
+    ring = [str(tmp_path / ("w%d.ckpt" % i)) for i in range(R)]
+    moves, nucl = [], []
+    for k in range(6000):
+        e.checkpoint_save(ring[k % R])
+        i = e.step()
+        moves.append(i.n_flips + i.n_removals + i.n_two_three)
+        nucl.append(i.n_nucleations)
+        c = k - after
+        if c - before >= 0 and nucl[c] > 0 and not (quiet and any(moves[c - before:k + 1])):
             e.close()
-            return o, mesh, ring[(k - before) % len(ring)], before + 1 + after
-    pytest.fail("no nucleation accepted within 4000 steps past the gate")
+            return o, mesh, ring[(c - before) % R], before + 1 + after
+    pytest.fail("no suitable nucleation within 6000 steps past the gate")
+
+
+def window_run(gpu, o, mesh, ckpt, window, se, gam, mu, every=None):
+    ee = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    ee.checkpoint_load(ckpt)
+    ee.set_stored_energy(se)
+    ee.set_gb_scaling(gam)
+    ee.set_mobility(mu)
+    if every:
+        ee.tape_start(every)
+    ev = []
+    for _ in range(window):
+        i = ee.step()
+        ev.append((i.n_flips, i.n_removals, i.n_two_three, i.n_nucleations,
+                   i.nucleation_candidate if i.nucleation_attempted else -2))
+    return ee, ee.area_histogram(NB, AMAX), ev
+
+
+def window_state(gpu, o, mesh, ckpt):
+    p = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    p.checkpoint_load(ckpt)
+    st = p.get_state()
+    p.close()
+    return st
 
 
 def test_adjoint_matches_central_differences_through_nucleation(gpu, tmp_path):
     """A window around an accepted nucleation (nucleation_window): the
-    adjoint follows the inserted triangle's position map (the new corners
-    A + 0.99 r u, r = 0.8 U |A - X*| + 0.1 with the replayed draw U) back to
-    the positions the step before moved.  Central differences of the GPU
+    adjoint follows the inserted triangle's position map back to the
+    positions the step before moved.  Five-point differences of the GPU
     forward over the same window (every run starts from the checkpoint; the
     perturbed runs are checked to take the same events, the nucleation site
-    included) agree within 1e-6 relative for the mobility, the boundary
-    energy scale and a direction in the stored energies of the original
-    grains (a nucleated grain's stored energy is 0, not a parameter).
-    The forward's finite-difference velocity carries rounding noise of
-    ~1e-8 relative, so a difference quotient over a few steps is only good
-    to ~1e-8/h; h is 1e-2..1e-3, where the loss is still quadratic in the
-    parameters to far better than 1e-6 over so short a window."""
+    included) agree within 2e-5 relative for the mobility, the boundary
+    energy scale and the stored energies of the original grains along the
+    gradient (a nucleated grain's stored energy is 0, not a parameter).
+    The loss compares the histogram with itself shifted by one bin, so its
+    gradient is no near-cancellation of bins.  The forward's
+    finite-difference velocity carries rounding noise of ~1e-8 relative, so
+    a difference quotient over a few steps is good to ~1e-8/h only: h is
+    3e-3..3e-2 (the exact check is the FP64 reference below)."""
     o, mesh, ckpt, window = nucleation_window(gpu, tmp_path)
-    probe = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
-    probe.checkpoint_load(ckpt)
-    st = probe.get_state()
-    probe.close()
-    n = len(st["gse"])
+    st = window_state(gpu, o, mesh, ckpt)
     se0 = st["gse"].copy()
     free = (st["gen"] > 0) & (st["gtype"] == 0)          # grains whose stored energy is a parameter
-
-    def run(se, gam, mu, every=None):
-        ee = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
-        ee.checkpoint_load(ckpt)
-        ee.set_stored_energy(se)
-        ee.set_gb_scaling(gam)
-        ee.set_mobility(mu)
-        if every:
-            ee.tape_start(every)
-        ev = []
-        for _ in range(window):
-            i = ee.step()
-            ev.append((i.n_flips, i.n_removals, i.n_two_three, i.n_nucleations,
-                       i.nucleation_candidate if i.nucleation_attempted else -2))
-        return ee, ee.area_histogram(NB, AMAX), ev
-
-    e, h, events = run(se0, 1.0, 1.0, every=2)
-    assert [x[3] for x in events][1] == 1 and sum(x[3] for x in events) >= 1, events
-    e2, target, _ = run(np.where(free, se0 * 1.05, se0), 1.05, 0.95)
-    e2.close()
+    run = lambda se, g, m, every=None: window_run(gpu, o, mesh, ckpt, window, se, g, m, every)
+    e0, h0, events = run(se0, 1.0, 1.0)
+    e0.close()
+    assert events[1][3] == 1, events
+    target = np.roll(h0, 1)
+    e, h, _ = run(se0, 1.0, 1.0, every=2)
     gse, ggam, gmu = e.adjoint_histogram(NB, AMAX, dloss(h, target))
     e.close()
-    dirn = np.where(free, np.random.default_rng(4).standard_normal(n), 0.0)
+    assert np.all(gse[~free] == 0.0)
+    dirn = np.where(free, gse, 0.0)
+    dirn /= np.linalg.norm(dirn)
     for which, adj in (("mu", gmu), ("gamma", ggam), ("se", float(gse @ dirn))):
         errs = []
-        for hstep in (1e-2, 3e-3, 1e-3):
-            out = []
-            for sgn in (1.0, -1.0):
+        for hstep in (3e-2, 1e-2, 3e-3):
+            f = {}
+            for k in (2, 1, -1, -2):
                 s_, g, m = se0.copy(), 1.0, 1.0
                 if which == "se":
-                    s_ = se0 + sgn * hstep * dirn
+                    s_ = se0 + k * hstep * dirn
                 elif which == "gamma":
-                    g += sgn * hstep
+                    g += k * hstep
                 else:
-                    m += sgn * hstep
+                    m += k * hstep
                 ee, hh, ev = run(s_, g, m)
                 ee.close()
                 if ev != events:
                     break
-                out.append(loss_of(hh, target))
-            if len(out) == 2:
-                fd = (out[0] - out[1]) / (2 * hstep)
+                f[k] = loss_of(hh, target)
+            if len(f) == 4:
+                fd = (-f[2] + 8 * f[1] - 8 * f[-1] + f[-2]) / (12 * hstep)
                 errs.append((abs(adj - fd) / abs(fd), hstep, fd))
         assert errs, "%s: every perturbed run changed the event sequence" % which
-        assert min(errs)[0] <= 1e-6, (which, adj, errs)
+        assert min(errs)[0] <= 2e-5, (which, adj, errs)
+
+
+def nucleation_record(gpu, o, mesh, ckpt, k):
+    """What the FP64 reference needs of the nucleation at window step k:
+    the vertices of the map and its factor k = 0.8 U, read from a copy of
+    the run whose mobility is 1e-300 for that step only (the step then
+    moves no vertex by a representable amount, so the new corners are where
+    the nucleation put them; the attempt itself does not depend on the
+    mobility), and the mesh right after it."""
+    e = gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    e.checkpoint_load(ckpt)
+    for _ in range(k):
+        e.step()
+    pre = e.get_state()
+    e.set_mobility(1e-300)
+    info = e.step()
+    post = e.get_state()
+    e.close()
+    assert info.n_nucleations == 1
+    D = o.domain_bound
+    wrap = lambda d: d - D * np.round(d / D)
+    g = int(np.nonzero((post["gen"] > 0) & (pre["gen"] == 0))[0][0])
+    A, B, C = (int(v) for v in post["glist"].reshape(-1, 100)[g, :3])
+    far = []
+    for j in range(3):
+        b = pre["vb"].reshape(-1, 3)[A, j]
+        far.append(int(pre["bend"][b] if pre["bini"][b] == A else pre["bini"][b]))
+    pa = np.array([pre["px"][A], pre["py"][A]])
+    AL = [np.hypot(*wrap(np.array([pre["px"][X], pre["py"][X]]) - pa)) for X in far]
+    imin = int(np.argmin(AL))
+    r = np.hypot(*wrap(np.array([post["px"][A], post["py"][A]]) - pa)) / 0.99
+    return {"A": A, "B": B, "C": C, "far": far, "xstar": far[imin], "k": (r - 0.1) / AL[imin], "state": post}
+
+
+def test_adjoint_matches_fp64_reference_through_nucleation(gpu, tmp_path):
+    """A window whose only topology changes are nucleations (no flip, no
+    removal; nucleation_window with quiet=True), against the FP64 torch
+    restatement of the same map (oracle/adjoint_ref.py: the velocity and
+    translation steps and the inserted triangle's position map with the
+    recorded draw), differentiated by torch.autograd: every gradient within
+    1e-6 relative, the same bound as the event-free window."""
+    pytest.importorskip("torch")
+    from oracle import adjoint_ref
+    o, mesh, ckpt, window = nucleation_window(gpu, tmp_path, dt_window=2.5e-4, before=1, after=2, quiet=True)
+    st = window_state(gpu, o, mesh, ckpt)
+    se0 = st["gse"].copy()
+    e, h, events = window_run(gpu, o, mesh, ckpt, window, se0, 1.0, 1.0, every=2)
+    assert all(ev[:3] == (0, 0, 0) for ev in events), events
+    nsteps = [k for k, ev in enumerate(events) if ev[3]]
+    assert 1 in nsteps, events
+    target = np.roll(h, 1)
+    gse, ggam, gmu = e.adjoint_histogram(NB, AMAX, dloss(h, target))
+    e.close()
+    recs = {k: nucleation_record(gpu, o, mesh, ckpt, k) for k in nsteps}
+    loss_r, gse_r, ggam_r, gmu_r, h_r = adjoint_ref.loss_and_grads_nucleation(
+        st, recs, se0, 1.0, 1.0, o.dt, window, o.domain_bound, NB, AMAX, target)
+    # the restated map rounds differently from the engine's (and k comes
+    # back from the corners' positions): last-bit differences that the
+    # finite-difference velocity (a quotient by 1e-8) turns into ~1e-10
+    # relative in the new grain's area
+    err = {"hist": float(np.max(np.abs(h - h_r) / np.maximum(np.abs(h_r), 1e-3))),
+           "se": float(np.abs(gse - gse_r).max() / np.abs(gse_r).max()),
+           "gamma": abs(ggam - ggam_r) / abs(ggam_r), "mu": abs(gmu - gmu_r) / abs(gmu_r)}
+    assert err["hist"] <= 1e-7 and max(err["se"], err["gamma"], err["mu"]) <= 1e-6, err
