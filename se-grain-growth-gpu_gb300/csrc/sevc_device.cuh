@@ -82,10 +82,6 @@ struct DevMesh {
      * else); the control block lives in device memory so that captured
      * launches stay valid whether or not events are recorded */
     struct EventLog *elog;
-    /* grains whose list changed since the step's grain pass (their area is
-     * recomputed after removals, src/main.cu:266) */
-    int *adirty, *nadirty;
-    uint8_t *gadirty;
     /* slots that ever held a nucleated grain, ascending; instance i's
      * entries start at nlist[goff[i]], nnlist[i] of them */
     int *nlist, *nnlist;

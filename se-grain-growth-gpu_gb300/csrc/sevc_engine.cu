@@ -184,6 +184,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&m.voff, (I + 1) * 4 }, { (void **)&m.boff, (I + 1) * 4 }, { (void **)&m.goff, (I + 1) * 4 },
         { (void **)&m.binst, B * 4 }, { (void **)&m.ginst, G * 4 }, { (void **)&m.pdone, I * 4 },
         { (void **)&x.pblock, I * h->p.n_blocks * 4 }, { (void **)&x.piters, I * 4 }, { (void **)&x.nrun, 4 },
+        { (void **)&x.pcnt, I * 4 },
         { (void **)&x.segcnt, I * TWO_THREE_PASSES * 4 }, { (void **)&x.nucl_on, I * 4 }, { (void **)&x.flags, 16 },
         { (void **)&x.summary, h->h_big_ints * 4 }, { (void **)&m.elog, sizeof(EventLog) },
         { (void **)&m.pos, V * 16 }, { (void **)&m.vel, V * 16 }, { (void **)&m.terms, V * 32 },
@@ -205,8 +206,7 @@ bool alloc_device(sevc_handle *h)
         { (void **)&x.block_area, I * h->p.n_blocks * 8 }, { (void **)&x.counters, I * CTR_COUNT * 4 },
         { (void **)&x.rng, nrng * sizeof(curandState) }, { (void **)&x.rng_saved, nrng * sizeof(curandState) },
         { (void **)&x.nucl_buf, I * 96 * 4 }, { (void **)&x.vbucket, 64 * 4 }, { (void **)&x.perm, G * 4 },
-        { (void **)&x.n_perm, 4 }, { (void **)&m.adirty, G * 4 }, { (void **)&m.nadirty, 4 }, { (void **)&m.gadirty, G },
-        { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
+        { (void **)&x.n_perm, 4 }, { (void **)&m.nlist, G * 4 }, { (void **)&m.nnlist, I * 4 }, { (void **)&m.pos0, V * 16 },
         { (void **)&m.vel0, V * 16 }, { (void **)&m.bv0, B * 8 }, { (void **)&m.vstamp, V * 4 },
         { (void **)&m.bstamp, B * 4 }, { (void **)&m.stamp, 4 }, { (void **)&m.bexact, B }, { (void **)&m.gexact, G },
         { (void **)&m.bmark, B }, { (void **)&m.lastblk, 8 * 4 },
@@ -568,7 +568,6 @@ void enqueue_tail(sevc_handle *h, int lists_unchanged)
     { Prof pr(h, "compact"); launch_compact(m, x, CK_GRAIN_CAND, x.list_c, x.n_c, s); }
     { Prof pr(h, "remove_grains"); launch_remove_grains(m, x, x.list_c, x.n_c, s); }              /* :259 */
     { Prof pr(h, "fix_lists"); launch_fix_lists(m, s); }                                          /* :262 */
-    { Prof pr(h, "grain_area"); launch_area_dirty(m, 1, s); }                                     /* :266 */
     /* The counts (:317-325) read only grain flags, types and areas, which
      * are final here (the flips and the list fix-up after them change
      * none): side0 computes them beside the flips, the fix-up and the

@@ -603,26 +603,6 @@ __global__ void k_grain_area(DevMesh m)
     m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
 }
 
-/* compute_grain_areas after the removals (src/main.cu:266): only grains
- * whose vertex list changed since the grain pass can have a new area (the
- * moved vertex of a removal belongs only to such grains); the others keep
- * the identical value the grain pass computed.  compute = 0 just drops
- * the list (marks made by the flips' fix-up after this point). */
-__global__ void k_area_dirty(DevMesh m, int compute)
-{
-    griddep_wait();
-    int n = *m.nadirty;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int g = m.adirty[i];
-        if (compute && m.gen[g]) {
-            double2 none = make_double2(0, 0);
-            m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
-        }
-        m.gadirty[g] = 0;
-    }
-    if (last_block(m.lastblk + 1) && threadIdx.x == 0) *m.nadirty = 0;   /* the list is consumed */
-}
-
 /* the step's summary in one buffer, for one readback: counters, events,
  * error bits, polling iterations, 2x3 pass counts (all per instance) and
  * the output decision */
@@ -782,10 +762,6 @@ void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const L
         launch_dep(k_text_label, (m.nb + 2 * t - 1) / (2 * t), t, s, m, dt, Df, hDf, inv_dt, dt_up, x.flags);
 }
 void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
-void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s)
-{
-    launch_dep(k_area_dirty, 152, TPB, s, m, compute);
-}
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { launch_dep(k_update, nblk(m.nv), TPB, s, m, dt); }
 
 void launch_pack_summary(const DevMesh &m, const DevScratch &x, int ninst, int *out, cudaStream_t s)

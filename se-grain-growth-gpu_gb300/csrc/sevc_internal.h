@@ -18,6 +18,7 @@ struct DevScratch {
     int *extra;                      /* dynamic insertions of the 2x3 pass, EXTRA_CAP per instance */
     int *threadfail;                 /* polling predicate: one flag per grid thread, per instance */
     int *pblock;                     /* polling predicate: one result per grid block, per instance */
+    int *pcnt;                       /* per instance: blocks of k_poll_final done (zero between launches) */
     int *piters;                     /* polling iterations this step, per instance */
     int *nrun;                       /* instances whose polling has not converged */
     int *segcnt;                     /* 2x3 count of each pass (20), per instance */
@@ -97,7 +98,6 @@ void launch_full_flag(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s);
 void launch_grain_area(const DevMesh &m, cudaStream_t s);
-void launch_area_dirty(const DevMesh &m, int compute, cudaStream_t s);
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s);
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s);
 /* counters | events | error bits | polling iterations | 2x3 counts | output decision, into out */
@@ -137,7 +137,7 @@ void launch_remove_grains(const DevMesh &m, const DevScratch &x, const int *list
 /* clears the candidate flag of every listed grain (after the removals) */
 void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncand, const DevScratch &x,
                   cudaStream_t s);
-void launch_fix_lists(const DevMesh &m, cudaStream_t s, bool queue_areas = true);
+void launch_fix_lists(const DevMesh &m, cudaStream_t s, bool areas = true);
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s);
 
 /* check_data on the device (sevc_check.cu): violations counted into *out */

@@ -267,10 +267,13 @@ __global__ void k_flag_scatter(DevMesh m, int n, const int *blockcnt, int *out, 
 /* ------------------------------------------------------------------ */
 /* polling system, src/topological.h:362-578                           */
 /* ------------------------------------------------------------------ */
-/* vertices_vote (:362) for the endpoints of listed boundaries */
-__global__ void k_poll_vote(DevMesh m, const int *list, const int *n)
+/* vertices_vote (:362) for the endpoints of listed boundaries; it also
+ * zeroes the iteration's count of unconverged instances (the previous
+ * iteration's was read before this kernel starts) */
+__global__ void k_poll_vote(DevMesh m, const int *list, const int *n, int *nrun)
 {
     griddep_wait();
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nrun = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < *n; i += gridDim.x * blockDim.x) {
     if (m.pdone[m.binst[list[i]]]) continue;
     int2 e = m.bv[list[i]];
@@ -369,13 +372,16 @@ __global__ void k_poll_compare_write16(DevMesh m, int *threadfail, int grid)
 /* part two, on the reference's grid (blockIdx.y = instance): per thread
  * AND over its stride set (already folded into threadfail), per block the
  * shared-memory tree whose bool += acts as OR (compare_candidates
- * :526-537) */
-__global__ void k_poll_final(DevMesh m, int *threadfail, int *pblock)
+ * :526-537); then, in the instance's last block to finish, the host's AND
+ * over blocks (:533-535): an instance whose blocks all passed has
+ * converged and takes no further iteration this step */
+__global__ void k_poll_final(DevMesh m, int *threadfail, int *pblock, int *pcnt, int *piters, int *nrun)
 {
     griddep_wait();
     __shared__ int t[256];
+    __shared__ int last;
     int inst = blockIdx.y;
-    if (m.pdone[inst]) return;
+    if (m.pdone[inst]) return;                       /* uniform over the instance's blocks */
     size_t tid = (size_t)inst * gridDim.x * blockDim.x + blockIdx.x * blockDim.x + threadIdx.x;
     t[threadIdx.x] = threadfail[tid] ? 0 : 1;
     threadfail[tid] = 0;
@@ -384,18 +390,18 @@ __global__ void k_poll_final(DevMesh m, int *threadfail, int *pblock)
         if ((int)threadIdx.x < i) t[threadIdx.x] = (t[threadIdx.x] || t[threadIdx.x + i]) ? 1 : 0;
         __syncthreads();
     }
-    if (threadIdx.x == 0) pblock[(size_t)inst * gridDim.x + blockIdx.x] = t[0];
-}
-/* then the host's AND over blocks (:533-535): an instance whose blocks all
- * passed has converged and takes no further iteration this step */
-__global__ void k_poll_status(DevMesh m, const int *pblock, int nblocks, int *piters, int *nrun)
-{
-    griddep_wait();
-    int inst = blockIdx.x * blockDim.x + threadIdx.x;
-    if (inst >= m.ninst || m.pdone[inst]) return;
+    if (threadIdx.x == 0) {
+        pblock[(size_t)inst * gridDim.x + blockIdx.x] = t[0];
+        __threadfence();
+        last = atomicAdd(pcnt + inst, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    pcnt[inst] = 0;
+    __threadfence();
     piters[inst]++;
     int ok = 1;
-    for (int i = 0; i < nblocks; i++) ok &= pblock[(size_t)inst * nblocks + i] != 0;
+    for (int i = 0; i < (int)gridDim.x; i++) ok &= __ldcg(pblock + (size_t)inst * gridDim.x + i) != 0;
     if (ok) m.pdone[inst] = 1;
     else atomicAdd(nrun, 1);
 }
@@ -1461,10 +1467,16 @@ __global__ void __launch_bounds__(FIX_TPB) k_fix_edit(DevMesh m)
 /* clear_grains_fix_state (:1150-1163): fix = false for enabled grains and
  * reset the mods of every vertex listed by an enabled grain.  Only queued
  * grains can have fix set and only marked vertices can hold mods.
- * queue_areas: the edited grains' areas are recomputed before the step's
- * counts (after the removals' fix-up; the flips' fix-up comes after the
- * counts, and the next step's grain pass computes every area). */
-__global__ void k_fix_clear(DevMesh m, int queue_areas)
+ *
+ * areas: compute_grain_areas after the removals (src/main.cu:266) for the
+ * grains this fix-up edited.  Only a grain whose list changed since the
+ * grain pass can have a new area (the vertex a 3-sided removal moves
+ * belongs only to grains that removal queues), and its list and vertices
+ * are final for the step here; a grain edited by several fix-ups (2x3
+ * passes, then the removals) is computed again by each, the last one on
+ * the final positions.  The flips' fix-up comes after the counts and needs
+ * none (the next step's grain pass computes every area). */
+__global__ void k_fix_clear(DevMesh m, int areas)
 {
     griddep_wait();
     int nf = min(*m.nfix, m.fixcap), nm = min(*m.nmod, m.modcap);
@@ -1472,10 +1484,9 @@ __global__ void k_fix_clear(DevMesh m, int queue_areas)
         int g = m.fixlist[w];
         if (m.gen[g]) {
             m.gfix[g] = 0;
-            if (queue_areas && !m.gadirty[g]) {   /* its area must be recomputed */
-                m.gadirty[g] = 1;
-                int i = atomicAdd(m.nadirty, 1);
-                if (i < m.ng) m.adirty[i] = g; else raise_err(m, ERRB_WORKLIST);
+            if (areas) {
+                double2 none = make_double2(0, 0);
+                m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
             }
         }
     }
@@ -1554,7 +1565,7 @@ void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *can
                            const StepParams &p, cudaStream_t s)
 {
     int g = listgrid(m.nb);
-    launch_dep(k_poll_vote, g, TPB, s, m, cand, ncand);
+    launch_dep(k_poll_vote, g, TPB, s, m, cand, ncand, x.nrun);
     launch_dep(k_poll_count, g, TPB, s, m, cand, ncand);
     launch_dep(k_poll_unlabel, g, TPB, s, m, cand, ncand);
     int grid = p.n_blocks * p.n_threads;
@@ -1565,9 +1576,8 @@ void launch_poll_iteration(const DevMesh &m, const DevScratch &x, const int *can
     } else {
         launch_dep(k_poll_compare_write, (m.nb + TPB - 1) / TPB, TPB, s, m, x.threadfail, grid);
     }
-    launch_dep(k_poll_final, dim3(p.n_blocks, p.ninst), p.n_threads, s, m, x.threadfail, x.pblock);
-    cudaMemsetAsync(x.nrun, 0, sizeof(int), s);
-    launch_dep(k_poll_status, (p.ninst + 127) / 128, 128, s, m, x.pblock, p.n_blocks, x.piters, x.nrun);
+    launch_dep(k_poll_final, dim3(p.n_blocks, p.ninst), p.n_threads, s, m, x.threadfail, x.pblock, x.pcnt, x.piters,
+               x.nrun);
 }
 
 void launch_conflicts(const DevMesh &m, const int *cand, const int *ncand, cudaStream_t s)
@@ -1633,10 +1643,10 @@ void launch_flips(const DevMesh &m, double eps, const int *cand, const int *ncan
     launch_dep(k_flip_deferred, m.ninst, FLIP_TPB, s, m, x, eps, cand, ncand);
 }
 
-void launch_fix_lists(const DevMesh &m, cudaStream_t s, bool queue_areas)
+void launch_fix_lists(const DevMesh &m, cudaStream_t s, bool areas)
 {
     launch_dep(k_fix_edit, WL_BLOCKS, FIX_TPB, s, m);
-    launch_dep(k_fix_clear, WL_BLOCKS, TPB, s, m, (int)queue_areas);
+    launch_dep(k_fix_clear, WL_BLOCKS, TPB, s, m, (int)areas);
 }
 
 void launch_fill_instance_ids(const DevMesh &m, cudaStream_t s)
