@@ -274,6 +274,9 @@ def run_calibration(n_inst=16, lo=2000, hi=5000, steps=200, iters=30, dt=2e-3, s
                          domain=float(np.sqrt(sizes.mean())), nucleation=nucleation)
 
 
+LAUNCH_MODES = {"graph": 1, "hostloops": 2, "direct": 0}
+
+
 def run_window(args):
     """The main workload's mesh at --grains, run to W steps past the 5/6
     nucleation gate and saved to --ckpt (or loaded from it when it exists),
@@ -287,8 +290,7 @@ def run_window(args):
     opt.domain_bound = float(n) ** 0.5
     eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
     made = False
-    if args.direct:
-        eng.set_graphs(False)
+    eng.set_graphs(LAUNCH_MODES[args.launch])
     if args.ckpt and os.path.exists(args.ckpt):
         eng.checkpoint_load(args.ckpt)
     else:
@@ -303,6 +305,12 @@ def run_window(args):
         if args.ckpt:
             eng.checkpoint_save(args.ckpt)
         made = True
+    if args.ckpt:
+        # three untimed steps (first launches load kernel code, graphs are
+        # captured), then the checkpoint again: the window is the same steps
+        for _ in range(3):
+            eng.step()
+        eng.checkpoint_load(args.ckpt)
     g0 = eng.grain_stats(-1)["n_grains"]
     ms, vs, g, ev = 0.0, 0, g0, [0, 0, 0]
     for _ in range(args.steps):
@@ -431,6 +439,7 @@ def run_engine(args):
     # ---------------- full run, end to end through the C ABI ----------------
     e0 = time.time()
     eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    eng.set_graphs(LAUNCH_MODES[args.launch])
     g, vs, ms_full, k = n, 0, 0.0, 0
     gate, ck_s, win_state, t0_ms, t0_vs = None, 0.0, None, 0.0, 0
     ev_full = np.zeros(5, np.int64)
@@ -461,6 +470,7 @@ def run_engine(args):
 
     # ---------------- the window past the gate, device-timed ----------------
     eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
+    eng.set_graphs(LAUNCH_MODES[args.launch])
     eng.checkpoint_load(ckpt)
     shapes = eng.autotune(3)          # launch shapes for this state; the state is left as it was
     for _ in range(W):                # graphs captured, caches warm
@@ -529,7 +539,9 @@ def run_engine(args):
                    "launch_shapes": {"tpb_vertex": shapes[0], "tpb_boundary": shapes[1], "wide_sides": shapes[2],
                                      "grain_blocks_per_sm": shapes[3],
                                      "picked_by": "sevc_autotune, 3 steps per candidate"},
-                   "launch_mode": "CUDA graphs"},
+                   "launch_mode": {"graph": "one CUDA graph per step (device-driven loops)",
+                                   "hostloops": "CUDA graphs of the step's fixed sequences, loops on the host",
+                                   "direct": "direct launches"}[args.launch]},
         "e2e": {"value": vs / e_wall, "unit": UNIT, "h2d_bytes_per_step": host_bytes / k,
                 "d2h_bytes_per_step": step_info_bytes + state_bytes / k,
                 "run": "the configuration's whole run through the C ABI: sevc_create_from_arrays from host arrays, "
@@ -645,8 +657,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--mesh-cache", default=None, help="npz file to reuse the generated mesh")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--direct", action="store_true",
-                    help="--workload window: launch every kernel directly (no CUDA graphs), for profilers")
+    ap.add_argument("--launch", default="graph", choices=["graph", "hostloops", "direct"],
+                    help="one graph per step (default), graphs with the loops on the host, or every kernel "
+                         "launched directly (for profilers)")
     ap.add_argument("--cal-dt", type=float, default=1e-4, help="--workload calibrate: time step")
     ap.add_argument("--ckpt", default=None, help="--workload window: checkpoint file past the gate (made if absent)")
     ap.add_argument("--workload", default="single", choices=["single", "ensemble", "calibrate", "small", "window"],

@@ -305,10 +305,12 @@ sevc_status sevc_set_exact_all(sevc_handle *h, int on);
  * or load a checkpoint.  No counterpart in the reference. */
 sevc_status sevc_set_limits(sevc_handle *h, int polling_cap, int worklist_cap);
 
-/* The fixed launch sequences of a step (its first half, one polling
- * iteration, the second half of a step without 2x3 pairs) are captured
- * into CUDA graphs on first use and replayed (on = 1, the default); on = 0
- * launches every kernel directly.  Results are identical either way.
+/* Launch mode.  on = 1 (the default): a step is one CUDA graph, captured
+ * on first use and replayed, whose polling and 2x3 loops are conditional
+ * nodes driven from the device; on = 2: the step's fixed launch sequences
+ * (its first half, one polling iteration, the second half of a step
+ * without 2x3 pairs) are graphs and the loops run on the host; on = 0
+ * launches every kernel directly.  Results are identical in every mode.
  * Profiling and adjoint replays always launch directly. */
 sevc_status sevc_set_graphs(sevc_handle *h, int on);
 

@@ -587,6 +587,21 @@ __device__ __forceinline__ int gintersect(int4 a, int4 b, int *out)
             }
     return k;
 }
+/* compute_boundaries_energies for boundary b (src/calculus.h:100-114):
+ * the energy of the misorientation between its two grains, times
+ * GB_scaling; isotropic boundaries take 1 * scaling without the
+ * transcendental (1 + 0.5 * 0 * (1 - cos^3) is exactly 1 for every finite
+ * cosine).  False (energy unset) when the ends share fewer than two
+ * grains. */
+__device__ __forceinline__ bool boundary_gamma(const DevMesh &m, int b, double eps, double scaling, double &gamma)
+{
+    if (eps == 0.0) { gamma = 1.0 * scaling; return true; }
+    int2 e = m.bv[b];
+    int gic[2];
+    if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) return false;
+    gamma = gb_energy(m.gori[gic[0]] - m.gori[gic[1]], eps) * scaling;
+    return true;
+}
 /* grains_union + grains_symdiff, src/geometry.h:863-898 */
 __device__ __forceinline__ void gsymdiff(int4 a, int4 b, int *out)
 {

@@ -29,6 +29,7 @@
 
 long long sevc_kernel_launches = 0;
 thread_local bool sevc_pdl_off = false;
+thread_local int sevc_pdl_skip = 0;
 
 struct ProfEntry { double ms = 0; int64_t launches = 0; };
 
@@ -479,9 +480,8 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     cudaMemsetAsync(m.evt, 0, I * EVT_COUNT * sizeof(int), s);
     cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
     cudaMemsetAsync(m.gexact, 0, (size_t)h->ng, s);
-    if (nucleation) {
-        { Prof pr(h, "boundary_geometry"); launch_boundary_geometry(m, o.GB_eps, o.GB_scaling, h->p.shape, s); } /* :124-130 */
-        { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }                           /* :144-168 */
+    if (nucleation) {   /* :124-130 for the attempt's vertex (k_nucl_finish), then :144-168 */
+        { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }
         if (h->tape.after_nucleation) h->tape.after_nucleation(s);
     }
     /* From here three branches that share no written data run concurrently
@@ -558,9 +558,9 @@ void enqueue_tail(sevc_handle *h, int lists_unchanged)
     DevMesh &m = h->m;
     DevScratch &x = h->x;
     if (lists_unchanged < 0) {                                                                    /* :252-255 */
-        sevc_pdl_off = true;     /* the first kernel after a conditional node */
+        sevc_pdl_skip = 1;       /* the first kernel after a conditional node */
         launch_label_3sided_auto(m, x, o.dt, s);
-        sevc_pdl_off = false;
+        sevc_pdl_skip = 0;
     } else {
         Prof pr(h, "label_3sided");
         launch_label_3sided(m, x, o.dt, lists_unchanged != 0, s);
@@ -597,8 +597,8 @@ void enqueue_post(sevc_handle *h)
  * handle's stream.  pre(handle) enqueues on that stream what runs just
  * before the node (it may set the condition); body(stream, handle)
  * enqueues the loop body onto the given stream, captured into the node's
- * body graph.  Launches in the body go without programmatic serialisation
- * (a body holds kernels, memsets and copies with plain dependencies). */
+ * body graph.  The body's first kernel goes without programmatic
+ * serialisation (nothing precedes it in the body); the others keep it. */
 template <class Pre, class Body>
 bool capture_while(sevc_handle *h, unsigned dflt, unsigned flags, Pre &&pre, Body &&body)
 {
@@ -628,9 +628,9 @@ bool capture_while(sevc_handle *h, unsigned dflt, unsigned flags, Pre &&pre, Bod
     bool ok = cuda_ok(cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
                       "body capture");
     if (ok) {
-        sevc_pdl_off = true;
+        sevc_pdl_skip = 1;       /* the body's first kernel has no kernel before it */
         body(bs, hnd);
-        sevc_pdl_off = false;
+        sevc_pdl_skip = 0;
         cudaGraph_t out = nullptr;
         ok = cuda_ok(cudaStreamEndCapture(bs, &out), "body capture");
     }
@@ -654,9 +654,9 @@ bool enqueue_step_graph(sevc_handle *h, bool nucleation)
                                 launch_poll_cond(m, x, hnd, h->polling_cap, bs);
                             });
     if (!ok) return false;
-    sevc_pdl_off = true;         /* the first kernels after a conditional node */
+    sevc_pdl_skip = 1;           /* the first kernel after a conditional node */
     launch_conflicts(m, x.list_a, x.n_a, s);                                                        /* :222-225 */
-    sevc_pdl_off = false;
+    sevc_pdl_skip = 0;
     ok = capture_while(h, 0u, 0u, [&](cudaGraphConditionalHandle hnd) { launch_tt_init(x, hnd, s); },  /* :227-250 */
                        [&](cudaStream_t bs, cudaGraphConditionalHandle hnd) {
                            launch_remove_two_three_dev(m, x, x.list_b, x.n_b, bs);
@@ -1315,9 +1315,10 @@ sevc_status sevc_set_limits(sevc_handle *h, int polling_cap, int worklist_cap)
 
 sevc_status sevc_set_graphs(sevc_handle *h, int on)
 {
-    if (!h) return SEVC_ERR_ARG;
+    if (!h || on < 0 || on > 2) return SEVC_ERR_ARG;
     h->use_graphs = on != 0;
-    if (!on) drop_graphs(h);
+    h->device_loops = on == 1;
+    drop_graphs(h);
     return SEVC_OK;
 }
 

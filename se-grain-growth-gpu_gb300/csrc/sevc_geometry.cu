@@ -31,15 +31,7 @@ __global__ void k_boundary_geometry(DevMesh m, double eps, double scaling)
     double2 a = m.pos[e.x], c = m.pos[e.y];
     m.blen[b] = arclen(a, c, m.D);
     double gamma;
-    if (eps == 0.0) {
-        /* 1 + 0.5*0*(1 - cos^3) is exactly 1 for every finite cosine */
-        gamma = 1.0 * scaling;
-    } else {
-        int gic[2];
-        if (gintersect(m.vg[e.x], m.vg[e.y], gic) < 2) { raise_err(m, ERRB_TOPOLOGY); return; }
-        double d_alpha = m.gori[gic[0]] - m.gori[gic[1]];
-        gamma = gb_energy(d_alpha, eps) * scaling;
-    }
+    if (!boundary_gamma(m, b, eps, scaling, gamma)) { raise_err(m, ERRB_TOPOLOGY); return; }
     m.benergy[b] = gamma;
 }
 
@@ -320,7 +312,11 @@ __global__ void __launch_bounds__(32 * WIDE_WARPS) k_grain_fd_wide(DevMesh m, co
 /* counting sort of the enabled grains by side count (16 buckets, the last
  * one for 15 or more sides) */
 constexpr int NBUCKET = 16;
-__global__ void k_vlen_hist(DevMesh m, int *cnt)
+/* Side-count histogram of the enabled grains into cnt[0..15]; the last
+ * block to finish turns it into cursor[16..31] (bucket starts, advanced by
+ * the scatter), start[32..47] and count[48..63] (kept for later passes
+ * over one bucket) and leaves cnt[0..15] zero for the next step. */
+__global__ void k_vlen_hist(DevMesh m, int *cnt, int *cursor, int *total)
 {
     __shared__ int h[NBUCKET];
     if (threadIdx.x < NBUCKET) h[threadIdx.x] = 0;
@@ -329,18 +325,16 @@ __global__ void k_vlen_hist(DevMesh m, int *cnt)
     if (g < m.ng && m.gen[g]) atomicAdd(&h[min(m.gvlen[g], NBUCKET - 1)], 1);
     __syncthreads();
     if (threadIdx.x < NBUCKET && h[threadIdx.x]) atomicAdd(&cnt[threadIdx.x], h[threadIdx.x]);
-}
-/* cnt[0..15] -> cursor[16..31] (bucket starts, advanced by the scatter),
- * start[32..47] and count[48..63] kept for later passes over one bucket */
-__global__ void k_vlen_offsets(int *cnt, int *cursor, int *total)
-{
-    if (threadIdx.x == 0) {
+    bool last = last_block(m.lastblk + 1);
+    if (last && threadIdx.x == 0) {
+        __threadfence();
         int acc = 0;
         for (int b = 0; b < NBUCKET; b++) {
+            int c = __ldcg(cnt + b);
             cursor[b] = acc;
             cnt[2 * NBUCKET + b] = acc;
-            cnt[3 * NBUCKET + b] = cnt[b];
-            acc += cnt[b];
+            cnt[3 * NBUCKET + b] = c;
+            acc += c;
             cnt[b] = 0;
         }
         *total = acc;
@@ -712,8 +706,7 @@ void launch_boundary_geometry(const DevMesh &m, double eps, double scaling, cons
 }
 void launch_grain_sort(const DevMesh &m, const DevScratch &x, cudaStream_t s)
 {
-    COUNT_LAUNCHES(1), k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket);
-    COUNT_LAUNCHES(1), k_vlen_offsets<<<1, 32, 0, s>>>(x.vbucket, x.vbucket + NBUCKET, x.n_perm);
+    COUNT_LAUNCHES(1), k_vlen_hist<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket, x.vbucket + NBUCKET, x.n_perm);
     COUNT_LAUNCHES(1), k_vlen_scatter<<<nblk(m.ng), TPB, 0, s>>>(m, x.vbucket + NBUCKET, x.perm);
 }
 void launch_grain_fd_wide(const DevMesh &m, const DevScratch &x, const LaunchShape &sh, cudaStream_t s)

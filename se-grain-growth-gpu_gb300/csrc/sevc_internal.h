@@ -182,10 +182,13 @@ void launch_grain_stats(const DevMesh &m, int lo, int hi, double *out, cudaStrea
 
 /* kernels launched by this process (reported per step) */
 extern long long sevc_kernel_launches;
-/* set while the body of a conditional graph node, or the first kernels
- * after one, are captured: launches then go without the
- * programmatic-serialisation attribute */
+/* set while launches must go without the programmatic-serialisation
+ * attribute (a whole stretch of capture); sevc_pdl_skip counts the next
+ * launches that must (the first kernel of a conditional node's body and
+ * the first kernel after a conditional node, whose predecessor is not a
+ * kernel) */
 extern thread_local bool sevc_pdl_off;
+extern thread_local int sevc_pdl_skip;
 #define COUNT_LAUNCHES(k) (sevc_kernel_launches += (k))
 
 /* Launch with programmatic dependent launch allowed: the grid may be
@@ -206,7 +209,9 @@ inline void launch_dep(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s, A
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cfg.attrs = at;
-    cfg.numAttrs = sevc_pdl_off ? 0 : 1;
+    bool plain = sevc_pdl_off || sevc_pdl_skip > 0;
+    if (sevc_pdl_skip > 0) sevc_pdl_skip--;
+    cfg.numAttrs = plain ? 0 : 1;
     COUNT_LAUNCHES(1);
     cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(args)...);
 }

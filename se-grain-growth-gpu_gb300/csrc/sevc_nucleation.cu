@@ -134,7 +134,7 @@ __device__ double area3(double2 a, double2 b, double2 c, double D)
 
 /* generate_grain_for_nucleation, src/nucleation2.cu:116-212 */
 __device__ int gen_triangle(const DevMesh &m, int A, double nucl_r, double nucl_ori, double eps, double scaling,
-                            bool do_scale, NuclGeo &o)
+                            bool do_scale, const double *gam3, NuclGeo &o)
 {
     double D = m.D;
     int4 sa = m.vb[A];
@@ -174,7 +174,7 @@ __device__ int gen_triangle(const DevMesh &m, int A, double nucl_r, double nucl_
     double A3 = area3(pa, o.Bpos, o.Cpos, D);
     double E0 = 0.0, E1 = 0.0;
     for (int i = 0; i < 3; i++) {
-        double gam = m.benergy[slot3(sa, i)];
+        double gam = gam3[i];   /* the energy of A's i-th boundary this step */
         if (do_scale) E0 += 0.99 * nucl_r * gam;
         else E0 += nucl_r * gam;
     }
@@ -294,16 +294,32 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     for (int j = 0; j < 2 * k; j++) (void)curand_uniform_double(&s);
     double u1 = curand_uniform_double(&s);
     double u2 = curand_uniform_double(&s);
+    /* the arclengths and energies of v's boundaries this step
+     * (compute_boundaries_lengths / _energies, src/main.cu:124-130, run on
+     * every boundary before the attempt in the reference; only v's three
+     * are read, so they are computed here, with the same arithmetic as
+     * the step's boundary pass that follows) */
     int4 sb = m.vb[v];
-    double AL[3] = { m.blen[sb.x], m.blen[sb.y], m.blen[sb.z] };
+    double AL[3], gam3[3];
+    for (int i = 0; i < 3; i++) {
+        int b = slot3(sb, i);
+        int2 e = m.bv[b];
+        AL[i] = arclen(m.pos[e.x], m.pos[e.y], m.D);
+        if (!boundary_gamma(m, b, eps, scaling, gam3[i])) {
+            raise_err(m, ERRB_TOPOLOGY);
+            ctr[CTR_CANDIDATE] = -1;
+            rng[0] = s0;
+            return;
+        }
+    }
     double mn = AL[0];
     int imin = 0;
     for (int i = 0; i < 3; i++) if (mn > AL[i]) { mn = AL[i]; imin = i; }   /* min(), src/geometry.h:116 */
     double nucl_r = 0.8 * mn * u1 + 0.1;
     double nucl_ori = 2 * M_PI * u2;
     NuclGeo o0, o1;
-    if (gen_triangle(m, v, nucl_r, nucl_ori, eps, scaling, false, o0) ||
-        gen_triangle(m, v, nucl_r, nucl_ori, eps, scaling, true, o1)) {
+    if (gen_triangle(m, v, nucl_r, nucl_ori, eps, scaling, false, gam3, o0) ||
+        gen_triangle(m, v, nucl_r, nucl_ori, eps, scaling, true, gam3, o1)) {
         raise_err(m, ERRB_TOPOLOGY);
         ctr[CTR_CANDIDATE] = -1;
         rng[0] = s0;
@@ -336,7 +352,7 @@ __global__ void k_nucl_finish(DevMesh m, curandState *rng, const curandState *sa
     /* the reference passes (scaling, eps) swapped here; only the unused
      * energy changes */
     NuclGeo o;
-    if (gen_triangle(m, A, nucl_r, nucl_ori, scaling, eps, true, o)) { raise_err(m, ERRB_TOPOLOGY); return; }
+    if (gen_triangle(m, A, nucl_r, nucl_ori, scaling, eps, true, gam3, o)) { raise_err(m, ERRB_TOPOLOGY); return; }
     {   /* the triangle's position map, for an adjoint replay */
         EventRec r0, r1;
         r0.type = EV_NUCL; r0.a = A; r0.b = B; r0.c = C;

@@ -480,7 +480,7 @@ class Engine:
 
     def set_graphs(self, on):
         lib().sevc_set_graphs.argtypes = [C.c_void_p, C.c_int]
-        _check(lib().sevc_set_graphs(self._h, 1 if on else 0))
+        _check(lib().sevc_set_graphs(self._h, int(on) if not isinstance(on, bool) else (1 if on else 0)))
 
     def set_profiling(self, on):
         _check(lib().sevc_set_profiling(self._h, 1 if on else 0))

@@ -227,12 +227,13 @@ def test_state_digest_matches_its_definition(gpu, oracle_mod, tmp_path):
 def test_whole_step_graph_equals_host_loops(gpu, tmp_path, grid):
     """A step replayed as one CUDA graph, whose polling and 2x3 loops are
     conditional nodes the device drives, equals the step launched kernel by
-    kernel with the loops on the host: every summary field and every state
+    kernel with the loops on the host, and the step's fixed sequences as
+    graphs with the loops on the host: every summary field and every state
     digest, through 2x3 pairs, conflicts and (on a 1 x 1 grid, where the
     convergence predicate covers every boundary) multi-iteration polling."""
     ini = configs.write_ini(os.path.join(str(tmp_path), "e.ini"), "events_m1000", os.path.join(str(tmp_path), "o"))
     engines = []
-    for on in (True, False):
+    for on in (1, 0, 2):
         o = gpu.load_ini(ini)
         o.min_grains = 10
         o.n_blocks, o.n_threads = grid
@@ -241,13 +242,13 @@ def test_whole_step_graph_equals_host_loops(gpu, tmp_path, grid):
         engines.append(e)
     seen = {"tt": 0, "poll2": 0, "conf": 0}
     for k in range(300):
-        a, b = engines[0].step(), engines[1].step()
-        da, db = a.as_dict(), b.as_dict()
+        a, b, c = (e.step() for e in engines)
+        da, db, dc = a.as_dict(), b.as_dict(), c.as_dict()
         for key in ("gpu_ms", "kernel_launches"):
-            da.pop(key)
-            db.pop(key)
-        assert da == db, (k, da, db)
-        assert engines[0].state_digest() == engines[1].state_digest(), k
+            for d in (da, db, dc):
+                d.pop(key)
+        assert da == db == dc, (k, da, db, dc)
+        assert engines[0].state_digest() == engines[1].state_digest() == engines[2].state_digest(), k
         seen["tt"] += a.n_two_three
         seen["poll2"] += a.polling_iters >= 2
         seen["conf"] += a.n_conflicts
