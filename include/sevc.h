@@ -124,8 +124,12 @@ sevc_status sevc_load_mesh_host(const sevc_options *opt, sevc_mesh_host *out, in
  * fix-ups, position update, grain count and nucleated area; then n++ and
  * t = n*dt.  `info` (may be NULL) describes the step that ran. */
 sevc_status sevc_step(sevc_handle *h, sevc_step_info *info);
-/* Run `nsteps` iterations back to back without per-step host reads of the
- * step counters (stops early on the stop criterion).  `done` = steps run. */
+/* Run up to `nsteps` iterations, as many calls of sevc_step would: it
+ * stops early after a step whose keep_going is 0 (the reference's loop
+ * condition, src/main.cu:120) or that fails.  `done` = steps run, `last`
+ * (may be NULL) the last step's info.  Each step's stop test needs that
+ * step's grain count, so the steps are not pipelined: every step reads its
+ * summary back before the next is launched. */
 sevc_status sevc_run_steps(sevc_handle *h, int nsteps, int *done, sevc_step_info *last);
 /* Loop condition of src/main.cu:120 for the current state. */
 int sevc_should_continue(const sevc_handle *h);
