@@ -131,6 +131,18 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info);
  * step's grain count, so the steps are not pipelined: every step reads its
  * summary back before the next is launched. */
 sevc_status sevc_run_steps(sevc_handle *h, int nsteps, int *done, sevc_step_info *last);
+/* Run `nsteps` iterations (fewer only on a failure) and write each step's
+ * info to infos[k] (may be NULL); `done` = steps run.  It does not stop at
+ * the reference's stop criterion: the caller reads keep_going and the
+ * counts from `infos`.  With one graph per step (sevc_set_graphs(h, 1), the
+ * default), no profiling or tape, and no grain-count stop (min_grains <= 0,
+ * or a batch), the steps are pipelined: each step is launched while the one
+ * before it runs and its summary is read back afterwards, so the GPU does
+ * not wait on the host between steps (an attempt step waits for the step
+ * before it until every instance has passed the 5/6 gate, whose count it
+ * needs); otherwise it steps as sevc_step does.  Results are those of
+ * nsteps calls of sevc_step. */
+sevc_status sevc_run(sevc_handle *h, int nsteps, sevc_step_info *infos, int *done);
 /* Loop condition of src/main.cu:120 for the current state. */
 int sevc_should_continue(const sevc_handle *h);
 

@@ -108,6 +108,15 @@ struct sevc_handle {
     bool use_graphs = true;
     bool force_direct = false;   /* this step launches directly (an adjoint replay records inside it) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    /* sevc_run keeps two steps in flight, each with its own pinned upload
+     * and readback buffers and its events (allocated on first use) */
+    struct RunSlot {
+        int *big = nullptr, *on = nullptr, *flags = nullptr;
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr, done = nullptr;
+        sevc_step_info loc;
+        long long launches = 0;
+    } rslot[2];
+    bool rslot_ready = false;
     /* side streams of the step (branches that do not depend on each other
      * run concurrently; captured as graph branches) and the fork / join
      * events between them: 0-5 in the first half, 6-7 in the tail */
@@ -684,6 +693,108 @@ sevc_status err_bits_to_status(int bits)
 /* ================================================================== */
 /* C ABI                                                               */
 /* ================================================================== */
+namespace {
+/* bytes of the packed step summary (k_pack_summary's layout) */
+size_t summary_bytes(const sevc_handle *h)
+{
+    size_t I = h->ninst;
+    return (I * CTR_COUNT + I * EVT_COUNT + 4 + I + I * TWO_THREE_PASSES + 1) * sizeof(int);
+}
+/* The step's summary (hb: counters, events, error bits, polling
+ * iterations and 2x3 counts of every instance; h_on: the instances that
+ * attempted a nucleation) into the run state and `info`; then n++ and
+ * t = n dt (src/main.cu:388-391).  loc carries n, t and the attempt flag of
+ * the step. */
+sevc_status finish_step(sevc_handle *h, const int *hb, const int *h_on, bool whole, float ms, int launches,
+                        sevc_step_info loc, sevc_step_info *info)
+{
+    const sevc_options &o = h->opt;
+    const int I = h->ninst;
+    const bool batch = I > 1;
+    const int mg = o.min_grains;
+    const size_t o_evt = (size_t)I * CTR_COUNT, o_err = o_evt + (size_t)I * EVT_COUNT, o_pit = o_err + 4,
+                 o_seg = o_pit + I, o_full = o_seg + (size_t)I * TWO_THREE_PASSES;
+    const int full = hb[o_full] != 0;
+    loc.outputs_complete = full;
+    h->outputs_complete = full;
+    int total = 0;
+    double area_sum = 0;
+    for (int i = 0; i < I; i++) {
+        const int *ctr = hb + (size_t)i * CTR_COUNT, *ev = hb + o_evt + (size_t)i * EVT_COUNT;
+        double na;
+        memcpy(&na, ctr + CTR_NUCL_AREA_SLOT, sizeof(double));
+        h->icurr[i] = ctr[CTR_NGRAINS];
+        h->iarea[i] = na;
+        total += h->icurr[i];
+        area_sum += na;
+        sevc_step_info &ii = h->iinfo[i];
+        memset(&ii, 0, sizeof ii);
+        ii.n = loc.n;
+        ii.t = loc.t;
+        ii.curr_n_grains = h->icurr[i];
+        ii.nucleated_area = na;
+        ii.polling_iters = hb[o_pit + i];
+        for (int k = 0; k < TWO_THREE_PASSES; k++) {
+            int c = hb[o_seg + (size_t)k * I + i];
+            ii.two_three_counts[k] = c;
+            ii.n_two_three_iters = k + 1;
+            if (c == 0) break;
+        }
+        ii.n_two_three = ev[EVT_TWO_THREE];
+        ii.n_removals = ev[EVT_REMOVALS];
+        ii.n_flips = ev[EVT_FLIPS];
+        ii.n_nucleations = ev[EVT_NUCLEATIONS];
+        ii.n_conflicts = ev[EVT_CONFLICTS];
+        ii.nucleation_attempted = h_on[i];
+        /* reported in the instance's own vertex indices */
+        ii.nucleation_candidate = (h_on[i] && ctr[CTR_CANDIDATE] >= 0) ? ctr[CTR_CANDIDATE] - h->voff[i] : -1;
+        ii.gpu_ms = ms;
+        ii.outputs_complete = full;
+        ii.kernel_launches = launches;
+        ii.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (h->icurr[i] <= mg && mg > 0); /* :328 */
+        loc.n_two_three += ii.n_two_three;
+        loc.n_removals += ii.n_removals;
+        loc.n_flips += ii.n_flips;
+        loc.n_nucleations += ii.n_nucleations;
+        loc.n_conflicts += ii.n_conflicts;
+    }
+    if (whole) {        /* the loops' counts, as the host loops report them */
+        loc.polling_iters = 0;
+        for (int i = 0; i < I; i++) loc.polling_iters = std::max(loc.polling_iters, h->iinfo[i].polling_iters);
+        for (int k = 0; k < TWO_THREE_PASSES; k++) {
+            int c = 0;
+            for (int i = 0; i < I; i++) c += hb[o_seg + (size_t)k * I + i];
+            loc.two_three_counts[k] = c;
+            loc.n_two_three_iters = k + 1;
+            if (c == 0) break;
+        }
+    }
+    h->curr_n_grains = total;
+    h->nucleated_area = batch ? area_sum / I : area_sum;
+    loc.curr_n_grains = total;
+    loc.nucleated_area = h->nucleated_area;
+    loc.nucleation_candidate = (!batch && loc.nucleation_attempted) ? h->iinfo[0].nucleation_candidate : -1;
+    loc.gpu_ms = ms;
+    loc.kernel_launches = launches;
+    loc.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (!batch && h->curr_n_grains <= mg && mg > 0);
+    h->n++;                                                                                         /* :388-389 */
+    h->t = h->n * o.dt;
+    for (int i = 0; i < I; i++) {
+        int cont = ((h->t <= o.tmax && o.tmax > 0) || (h->n <= o.nmax && o.nmax > 0)) && (h->icurr[i] >= mg && mg > 0);
+        h->iinfo[i].keep_going = (h->icurr[i] <= mg && mg > 0) ? 0 : cont;                          /* :391 */
+    }
+    loc.keep_going = batch ? sevc_should_continue(h) : h->iinfo[0].keep_going;
+    if (info) *info = loc;
+    sevc_status st = err_bits_to_status(hb[o_err]);
+    if (!st && h->tape.every > 0 && !h->tape.replaying) {
+        h->tape.nsteps++;
+        if (h->tape.nsteps % h->tape.every == 0 && !tape_checkpoint(h)) return SEVC_ERR_CUDA;
+    }
+    return st;
+}
+
+} // namespace
+
 extern "C" {
 
 sevc_status sevc_create(const sevc_options *opt, sevc_handle **out)
@@ -823,6 +934,14 @@ void sevc_destroy(sevc_handle *h)
     if (h->h_big) cudaFreeHost(h->h_big);
     if (h->h_on) cudaFreeHost(h->h_on);
     if (h->h_flags) cudaFreeHost(h->h_flags);
+    for (auto &sl : h->rslot) {
+        if (sl.big) cudaFreeHost(sl.big);
+        if (sl.on) cudaFreeHost(sl.on);
+        if (sl.flags) cudaFreeHost(sl.flags);
+        if (sl.ev0) cudaEventDestroy(sl.ev0);
+        if (sl.ev1) cudaEventDestroy(sl.ev1);
+        if (sl.done) cudaEventDestroy(sl.done);
+    }
     tape_free(h);
     drop_graphs(h);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -930,91 +1049,115 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info)
     /* one readback: counters, events, error bits, polling iterations and
      * 2x3 counts of every instance */
     int *hb = h->h_big;
-    const size_t o_evt = (size_t)I * CTR_COUNT, o_err = o_evt + (size_t)I * EVT_COUNT, o_pit = o_err + 4,
-                 o_seg = o_pit + I, o_full = o_seg + (size_t)I * TWO_THREE_PASSES;
-    if (!cuda_ok(cudaMemcpyAsync(hb, x.summary, (o_full + 1) * sizeof(int), cudaMemcpyDeviceToHost, s), "readback") ||
+    if (!cuda_ok(cudaMemcpyAsync(hb, x.summary, summary_bytes(h), cudaMemcpyDeviceToHost, s), "readback") ||
         !cuda_ok(cudaStreamSynchronize(s), "readback sync"))
         return SEVC_ERR_CUDA;
-    const int full = hb[o_full] != 0;
-    loc.outputs_complete = full;
-    h->outputs_complete = full;
     float ms = 0;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     if (h->profiling) prof_collect(h);
     int launches = (int)(sevc_kernel_launches - launches0);
-    int total = 0;
-    double area_sum = 0;
-    for (int i = 0; i < I; i++) {
-        const int *ctr = hb + (size_t)i * CTR_COUNT, *ev = hb + o_evt + (size_t)i * EVT_COUNT;
-        double na;
-        memcpy(&na, ctr + CTR_NUCL_AREA_SLOT, sizeof(double));
-        h->icurr[i] = ctr[CTR_NGRAINS];
-        h->iarea[i] = na;
-        total += h->icurr[i];
-        area_sum += na;
-        sevc_step_info &ii = h->iinfo[i];
-        memset(&ii, 0, sizeof ii);
-        ii.n = loc.n;
-        ii.t = loc.t;
-        ii.curr_n_grains = h->icurr[i];
-        ii.nucleated_area = na;
-        ii.polling_iters = hb[o_pit + i];
-        for (int k = 0; k < TWO_THREE_PASSES; k++) {
-            int c = hb[o_seg + (size_t)k * I + i];
-            ii.two_three_counts[k] = c;
-            ii.n_two_three_iters = k + 1;
-            if (c == 0) break;
+    return finish_step(h, hb, h->h_on, whole, ms, launches, loc, info);
+}
+
+sevc_status sevc_run(sevc_handle *h, int nsteps, sevc_step_info *infos, int *done)
+{
+    if (!h || nsteps < 0) return SEVC_ERR_ARG;
+    if (done) *done = 0;
+    const sevc_options &o = h->opt;
+    const int I = h->ninst;
+    const bool batch = I > 1;
+    const int mg = o.min_grains;
+    /* pipelined: one graph per step, nothing read inside a step, and no
+     * input of a step that depends on the previous step's counts (a single
+     * mesh with a grain-count stop feeds its count to the output decision) */
+    const bool pipe = graphs_on(h) && h->device_loops && !h->profiling && h->tape.every <= 0 && (batch || mg <= 0);
+    if (!pipe) {
+        for (int k = 0; k < nsteps; k++) {
+            sevc_step_info inf;
+            sevc_status st = sevc_step(h, &inf);
+            if (infos) infos[k] = inf;
+            if (done) *done = k + 1;
+            if (st) return st;
         }
-        ii.n_two_three = ev[EVT_TWO_THREE];
-        ii.n_removals = ev[EVT_REMOVALS];
-        ii.n_flips = ev[EVT_FLIPS];
-        ii.n_nucleations = ev[EVT_NUCLEATIONS];
-        ii.n_conflicts = ev[EVT_CONFLICTS];
-        ii.nucleation_attempted = h->h_on[i];
-        /* reported in the instance's own vertex indices */
-        ii.nucleation_candidate = (h->h_on[i] && ctr[CTR_CANDIDATE] >= 0) ? ctr[CTR_CANDIDATE] - h->voff[i] : -1;
-        ii.gpu_ms = ms;
-        ii.outputs_complete = full;
-        ii.kernel_launches = launches;
-        ii.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (h->icurr[i] <= mg && mg > 0); /* :328 */
-        loc.n_two_three += ii.n_two_three;
-        loc.n_removals += ii.n_removals;
-        loc.n_flips += ii.n_flips;
-        loc.n_nucleations += ii.n_nucleations;
-        loc.n_conflicts += ii.n_conflicts;
+        return SEVC_OK;
     }
-    if (whole) {        /* the loops' counts, as the host loops report them */
-        loc.polling_iters = 0;
-        for (int i = 0; i < I; i++) loc.polling_iters = std::max(loc.polling_iters, h->iinfo[i].polling_iters);
-        for (int k = 0; k < TWO_THREE_PASSES; k++) {
-            int c = 0;
-            for (int i = 0; i < I; i++) c += hb[o_seg + (size_t)k * I + i];
-            loc.two_three_counts[k] = c;
-            loc.n_two_three_iters = k + 1;
-            if (c == 0) break;
+    cudaStream_t s = h->stream;
+    DevScratch &x = h->x;
+    if (!h->rslot_ready) {
+        for (auto &sl : h->rslot)
+            if (!cuda_ok(cudaMallocHost(&sl.big, h->h_big_ints * sizeof(int)), "pinned") ||
+                !cuda_ok(cudaMallocHost(&sl.on, I * sizeof(int)), "pinned") ||
+                !cuda_ok(cudaMallocHost(&sl.flags, 4 * sizeof(int)), "pinned") || !cuda_ok(cudaEventCreate(&sl.ev0), "event") ||
+                !cuda_ok(cudaEventCreate(&sl.ev1), "event") ||
+                !cuda_ok(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming), "event"))
+                return SEVC_ERR_CUDA;
+        h->rslot_ready = true;
+    }
+    int launched = 0, finished = 0;
+    sevc_status st = SEVC_OK;
+    auto finish_one = [&]() -> sevc_status {
+        sevc_handle::RunSlot &sl = h->rslot[finished % 2];
+        if (!cuda_ok(cudaEventSynchronize(sl.done), "readback sync")) return SEVC_ERR_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, sl.ev0, sl.ev1);
+        sevc_step_info inf;
+        sevc_status r = finish_step(h, sl.big, sl.on, true, ms, (int)sl.launches, sl.loc, &inf);
+        if (infos) infos[finished] = inf;
+        finished++;
+        if (done) *done = finished;
+        return r;
+    };
+    /* step `launched` goes in while the one before it runs; what it needs
+     * of the host is known in advance (its index, hence its snapshot and
+     * attempt decisions) except whether an instance has just passed the
+     * 5/6 gate (src/main.cu:137-139), so an attempt step waits for the step
+     * before it unless every instance has already passed */
+    while (finished < nsteps && !st) {
+        bool can_launch = launched < nsteps && launched - finished < 2;
+        const int nk = h->n + (launched - finished);
+        const bool attempt = o.do_nucleation && o.nucleation_gap > 0 && (nk % o.nucleation_gap) == 0;
+        if (can_launch && attempt && launched > finished)
+            for (int i = 0; i < I; i++) can_launch = can_launch && h->iallow[i];
+        if (!can_launch) {
+            st = finish_one();
+            continue;
         }
+        sevc_handle::RunSlot &sl = h->rslot[launched % 2];
+        memset(&sl.loc, 0, sizeof sl.loc);
+        sl.loc.n = nk;
+        sl.loc.t = nk * o.dt;
+        int n_on = 0;                                                                              /* :137-141 */
+        for (int i = 0; i < I; i++) {
+            if (h->icurr[i] <= 5 * h->ng0[i] / 6) h->iallow[i] = 1;
+            sl.on[i] = attempt && h->iallow[i];
+            n_on += sl.on[i];
+        }
+        sl.loc.nucleation_attempted = n_on > 0;
+        sl.flags[1] = h->exact_all || o.dt >= 100 || (o.snap_gap > 0 && nk % o.snap_gap == 0);
+        sl.flags[2] = batch ? 0 : mg;
+        sl.flags[3] = h->curr_n_grains;   /* read only when min_grains > 0: not here */
+        if ((n_on && !cuda_ok(cudaMemcpyAsync(x.nucl_on, sl.on, I * sizeof(int), cudaMemcpyHostToDevice, s), "upload")) ||
+            !cuda_ok(cudaMemcpyAsync(x.flags + 1, sl.flags + 1, 3 * sizeof(int), cudaMemcpyHostToDevice, s), "upload")) {
+            st = SEVC_ERR_CUDA;
+            break;
+        }
+        cudaEventRecord(sl.ev0, s);
+        long long k0 = sevc_kernel_launches;
+        bool cap_ok = true;
+        if (!run_seq(h, h->g_step[n_on ? 1 : 0], [&] { cap_ok = enqueue_step_graph(h, n_on > 0); }) || !cap_ok) {
+            st = SEVC_ERR_CUDA;
+            break;
+        }
+        sl.launches = sevc_kernel_launches - k0;
+        cudaEventRecord(sl.ev1, s);
+        if (!cuda_ok(cudaMemcpyAsync(sl.big, x.summary, summary_bytes(h), cudaMemcpyDeviceToHost, s), "readback") ||
+            !cuda_ok(cudaEventRecord(sl.done, s), "event")) {
+            st = SEVC_ERR_CUDA;
+            break;
+        }
+        launched++;
     }
-    h->curr_n_grains = total;
-    h->nucleated_area = batch ? area_sum / I : area_sum;
-    loc.curr_n_grains = total;
-    loc.nucleated_area = h->nucleated_area;
-    loc.nucleation_candidate = (!batch && loc.nucleation_attempted) ? h->iinfo[0].nucleation_candidate : -1;
-    loc.gpu_ms = ms;
-    loc.kernel_launches = launches;
-    loc.export_due = (o.snap_gap > 0 && h->n % o.snap_gap == 0) || (!batch && h->curr_n_grains <= mg && mg > 0);
-    h->n++;                                                                                         /* :388-389 */
-    h->t = h->n * o.dt;
-    for (int i = 0; i < I; i++) {
-        int cont = ((h->t <= o.tmax && o.tmax > 0) || (h->n <= o.nmax && o.nmax > 0)) && (h->icurr[i] >= mg && mg > 0);
-        h->iinfo[i].keep_going = (h->icurr[i] <= mg && mg > 0) ? 0 : cont;                          /* :391 */
-    }
-    loc.keep_going = batch ? sevc_should_continue(h) : h->iinfo[0].keep_going;
-    if (info) *info = loc;
-    sevc_status st = err_bits_to_status(hb[o_err]);
-    if (!st && h->tape.every > 0 && !h->tape.replaying) {
-        h->tape.nsteps++;
-        if (h->tape.nsteps % h->tape.every == 0 && !tape_checkpoint(h)) return SEVC_ERR_CUDA;
-    }
+    if (launched > finished) cudaStreamSynchronize(s);   /* after a failure: let the step in flight end */
     return st;
 }
 

@@ -18,7 +18,7 @@ STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "CAPACITY", 4: "NONCONVERGED", 5: "TO
 
 # every symbol include/sevc.h declares
 EXPORTS = ["sevc_default_options", "sevc_load_ini", "sevc_create", "sevc_create_from_arrays", "sevc_destroy", "sevc_load_mesh_host",
-           "sevc_step", "sevc_run_steps", "sevc_should_continue", "sevc_export_text", "sevc_get_state",
+           "sevc_step", "sevc_run_steps", "sevc_run", "sevc_should_continue", "sevc_export_text", "sevc_get_state",
            "sevc_mesh_sizes", "sevc_check_data", "sevc_run_program", "sevc_rng_record", "sevc_set_profiling",
            "sevc_get_profile", "sevc_last_error", "sevc_set_exact_all", "sevc_rng_record_noalloc",
            "sevc_create_batch", "sevc_instance_count", "sevc_instance_ranges", "sevc_instance_info",
@@ -108,6 +108,7 @@ def lib():
         L.sevc_destroy.restype = None
         L.sevc_step.argtypes = [H, C.POINTER(StepInfo)]
         L.sevc_run_steps.argtypes = [H, C.c_int, C.POINTER(C.c_int), C.POINTER(StepInfo)]
+        L.sevc_run.argtypes = [H, C.c_int, C.POINTER(StepInfo), C.POINTER(C.c_int)]
         L.sevc_should_continue.argtypes = [H]
         L.sevc_export_text.argtypes = [H, C.c_char_p, C.c_double]
         L.sevc_get_state.argtypes = [H, C.POINTER(MeshHost)]
@@ -367,6 +368,16 @@ class Engine:
         info = StepInfo()
         _check(lib().sevc_step(self._h, C.byref(info)))
         return info
+
+    def run(self, n):
+        """n steps (sevc_run: pipelined when the handle allows it); the list
+        of their StepInfo"""
+        infos = (StepInfo * max(n, 1))()
+        done = C.c_int(0)
+        rc = lib().sevc_run(self._h, n, infos, C.byref(done))
+        out = [infos[k] for k in range(done.value)]
+        _check(rc)
+        return out
 
     def run_steps(self, n):
         info, done = StepInfo(), C.c_int()

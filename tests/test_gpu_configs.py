@@ -259,3 +259,51 @@ def test_whole_step_graph_equals_host_loops(gpu, tmp_path, grid):
         assert seen["poll2"] > 0, seen
     for e in engines:
         e.close()
+
+
+def _nucleating_engines(gpu, count, batch):
+    """`count` engines over the 300-grain fixture with its triangular
+    stored energies (grains one unit across, one Metropolis attempt every 3
+    steps past the 5/6 gate, no grain-count stop); batch: three copies of it
+    as one batched handle"""
+    import meshgen
+    d = os.path.join(configs.MESH_DIR, "m300")
+    mesh = meshgen.read_files(*[os.path.join(d, f) for f in ("vertices.txt", "ridges.txt", "oris.txt",
+                                                              "se_triangular.txt")])
+    dt = 4e-3
+    o = gpu.default_options(n_grains=300, dt=dt, dtau=3 * dt, domain_bound=17.0, GB_eps=0.0, GB_scaling=1.0,
+                            SE_eps=1.0, SE_min=999.0, SE_max=999.0, do_nucleation=1, MC_k=3.0, nmax=10 ** 8,
+                            tmax=-1, snap_gap=10 ** 8, n_blocks=32, n_threads=256)
+    o.min_grains = -1
+    if batch:   # meshes of different sizes pass their gates at different steps
+        meshes = [mesh] + [meshgen.make_inputs(n, 60 + n, se="triangular", generator="c") for n in (260, 330)]
+        return [gpu.Engine.from_batch(o, meshes) for _ in range(count)]
+    return [gpu.Engine.from_arrays(o, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"]) for _ in range(count)]
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_pipelined_run_equals_single_steps(gpu, batch):
+    """sevc_run launches each step while the one before it runs and reads
+    the summaries back afterwards; through the 5/6 gate (where an attempt
+    step must wait for the count of the step before it) and the attempts
+    after it, every step's summary equals the one sevc_step gives (timing
+    aside) and so does the state digest at the end."""
+    a, b = _nucleating_engines(gpu, 2, batch)
+    ref, gate = [], None
+    while gate is None or len(ref) < gate + 60:
+        ref.append(b.step().as_dict())
+        if gate is None and ref[-1]["nucleation_attempted"]:
+            gate = len(ref)
+        assert len(ref) < 5000, "the gate was not reached"
+    got = []
+    while len(got) < len(ref):
+        got += [i.as_dict() for i in a.run(min(37, len(ref) - len(got)))]
+    for k, (x, y) in enumerate(zip(got, ref)):
+        for key in ("gpu_ms", "kernel_launches"):
+            x.pop(key)
+            y.pop(key)
+        assert x == y, (k, x, y)
+    assert sum(r["nucleation_attempted"] for r in ref) >= 10
+    assert a.state_digest() == b.state_digest()
+    a.close()
+    b.close()
