@@ -121,7 +121,7 @@ struct sevc_handle {
      * run concurrently; captured as graph branches) and the fork / join
      * events between them: 0-5 in the first half, 6-7 in the tail */
     cudaStream_t side[3] = { nullptr, nullptr, nullptr };   /* [2]: capture of loop bodies */
-    cudaEvent_t evfork[8] = {};
+    cudaEvent_t evfork[10] = {};
     bool profiling = false;
     std::map<std::string, ProfEntry> prof;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -359,7 +359,7 @@ sevc_status create_from_host(const sevc_options *opt, sevc_hmesh *hm, sevc_handl
     bool streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
     for (int k = 0; streams_ok && k < 3; k++)
         streams_ok = cuda_ok(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking), "stream");
-    for (int k = 0; streams_ok && k < 8; k++)
+    for (int k = 0; streams_ok && k < 10; k++)
         streams_ok = cuda_ok(cudaEventCreateWithFlags(&h->evfork[k], cudaEventDisableTiming), "event");
     if (!streams_ok || !cuda_ok(cudaMallocHost(&h->h_ctr, 256), "pinned") ||
         !cuda_ok(cudaMallocHost(&h->h_big, h->h_big_ints * sizeof(int)), "pinned") ||
@@ -588,10 +588,24 @@ void enqueue_tail(sevc_handle *h, int lists_unchanged)
         cudaEventRecord(h->evfork[7], h->side[0]);
     }
     { Prof pr(h, "flips"); launch_flips(m, o.GB_eps, x.list_a, x.n_a, x, s); }             /* :282, :289 */
-    { Prof pr(h, "fix_lists"); launch_fix_lists(m, s, false); }                                   /* :294 */
-    { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                                /* :314 */
-    if (h->profiling) { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }
-    else cudaStreamWaitEvent(s, h->evfork[7], 0);
+    if (h->profiling) {
+        { Prof pr(h, "fix_lists"); launch_fix_lists(m, s, false); }                               /* :294 */
+        { Prof pr(h, "update"); launch_update_positions(m, o.dt, s); }                            /* :314 */
+        { Prof pr(h, "counts"); launch_counts(m, x, h->p, s); }
+    } else {
+        /* the position update reads positions and velocities, final once
+         * the flips are applied; the fix-up after them edits only lists
+         * and mods: side1 updates beside it */
+        cudaEventRecord(h->evfork[8], s);
+        cudaStreamWaitEvent(h->side[1], h->evfork[8], 0);
+        sevc_pdl_skip = 1;
+        launch_update_positions(m, o.dt, h->side[1]);                                             /* :314 */
+        sevc_pdl_skip = 0;
+        cudaEventRecord(h->evfork[9], h->side[1]);
+        launch_fix_lists(m, s, false);                                                            /* :294 */
+        cudaStreamWaitEvent(s, h->evfork[9], 0);
+        cudaStreamWaitEvent(s, h->evfork[7], 0);
+    }
     launch_pack_summary(m, x, h->ninst, x.summary, s);
 }
 
