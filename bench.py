@@ -483,7 +483,7 @@ def run_engine(args):
     eng = sevc.Engine.from_arrays(opt, mesh["xy"], mesh["ridges"], mesh["oris"], mesh["se"])
     eng.set_graphs(LAUNCH_MODES[args.launch])
     eng.checkpoint_load(ckpt)
-    shapes = eng.autotune(3)          # launch shapes for this state; the state is left as it was
+    shapes = eng.autotune(10)         # launch shapes for this state (10 steps per candidate); the state is left as it was
     for _ in range(W):                # graphs captured, caches warm
         eng.step()
     eng.checkpoint_load(ckpt)
@@ -549,7 +549,7 @@ def run_engine(args):
                    "mesh_generation_s": round(gen_s, 1), "wall_s": round(wall, 3),
                    "launch_shapes": {"tpb_vertex": shapes[0], "tpb_boundary": shapes[1], "wide_sides": shapes[2],
                                      "grain_blocks_per_sm": shapes[3],
-                                     "picked_by": "sevc_autotune, 3 steps per candidate"},
+                                     "picked_by": "sevc_autotune, 10 steps per candidate"},
                    "launch_mode": {"graph": "one CUDA graph per step (device-driven loops)",
                                    "hostloops": "CUDA graphs of the step's fixed sequences, loops on the host",
                                    "direct": "direct launches"}[args.launch]},

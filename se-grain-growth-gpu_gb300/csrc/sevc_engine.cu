@@ -485,10 +485,10 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
     DevMesh &m = h->m;
     DevScratch &x = h->x;
     size_t I = h->ninst;
-    cudaMemsetAsync(m.err, 0, 16, s);
-    cudaMemsetAsync(m.evt, 0, I * EVT_COUNT * sizeof(int), s);
-    cudaMemsetAsync(x.segcnt, 0, I * TWO_THREE_PASSES * sizeof(int), s);
-    cudaMemsetAsync(m.gexact, 0, (size_t)h->ng, s);
+    /* the per-step records (event counts, error bits, 2x3 pass counts,
+     * polling state, dA/dt exactness marks) are zero here: the previous
+     * step's summary kernel cleared them as it read them (a new handle's
+     * block starts zeroed, and checkpoints are taken between steps) */
     if (nucleation) {   /* :124-130 for the attempt's vertex (k_nucl_finish), then :144-168 */
         { Prof pr(h, "nucleation"); launch_nucleation(m, x, h->p, s); }
         if (h->tape.after_nucleation) h->tape.after_nucleation(s);
@@ -546,8 +546,6 @@ void enqueue_pre(sevc_handle *h, bool nucleation)
         launch_compact(m, x, CK_CAND, x.list_a, x.n_a, s);
         cudaStreamWaitEvent(s, ev[5], 0);
     }
-    cudaMemsetAsync(m.pdone, 0, I * sizeof(int), s);                                               /* :219 */
-    cudaMemsetAsync(x.piters, 0, I * sizeof(int), s);
 }
 
 void enqueue_poll(sevc_handle *h)
@@ -670,7 +668,6 @@ bool enqueue_step_graph(sevc_handle *h, bool nucleation)
     DevMesh &m = h->m;
     DevScratch &x = h->x;
     enqueue_pre(h, nucleation);
-    cudaMemsetAsync(x.ptot, 0, sizeof(int), s);
     bool ok = capture_while(h, 1u, cudaGraphCondAssignDefault, [](cudaGraphConditionalHandle) {},   /* :219 */
                             [&](cudaStream_t bs, cudaGraphConditionalHandle hnd) {
                                 launch_poll_iteration(m, x, x.list_a, x.n_a, h->p, bs);

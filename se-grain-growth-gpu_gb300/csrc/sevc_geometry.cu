@@ -600,23 +600,33 @@ __global__ void k_grain_area(DevMesh m)
 /* the step's summary in one buffer, for one readback: counters, events,
  * error bits, polling iterations, 2x3 pass counts (all per instance) and
  * the output decision */
+/* The step's summary in one buffer; each per-step record it packs (event
+ * counts, error bits, polling iterations and convergence, 2x3 pass counts)
+ * is zeroed once read, and so are the exactness marks of the grains' dA/dt
+ * and the polling iteration total, so the next step starts from zeros
+ * without resets of its own (the reset each step would otherwise begin
+ * with: src/main.cu's per-step clears of these values). */
 __global__ void k_pack_summary(DevMesh m, DevScratch x, int ninst, int *out)
 {
     griddep_wait();
     size_t nc = (size_t)ninst * CTR_COUNT, ne = (size_t)ninst * EVT_COUNT, np = ninst,
            ns = (size_t)ninst * TWO_THREE_PASSES;
     size_t total = nc + ne + 4 + np + ns + 1;
-    for (size_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (size_t i = t0; i < total; i += stride) {
         size_t k = i;
         int v;
         if (k < nc) v = x.counters[k];
-        else if ((k -= nc) < ne) v = m.evt[k];
-        else if ((k -= ne) < 4) v = m.err[k];
-        else if ((k -= 4) < np) v = x.piters[k];
-        else if ((k -= np) < ns) v = x.segcnt[k];
-        else v = x.flags[0];
+        else if ((k -= nc) < ne) { v = m.evt[k]; m.evt[k] = 0; }
+        else if ((k -= ne) < 4) { v = m.err[k]; m.err[k] = 0; }
+        else if ((k -= 4) < np) { v = x.piters[k]; x.piters[k] = 0; m.pdone[k] = 0; }
+        else if ((k -= np) < ns) { v = x.segcnt[k]; x.segcnt[k] = 0; }
+        else { v = x.flags[0]; *x.ptot = 0; }
         out[i] = v;
     }
+    const size_t nw = (size_t)m.ng / 16;                   /* gexact as 16-byte words (256-byte aligned array) */
+    for (size_t i = t0; i < nw; i += stride) reinterpret_cast<uint4 *>(m.gexact)[i] = make_uint4(0, 0, 0, 0);
+    for (size_t i = 16 * nw + t0; i < (size_t)m.ng; i += stride) m.gexact[i] = 0;
 }
 __global__ void k_reset_ngrains(int *counters, int ninst)
 {
