@@ -389,8 +389,10 @@ KERNEL_BYTES = {
     # per vertex: pos 16 + slots 32 + 3 boundary ends 24 + 3 neighbour positions 48 (shared) +
     # gamma/length 48 + terms in 48 + grain q 24 + vel/terms/energy out 56
     "vertex_fd": ("vertices", 16 + 32 + 24 + 24 + 48 + 48 + 24 + 56),
-    # per boundary: ends 8 + positions 32 + velocities 32 + t_ext 8 + flags 2
-    "text_label": ("boundaries", 8 + 32 + 32 + 8 + 2),
+    # per boundary decided by the speed bound (nearly all): enabled 1 + ends 8 + arclength 8 +
+    # the ends' speed bounds 8, then t_ext 8, exact flag 1, candidate 1, conflict 4 written
+    # (the few others also read both ends' positions and velocities, 64)
+    "text_label": ("boundaries", 1 + 8 + 8 + 8 + 8 + 1 + 1 + 4),
 }
 
 # DRAM bytes (read + write) per unit measured by ncu for each kernel phase on
