@@ -370,33 +370,6 @@ __global__ void k_vlen_scatter(DevMesh m, int *cursor, int *perm)
     if (b >= 0) perm[base[b] + r] = g;
 }
 
-/* grain pass of the finite-difference velocity, see file comment;
- * also compute_grain_areas (src/calculus.h:224) and the per-grain part of
- * vertex_compute_energy (src/geometry.h:476). */
-__global__ void k_grain_fd(DevMesh m)
-{
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= m.ng || !m.gen[g]) return;
-    const int *L = m.glist + (size_t)SEVC_MAXV * g;
-    int n = m.gvlen[g];
-    double2 none = make_double2(0, 0);
-    double A = area_stream(L, n, m.pos, -1, none, m.D);
-    m.garea[g] = A;
-    double se = m.gse[g];
-    m.gq[g] = se * A / n;
-    double absA = fabs(A);
-    for (int p = 0; p < n; p++) {
-        int v = L[p];
-        double2 q = m.pos[v];
-        double2 px = make_double2(dmod(q.x + SEVC_GRAD_EPS_D, m.D), dmod(q.y, m.D));
-        double2 py = make_double2(dmod(q.x, m.D), dmod(q.y + SEVC_GRAD_EPS_D, m.D));
-        double Ax = area_stream(L, n, m.pos, p, px, m.D);
-        double Ay = area_stream(L, n, m.pos, p, py, m.D);
-        int4 sg = m.vg[v];
-        int j = sg.x == g ? 0 : (sg.y == g ? 1 : (sg.z == g ? 2 : -1));
-        if (j >= 0) m.contrib[3 * v + j] = make_double2(se * (fabs(Ax) - absA), se * (fabs(Ay) - absA));
-    }
-}
 
 /* vertex pass: src/calculus.h:19-73 (boundary part) and :143-154;
  * vertex_compute_energy src/geometry.h:472-479.
@@ -588,14 +561,6 @@ __global__ void k_text_label(DevMesh m, double dt, float Df, float hDf, float in
     }
 }
 
-/* compute_grain_areas, src/calculus.h:224 */
-__global__ void k_grain_area(DevMesh m)
-{
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= m.ng || !m.gen[g]) return;
-    double2 none = make_double2(0, 0);
-    m.garea[g] = area_stream(m.glist + (size_t)SEVC_MAXV * g, m.gvlen[g], m.pos, -1, none, m.D);
-}
 
 /* the step's summary in one buffer, for one readback: counters, events,
  * error bits, polling iterations, 2x3 pass counts (all per instance) and
@@ -735,8 +700,6 @@ void launch_grain_fd_sorted(const DevMesh &m, const DevScratch &x, const LaunchS
     else COUNT_LAUNCHES(1), k_grain_fd_sorted<4><<<g, 128, 0, s>>>(m, x.perm, x.vbucket, sh.wide_sides);
 }
 
-/* the unsorted per-grain pass, kept for A/B timing */
-void launch_grain_fd_unsorted(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_fd<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_vertex_fd(const DevMesh &m, double mu, bool unit_gamma, const LaunchShape &sh, cudaStream_t s)
 {
     int t = sh.tpb_vertex;
@@ -764,7 +727,6 @@ void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const L
     if (m.nb > 0)
         launch_dep(k_text_label, (m.nb + 2 * t - 1) / (2 * t), t, s, m, dt, Df, hDf, inv_dt, dt_up, x.flags);
 }
-void launch_grain_area(const DevMesh &m, cudaStream_t s) { COUNT_LAUNCHES(1), k_grain_area<<<nblk(m.ng), TPB, 0, s>>>(m); }
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s) { launch_dep(k_update, nblk(m.nv), TPB, s, m, dt); }
 
 void launch_pack_summary(const DevMesh &m, const DevScratch &x, int ninst, int *out, cudaStream_t s)

@@ -97,7 +97,6 @@ void launch_vertex_fd(const DevMesh &m, double mu, bool unit_gamma, const Launch
 void launch_full_flag(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_grain_dadt(const DevMesh &m, const DevScratch &x, cudaStream_t s);
 void launch_text_label(const DevMesh &m, const DevScratch &x, double dt, const LaunchShape &sh, cudaStream_t s);
-void launch_grain_area(const DevMesh &m, cudaStream_t s);
 void launch_update_positions(const DevMesh &m, double dt, cudaStream_t s);
 void launch_counts(const DevMesh &m, const DevScratch &x, const StepParams &p, cudaStream_t s);
 /* counters | events | error bits | polling iterations | 2x3 counts | output decision, into out */
