@@ -817,6 +817,8 @@ __device__ __forceinline__ bool valid_v(const DevMesh &m, int v) { return (unsig
 __device__ __forceinline__ bool valid_b(const DevMesh &m, int b) { return (unsigned)b < (unsigned)m.nb; }
 __device__ __forceinline__ bool valid_g(const DevMesh &m, int g) { return (unsigned)g < (unsigned)m.ng; }
 
+/* bring a record into this SM's L1 (no register result, no wait) */
+__device__ __forceinline__ void l1_touch(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 /* An event's warp reserves its vertices and the boundaries in their slots
  * (lane 3j + k: vertex j, slot k) and settles the dA/dt of every grain
  * around them, one grain per lane (a grain an earlier lane also sees is
@@ -855,12 +857,25 @@ __device__ void reserve_warp(const DevMesh &m, const DevScratch &x, const int *v
         int hq = __shfl_sync(0xffffffffu, h, q);
         if (q < lane && hq == h) first = false;
     }
+    /* settling walks the grain's list with three dependent loads per
+     * vertex: the lanes first bring their grains' lists and vertex records
+     * into L1, every load of a list issued at once */
+    if (first && !m.gexact[h]) {
+        const int *L = m.glist + (size_t)SEVC_MAXV * h;
+        int n = m.gvlen[h];
+        n = n < SEVC_MAXV ? n : SEVC_MAXV;
+#pragma unroll 4
+        for (int k = 0; k < n; k++) {
+            int v = L[k];
+            if (valid_v(m, v)) { l1_touch(m.pos + v); l1_touch(m.vel + v); l1_touch(m.vstamp + v); }
+        }
+    }
+    __syncwarp();
     if (first) finalize_grain(m, h);
 }
 /* the records an event's single-thread code reads, brought into L1 by
  * the warp in two parallel rounds: the vertices' own records, then the
  * boundaries in their slots and the grains around them */
-__device__ __forceinline__ void l1_touch(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 __device__ void prefetch_event(const DevMesh &m, const int *verts, int nverts, int lane)
 {
     int j = lane / 3, k = lane - 3 * j;
