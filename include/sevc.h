@@ -131,9 +131,10 @@ sevc_status sevc_step(sevc_handle *h, sevc_step_info *info);
  * step's grain count, so the steps are not pipelined: every step reads its
  * summary back before the next is launched. */
 sevc_status sevc_run_steps(sevc_handle *h, int nsteps, int *done, sevc_step_info *last);
-/* Run `nsteps` iterations (fewer only on a failure) and write each step's
- * info to infos[k] (may be NULL); `done` = steps run.  It does not stop at
- * the reference's stop criterion: the caller reads keep_going and the
+/* Run `nsteps` iterations of the loop body src/main.cu:120-394 (fewer only
+ * on a failure) and write each step's info to infos[k] (may be NULL);
+ * `done` = steps run.  It does not stop at the reference's stop criterion
+ * (src/main.cu:120, :391): the caller reads keep_going and the
  * counts from `infos`.  With one graph per step (sevc_set_graphs(h, 1), the
  * default), no profiling or tape, and no grain-count stop (min_grains <= 0,
  * or a batch), the steps are pipelined: each step is launched while the one
